@@ -1,0 +1,197 @@
+/*
+ * horender — GB300 renderer for curved high-order (spectral/hp) hexahedral
+ * meshes and their modal scalar fields.
+ *
+ * C ABI. Plain pointers and sizes, int status codes, no exceptions across the
+ * boundary, caller-owned output buffers. One CUDA stream per context; a
+ * context is not thread-safe. Every call returns HO_OK (0) or a negative
+ * HO_ERR_* code; ho_last_error() gives the message of the last failure.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the reference project root).
+ */
+#ifndef HORENDER_H
+#define HORENDER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HO_OK 0
+#define HO_ERR_ARG (-1)      /* bad argument (null pointer, bad size)            */
+#define HO_ERR_CUDA (-2)     /* a CUDA call failed                               */
+#define HO_ERR_STATE (-3)    /* call out of order (e.g. render before build)     */
+#define HO_ERR_IO (-4)       /* file could not be read or written               */
+#define HO_ERR_PARSE (-5)    /* malformed XML / FLD input                       */
+#define HO_ERR_NOMEM (-6)    /* device or host allocation failed                */
+#define HO_ERR_RANGE (-7)    /* size beyond a documented limit                  */
+#define HO_ERR_DEVICE (-8)   /* a kernel reported an internal error status      */
+
+/* Solver modes (ho_set_mode). */
+#define HO_MODE_PLAIN 0      /* reference algorithm: cold-start Newton, 17-sample iso scan */
+#define HO_MODE_LEARNED 1    /* MLP initial guess + bracket, plain fallback and judge     */
+#define HO_MODE_BATCHED 2    /* element-binned wavefront, one persistent launch           */
+
+/* Hit kinds. */
+#define HO_HIT_MISS 0
+#define HO_HIT_FACE 1
+#define HO_HIT_ISO 2
+
+/* ho_hit.flags bits. */
+#define HO_FLAG_FALLBACK 1u      /* learned guess rejected, plain solver answered   */
+#define HO_FLAG_FP64_FAIL 2u     /* FP64 residual check above tolerance             */
+#define HO_FLAG_OVERFLOW 4u      /* candidate list restarted (more than K boxes)     */
+
+typedef struct ho_context ho_context;
+
+/* One ray-query result (48 bytes). kind: HO_HIT_*; elem: element index
+ * (-1 on miss); face: 0..5 for boundary-face hits (face table of
+ * FEM-AABB/high_order.h:164-184), -1 otherwise; xi: reference coordinates of
+ * the hit; n: unit normal facing the ray; u: field value at xi; iters: Newton
+ * iterations (inverse map + face) this query spent. */
+typedef struct {
+  float t;
+  int32_t elem;
+  int16_t face;
+  int16_t kind;
+  float xi[3];
+  float n[3];
+  float u;
+  uint32_t flags;
+  uint32_t iters;
+} ho_hit;
+
+/* Pinhole camera as FEM-AABB/raytracer.h:31-48 (aperture 0: primary rays go
+ * through pixel centres, no jitter). vfov in degrees; focus_dist <= 0 means
+ * |lookfrom - lookat|. */
+typedef struct {
+  float lookfrom[3];
+  float lookat[3];
+  float vup[3];
+  float vfov_deg;
+  float focus_dist;
+} ho_camera;
+
+/* Seeded synthetic scene: an nx*ny*nz grid of hexes over [0,1]^3, GLL
+ * geometry nodes displaced by curve_amp*h*sin(2 pi x)sin(2 pi y)sin(2 pi z)
+ * (the same scalar added to x, y and z), a field of n_gauss Gaussians
+ * (centres U[0,1]^3, sigma U[0.1,0.3], amplitude U[-1,1]) interpolated at
+ * the GLL nodes; both fitted to Modified-A modal coefficients in FP64 and
+ * stored as FP32. Per-element order P is drawn uniformly from
+ * [order_min, order_max] (modes n = P + 1). */
+typedef struct {
+  int32_t nx, ny, nz;
+  int32_t order_min, order_max;
+  double curve_amp;
+  int32_t n_gauss;
+  uint64_t seed;
+} ho_synth_params;
+
+typedef struct {
+  int64_t n_elem;
+  int64_t n_nodes;          /* BVH internal nodes                              */
+  int32_t max_modes;        /* largest modes count over geometry and field     */
+  int32_t bvh_depth;
+  int64_t device_bytes;     /* scene + BVH bytes resident on the device         */
+  float bounds[6];          /* scene box (lo xyz, hi xyz) over element boxes    */
+} ho_scene_info;
+
+/* Work counters of the last render/intersect call. */
+typedef struct {
+  uint64_t rays;
+  uint64_t candidates;       /* (ray, element) pairs visited                   */
+  uint64_t geom_evals;       /* x(xi) + Jacobian evaluations                   */
+  uint64_t map_evals;        /* x(xi)-only evaluations                         */
+  uint64_t field_evals;      /* u + grad evaluations                           */
+  uint64_t newton_iters;     /* inverse-map Newton iterations                  */
+  uint64_t face_iters;       /* surface Newton iterations                      */
+  uint64_t faces_culled;     /* faces skipped by the exact hull-box test       */
+  uint64_t node_visits;      /* BVH node fetches                               */
+  uint64_t mlp_accepted;     /* learned guesses that passed the checks         */
+  uint64_t mlp_rejected;
+  uint64_t restarts;         /* candidate-list overflows                       */
+  int32_t max_modes;
+  int32_t status;            /* device error status (0 = fine)                 */
+} ho_stats;
+
+/* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */
+int ho_create(int device, ho_context** out);
+/* Replaces: the cudaFree block of FEM-AABB/main.cu:580-597. */
+void ho_destroy(ho_context* ctx);
+/* Message of the last failed call on this context (never NULL). */
+const char* ho_last_error(const ho_context* ctx);
+
+/* Replaces: bool load_xml_fld(xml, fld, Scene&) (FEM-AABB/xml_fld_loader.h:14-16,
+ * xml_fld_loader.cpp:16-402). Hexahedra with curved edges/faces; FLD payload
+ * ASCII or base64+zlib FP64. Appends to the scene. */
+int ho_load_xml_fld(ho_context* ctx, const char* xml_path, const char* fld_path);
+
+/* Replaces: Scene::add_hex (FEM-AABB/raytracer.h:118-166), batched.
+ * corners: n*8*3 floats (XML vertex order); geom_modes / field_modes: n*3;
+ * geom_offsets[i]: float index of element i's x block in geom (y, z blocks
+ * follow, each nx*ny*nz floats), -1 = trilinear from corners;
+ * field_offsets[i]: float index into field, -1 = no field. */
+int ho_add_hexes(ho_context* ctx, int64_t n, const float* corners, const uint32_t* geom_modes,
+                 const float* geom, int64_t geom_len, const int64_t* geom_offsets,
+                 const uint32_t* field_modes, const float* field, int64_t field_len,
+                 const int64_t* field_offsets);
+
+/* Seeded synthetic scene (no reference counterpart: stands in for the
+ * reference's sample meshes at benchmark sizes). Appends to the scene. */
+int ho_generate_synthetic(ho_context* ctx, const ho_synth_params* params);
+
+/* Read back the scene as flat arrays (same layout as ho_add_hexes). Call with
+ * NULL outputs to get the lengths. */
+int ho_get_scene(ho_context* ctx, int64_t* n, float* corners, uint32_t* geom_modes, float* geom,
+                 int64_t* geom_len, int64_t* geom_offsets, uint32_t* field_modes, float* field,
+                 int64_t* field_len, int64_t* field_offsets);
+
+/* Replaces: Scene::build_bvh() -> BVH::build (FEM-AABB/raytracer.h:338-344,
+ * BVH.cu:180-247). Uploads the scene, computes element boxes and builds an
+ * LBVH on the device. */
+int ho_build_bvh(ho_context* ctx);
+int ho_scene_info_get(ho_context* ctx, ho_scene_info* out);
+/* Element boxes after ho_build_bvh: n*6 floats (padded sampled box lo, hi). */
+int ho_get_boxes(ho_context* ctx, float* out);
+/* Rigorous Bernstein hull boxes (n*6) and per-face hull boxes (n*36: 6 faces
+ * x lo,hi over u,v in [-1.001,1.001], inflated past the face tolerance);
+ * either output may be NULL. No reference counterpart (verification aid). */
+int ho_get_hull_boxes(ho_context* ctx, float* hull_out, float* face_out);
+
+/* Replaces: render_kernel<<<>>> + cudaMemcpy of the framebuffer
+ * (FEM-AABB/raytracer.cu:410-476, main.cu:515-543). One primary ray per
+ * pixel per isovalue; rgb_out receives n_iso images of H*W*3 bytes, row 0 =
+ * bottom of the view as in the reference. iso_zero_disables = 1 gives the
+ * reference renderer's rule that isovalue 0 turns the isosurface off
+ * (FEM-AABB/raytracer.cu:207). hits_out (optional) receives n_iso*H*W hits. */
+int ho_render(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int width,
+              int height, int iso_zero_disables, uint8_t* rgb_out, ho_hit* hits_out);
+
+/* Device-buffer variant of ho_render: rgb_dev / hits_dev are device pointers
+ * (either may be NULL); stream is a cudaStream_t (NULL = the context's). */
+int ho_render_device(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int width,
+                     int height, int iso_zero_disables, uint8_t* rgb_dev, ho_hit* hits_dev, void* stream);
+
+/* Replaces: bvh_intersect_device (FEM-AABB/raytracer.cu:102-358) for
+ * caller-supplied rays. rays: n*6 floats (origin xyz, direction xyz), host
+ * memory; iso_enabled = 0 traces boundary faces only. */
+int ho_intersect(ho_context* ctx, int64_t n, const float* rays, float iso, int iso_enabled, ho_hit* out);
+/* Device-buffer variant (rays_dev, out_dev on the device). */
+int ho_intersect_device(ho_context* ctx, int64_t n, const float* rays_dev, float iso, int iso_enabled,
+                        ho_hit* out_dev, void* stream);
+
+/* Solver mode (HO_MODE_*). No reference counterpart: the reference has one. */
+int ho_set_mode(ho_context* ctx, int mode);
+int ho_get_stats(ho_context* ctx, ho_stats* out);
+
+/* Replaces: save_image_ppm (FEM-AABB/raytracer.cu:480-494). P6, rows in
+ * buffer order. */
+int ho_save_ppm(const uint8_t* rgb, int width, int height, const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HORENDER_H */

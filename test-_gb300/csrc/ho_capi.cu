@@ -1,0 +1,439 @@
+// C ABI of the renderer (declared in include/horender.h).
+//
+// A context owns one CUDA stream and the device copy of one scene. The CUDA
+// context is touched lazily (first build / render), so scene assembly and
+// the host-side loader work without a GPU. Every call returns an HO_* status
+// and leaves its message in ho_last_error(); nothing throws across the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "ho_host.h"
+
+using ho::HostScene;
+
+namespace {
+
+int fail(ho_context* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(ho_context* c, int e, const char* what) {
+  return fail(c, HO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(static_cast<cudaError_t>(e)));
+}
+
+#define CK(call, what)                                   \
+  do {                                                   \
+    cudaError_t e__ = (call);                            \
+    if (e__ != cudaSuccess) return cuda_fail(c, int(e__), what); \
+  } while (0)
+
+int ensure_device(ho_context* c) {
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (!c->stream) CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (!c->d_stats) CK(cudaMalloc(&c->d_stats, sizeof(ho::DevStats)), "cudaMalloc(stats)");
+  return HO_OK;
+}
+
+void free_scene(ho_context* c) {
+  cudaFree(c->d_rec);
+  cudaFree(c->d_box);
+  cudaFree(c->d_hull);
+  cudaFree(c->d_fbox);
+  cudaFree(c->d_flags);
+  cudaFree(c->d_own);
+  cudaFree(c->d_nodes);
+  c->d_rec = c->d_box = c->d_hull = c->d_fbox = nullptr;
+  c->d_flags = nullptr;
+  c->d_own = nullptr;
+  c->d_nodes = nullptr;
+  c->built = false;
+  c->device_bytes = 0;
+}
+
+template <class T>
+int ensure_buf(ho_context* c, T*& p, size_t& cap, size_t count, const char* what) {
+  if (count <= cap && p) return HO_OK;
+  cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  CK(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)), what);
+  cap = count;
+  return HO_OK;
+}
+
+// Pinhole camera basis (FEM-AABB/raytracer.h:31-48, aperture 0).
+void camera_basis(const ho_camera& cam, int W, int H, ho::TraceArgs& a) {
+  auto sub = [](const float* x, const float* y, float* o) {
+    for (int i = 0; i < 3; ++i) o[i] = x[i] - y[i];
+  };
+  auto len = [](const float* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+  auto cross = [](const float* x, const float* y, float* o) {
+    o[0] = x[1] * y[2] - x[2] * y[1];
+    o[1] = x[2] * y[0] - x[0] * y[2];
+    o[2] = x[0] * y[1] - x[1] * y[0];
+  };
+  const float theta = cam.vfov_deg * 3.14159265f / 180.0f;
+  const float h = std::tan(theta / 2.0f);
+  const float vh = 2.0f * h, vw = (static_cast<float>(W) / static_cast<float>(H)) * vh;
+  float w[3], u[3], v[3];
+  sub(cam.lookfrom, cam.lookat, w);
+  float focus = cam.focus_dist > 0.f ? cam.focus_dist : len(w);
+  const float lw = len(w);
+  for (float& x : w) x = x * (1.0f / lw);
+  cross(cam.vup, w, u);
+  const float lu = len(u);
+  for (float& x : u) x = x * (1.0f / lu);
+  cross(w, u, v);
+  for (int i = 0; i < 3; ++i) {
+    a.origin[i] = cam.lookfrom[i];
+    a.horiz[i] = focus * vw * u[i];
+    a.vert[i] = focus * vh * v[i];
+    a.llc[i] = cam.lookfrom[i] - a.horiz[i] / 2.0f - a.vert[i] / 2.0f - focus * w[i];
+  }
+  a.width = W;
+  a.height = H;
+}
+
+int read_stats(ho_context* c) {
+  ho::DevStats ds;
+  CK(cudaMemcpyAsync(&ds, c->d_stats, sizeof(ds), cudaMemcpyDeviceToHost, c->stream), "read stats");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  ho_stats& s = c->last;
+  s.rays = ds.c[ho::ST_RAYS];
+  s.candidates = ds.c[ho::ST_CAND];
+  s.geom_evals = ds.c[ho::ST_GEOM];
+  s.map_evals = ds.c[ho::ST_MAP];
+  s.field_evals = ds.c[ho::ST_FIELD];
+  s.newton_iters = ds.c[ho::ST_NEWTON];
+  s.face_iters = ds.c[ho::ST_FACE];
+  s.faces_culled = ds.c[ho::ST_CULLED];
+  s.node_visits = ds.c[ho::ST_NODES];
+  s.mlp_accepted = ds.c[ho::ST_ACCEPT];
+  s.mlp_rejected = ds.c[ho::ST_REJECT];
+  s.restarts = ds.c[ho::ST_RESTART];
+  s.max_modes = c->N;
+  s.status = ds.status;
+  if (ds.status != 0)
+    return fail(c, HO_ERR_DEVICE, "kernel reported status " + std::to_string(ds.status) +
+                                      (ds.status & ho::kStatusStackOverflow ? " (traversal stack overflow)" : ""));
+  return HO_OK;
+}
+
+int check_iso(ho_context* c, const float* iso, int n_iso) {
+  if (n_iso < 1 || n_iso > 8) return fail(c, HO_ERR_RANGE, "n_iso must be in [1, 8]");
+  if (!iso) return fail(c, HO_ERR_ARG, "isovalues is NULL");
+  return HO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ho_create(int device, ho_context** out) {
+  if (!out) return HO_ERR_ARG;
+  *out = nullptr;
+  if (device < 0) return HO_ERR_ARG;
+  ho_context* c = new (std::nothrow) ho_context();
+  if (!c) return HO_ERR_NOMEM;
+  c->device = device;
+  *out = c;
+  return HO_OK;
+}
+
+void ho_destroy(ho_context* c) {
+  if (!c) return;
+  if (c->stream) {
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_scene(c);
+    cudaFree(c->d_stats);
+    cudaFree(c->d_hits);
+    cudaFree(c->d_rgb);
+    cudaFree(c->d_rays);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    cudaStreamDestroy(c->stream);
+  }
+  delete c;
+}
+
+const char* ho_last_error(const ho_context* c) { return c ? c->err.c_str() : "null context"; }
+
+int ho_add_hexes(ho_context* c, int64_t n, const float* corners, const uint32_t* gm, const float* geom,
+                 int64_t geom_len, const int64_t* goff, const uint32_t* fm, const float* field, int64_t field_len,
+                 const int64_t* foff) {
+  if (!c) return HO_ERR_ARG;
+  if (n < 0) return fail(c, HO_ERR_ARG, "n must be >= 0");
+  if (n > 0 && (!corners || !gm || !goff || !fm || !foff)) return fail(c, HO_ERR_ARG, "null array");
+  HostScene& hs = c->hs;
+  // validate first, so a failed call leaves the scene unchanged
+  for (int64_t i = 0; i < n; ++i) {
+    if (goff[i] >= 0) {
+      int64_t cnt = 1;
+      for (int a = 0; a < 3; ++a) {
+        if (gm[3 * i + a] < ho::kMinModes || gm[3 * i + a] > ho::kMaxModes)
+          return fail(c, HO_ERR_RANGE, "element " + std::to_string(i) + ": geometry modes must be in [2, 9]");
+        cnt *= gm[3 * i + a];
+      }
+      if (!geom || goff[i] + 3 * cnt > geom_len)
+        return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": geometry coefficients out of range");
+    }
+    if (foff[i] >= 0) {
+      int64_t cnt = 1;
+      for (int a = 0; a < 3; ++a) {
+        if (fm[3 * i + a] < 1 || fm[3 * i + a] > ho::kMaxModes)
+          return fail(c, HO_ERR_RANGE, "element " + std::to_string(i) + ": field modes must be in [1, 9]");
+        cnt *= fm[3 * i + a];
+      }
+      if (!field || foff[i] + cnt > field_len)
+        return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": field coefficients out of range");
+    }
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    hs.corners.insert(hs.corners.end(), corners + 24 * i, corners + 24 * i + 24);
+    if (goff[i] >= 0) {
+      const int64_t cnt = static_cast<int64_t>(gm[3 * i]) * gm[3 * i + 1] * gm[3 * i + 2];
+      hs.goff.push_back(static_cast<int64_t>(hs.geom.size()));
+      hs.geom.insert(hs.geom.end(), geom + goff[i], geom + goff[i] + 3 * cnt);
+      for (int a = 0; a < 3; ++a) hs.gmodes.push_back(gm[3 * i + a]);
+    } else {
+      hs.goff.push_back(-1);
+      for (int a = 0; a < 3; ++a) hs.gmodes.push_back(0);
+    }
+    if (foff[i] >= 0) {
+      const int64_t cnt = static_cast<int64_t>(fm[3 * i]) * fm[3 * i + 1] * fm[3 * i + 2];
+      hs.foff.push_back(static_cast<int64_t>(hs.field.size()));
+      hs.field.insert(hs.field.end(), field + foff[i], field + foff[i] + cnt);
+    } else {
+      hs.foff.push_back(-1);
+    }
+    for (int a = 0; a < 3; ++a) hs.fmodes.push_back(fm[3 * i + a]);
+  }
+  c->built = false;
+  return HO_OK;
+}
+
+int ho_generate_synthetic(ho_context* c, const ho_synth_params* p) {
+  if (!c) return HO_ERR_ARG;
+  if (!p) return fail(c, HO_ERR_ARG, "params is NULL");
+  std::string err;
+  const int rc = ho::generate_synthetic(*p, c->hs, err);
+  if (rc != HO_OK) return fail(c, rc, err);
+  c->built = false;
+  return HO_OK;
+}
+
+int ho_load_xml_fld(ho_context* c, const char* xml, const char* fld) {
+  if (!c) return HO_ERR_ARG;
+  if (!xml || !fld) return fail(c, HO_ERR_ARG, "path is NULL");
+  std::string err;
+  const int rc = ho::load_xml_fld(xml, fld, c->hs, err);
+  if (rc != HO_OK) return fail(c, rc, err);
+  c->built = false;
+  return HO_OK;
+}
+
+int ho_get_scene(ho_context* c, int64_t* n, float* corners, uint32_t* gm, float* geom, int64_t* geom_len,
+                 int64_t* goff, uint32_t* fm, float* field, int64_t* field_len, int64_t* foff) {
+  if (!c) return HO_ERR_ARG;
+  const HostScene& hs = c->hs;
+  if (n) *n = hs.size();
+  if (geom_len) *geom_len = static_cast<int64_t>(hs.geom.size());
+  if (field_len) *field_len = static_cast<int64_t>(hs.field.size());
+  if (corners) std::memcpy(corners, hs.corners.data(), hs.corners.size() * sizeof(float));
+  if (gm) std::memcpy(gm, hs.gmodes.data(), hs.gmodes.size() * sizeof(uint32_t));
+  if (geom) std::memcpy(geom, hs.geom.data(), hs.geom.size() * sizeof(float));
+  if (goff) std::memcpy(goff, hs.goff.data(), hs.goff.size() * sizeof(int64_t));
+  if (fm) std::memcpy(fm, hs.fmodes.data(), hs.fmodes.size() * sizeof(uint32_t));
+  if (field) std::memcpy(field, hs.field.data(), hs.field.size() * sizeof(float));
+  if (foff) std::memcpy(foff, hs.foff.data(), hs.foff.size() * sizeof(int64_t));
+  return HO_OK;
+}
+
+int ho_build_bvh(ho_context* c) {
+  if (!c) return HO_ERR_ARG;
+  const HostScene& hs = c->hs;
+  if (hs.size() == 0) return fail(c, HO_ERR_STATE, "scene is empty");
+  if (hs.size() > (int64_t(1) << 30)) return fail(c, HO_ERR_RANGE, "at most 2^30 elements");
+  int rc = ensure_device(c);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  free_scene(c);
+  const int N = ho::scene_max_modes(hs);
+  if (N > ho::kMaxModes) return fail(c, HO_ERR_RANGE, "modes per direction must be <= 9");
+  c->N = N;
+  c->n_elem = hs.size();
+  std::vector<float> rec;
+  std::vector<uint32_t> flags;
+  std::vector<int32_t> own;
+  ho::pack_records(hs, N, rec, flags, own);
+  const int64_t ne = c->n_elem;
+  CK(cudaMalloc(&c->d_rec, rec.size() * sizeof(float)), "cudaMalloc(records)");
+  CK(cudaMalloc(&c->d_flags, ne * sizeof(uint32_t)), "cudaMalloc(flags)");
+  CK(cudaMalloc(&c->d_own, ne * sizeof(int32_t)), "cudaMalloc(own)");
+  CK(cudaMalloc(&c->d_box, ne * 6 * sizeof(float)), "cudaMalloc(box)");
+  CK(cudaMalloc(&c->d_hull, ne * 6 * sizeof(float)), "cudaMalloc(hull)");
+  CK(cudaMalloc(&c->d_fbox, ne * ho::kFaceBoxFloats * sizeof(float)), "cudaMalloc(face boxes)");
+  CK(cudaMemcpyAsync(c->d_rec, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload");
+  CK(cudaMemcpyAsync(c->d_flags, flags.data(), ne * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream), "upload");
+  CK(cudaMemcpyAsync(c->d_own, own.data(), ne * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream), "upload");
+  rc = ho::launch_setup(c);
+  if (rc) return cuda_fail(c, rc, "setup kernel");
+  rc = ho::build_lbvh(c);
+  if (rc) return cuda_fail(c, rc, "LBVH build");
+  if (c->bvh_depth + 2 > 64) return fail(c, HO_ERR_RANGE, "BVH deeper than the traversal stack");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  c->device_bytes = static_cast<int64_t>(rec.size() * sizeof(float)) + ne * (4 + 4 + 24 + 24 + 144) +
+                    c->n_nodes * static_cast<int64_t>(sizeof(ho::BNode));
+  c->built = true;
+  return HO_OK;
+}
+
+int ho_scene_info_get(ho_context* c, ho_scene_info* out) {
+  if (!c || !out) return HO_ERR_ARG;
+  out->n_elem = c->hs.size();
+  out->n_nodes = c->built ? c->n_nodes : 0;
+  out->max_modes = c->built ? c->N : ho::scene_max_modes(c->hs);
+  out->bvh_depth = c->built ? c->bvh_depth : 0;
+  out->device_bytes = c->built ? c->device_bytes : 0;
+  for (int i = 0; i < 6; ++i) out->bounds[i] = c->bounds[i];
+  return HO_OK;
+}
+
+int ho_get_boxes(ho_context* c, float* out) {
+  if (!c || !out) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  CK(cudaMemcpyAsync(out, c->d_box, c->n_elem * 6 * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "read boxes");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return HO_OK;
+}
+
+int ho_get_hull_boxes(ho_context* c, float* out, float* face_out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (out)
+    CK(cudaMemcpyAsync(out, c->d_hull, c->n_elem * 6 * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "read");
+  if (face_out)
+    CK(cudaMemcpyAsync(face_out, c->d_fbox, c->n_elem * ho::kFaceBoxFloats * sizeof(float), cudaMemcpyDeviceToHost,
+                       c->stream),
+       "read");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return HO_OK;
+}
+
+int ho_render_device(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H,
+                     int iso_zero_disables, uint8_t* rgb_dev, ho_hit* hits_dev, void* stream) {
+  if (!c) return HO_ERR_ARG;
+  if (!cam) return fail(c, HO_ERR_ARG, "camera is NULL");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (W <= 0 || H <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
+  if (static_cast<int64_t>(W) * H * n_iso > (int64_t(1) << 31)) return fail(c, HO_ERR_RANGE, "too many rays");
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  ho::TraceArgs a;
+  camera_basis(*cam, W, H, a);
+  a.n_iso = n_iso;
+  for (int i = 0; i < n_iso; ++i) {
+    a.iso[i] = iso[i];
+    if (!(iso_zero_disables && iso[i] == 0.0f)) a.iso_on_mask |= 1u << i;
+  }
+  a.rgb = rgb_dev;
+  a.hits = hits_dev;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
+  rc = ho::launch_trace(c, a, s);
+  if (rc) return cuda_fail(c, rc, "trace kernel");
+  return HO_OK;
+}
+
+int ho_render(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int iso_zero_disables,
+              uint8_t* rgb_out, ho_hit* hits_out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (W <= 0 || H <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
+  const size_t nq = static_cast<size_t>(W) * H * n_iso;
+  if (rgb_out && (rc = ensure_buf(c, c->d_rgb, c->rgb_cap, nq * 3, "cudaMalloc(rgb)"))) return rc;
+  if (hits_out && (rc = ensure_buf(c, c->d_hits, c->hits_cap, nq, "cudaMalloc(hits)"))) return rc;
+  rc = ho_render_device(c, cam, iso, n_iso, W, H, iso_zero_disables, rgb_out ? c->d_rgb : nullptr,
+                        hits_out ? c->d_hits : nullptr, c->stream);
+  if (rc) return rc;
+  if (rgb_out) CK(cudaMemcpyAsync(rgb_out, c->d_rgb, nq * 3, cudaMemcpyDeviceToHost, c->stream), "read image");
+  if (hits_out)
+    CK(cudaMemcpyAsync(hits_out, c->d_hits, nq * sizeof(ho_hit), cudaMemcpyDeviceToHost, c->stream), "read hits");
+  return read_stats(c);
+}
+
+int ho_intersect_device(ho_context* c, int64_t n, const float* rays_dev, float iso, int iso_enabled, ho_hit* out_dev,
+                        void* stream) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (n < 0 || n > (int64_t(1) << 31)) return fail(c, HO_ERR_RANGE, "ray count out of range");
+  if (n > 0 && (!rays_dev || !out_dev)) return fail(c, HO_ERR_ARG, "null buffer");
+  ho::TraceArgs a;
+  a.rays = rays_dev;
+  a.n_rays = n;
+  a.n_iso = 1;
+  a.iso[0] = iso;
+  a.iso_on_mask = iso_enabled ? 1u : 0u;
+  a.hits = out_dev;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
+  if (n == 0) return HO_OK;
+  const int rc = ho::launch_trace(c, a, s);
+  if (rc) return cuda_fail(c, rc, "trace kernel");
+  return HO_OK;
+}
+
+int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso_enabled, ho_hit* out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (n < 0) return fail(c, HO_ERR_ARG, "n must be >= 0");
+  if (n > 0 && (!rays || !out)) return fail(c, HO_ERR_ARG, "null buffer");
+  int rc;
+  if ((rc = ensure_buf(c, c->d_rays, c->rays_cap, static_cast<size_t>(n) * 6, "cudaMalloc(rays)"))) return rc;
+  if ((rc = ensure_buf(c, c->d_hits, c->hits_cap, static_cast<size_t>(n), "cudaMalloc(hits)"))) return rc;
+  if (n > 0)
+    CK(cudaMemcpyAsync(c->d_rays, rays, n * 6 * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload rays");
+  rc = ho_intersect_device(c, n, c->d_rays, iso, iso_enabled, c->d_hits, c->stream);
+  if (rc) return rc;
+  if (n > 0) CK(cudaMemcpyAsync(out, c->d_hits, n * sizeof(ho_hit), cudaMemcpyDeviceToHost, c->stream), "read hits");
+  return read_stats(c);
+}
+
+int ho_set_mode(ho_context* c, int mode) {
+  if (!c) return HO_ERR_ARG;
+  if (mode != HO_MODE_PLAIN) return fail(c, HO_ERR_ARG, "mode not available in this build");
+  c->mode = mode;
+  return HO_OK;
+}
+
+int ho_get_stats(ho_context* c, ho_stats* out) {
+  if (!c || !out) return HO_ERR_ARG;
+  if (c->stream && c->d_stats) {
+    const int rc = read_stats(c);
+    if (rc && rc != HO_ERR_DEVICE) return rc;
+  }
+  *out = c->last;
+  return HO_OK;
+}
+
+int ho_save_ppm(const uint8_t* rgb, int W, int H, const char* path) {
+  if (!rgb || !path || W <= 0 || H <= 0) return HO_ERR_ARG;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return HO_ERR_IO;
+  std::fprintf(f, "P6\n%d %d\n255\n", W, H);
+  const size_t n = static_cast<size_t>(W) * H * 3;
+  const bool ok = std::fwrite(rgb, 1, n, f) == n;
+  std::fclose(f);
+  return ok ? HO_OK : HO_ERR_IO;
+}
+
+}  // extern "C"

@@ -1,0 +1,123 @@
+// Host-side types of the renderer: the context behind the C ABI, the scene as
+// the caller gave it, and the helpers shared by the host translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ho_layout.h"
+#include "horender.h"
+
+namespace ho {
+
+// Scene as supplied (ho_add_hexes / loader / generator): same layout as the
+// reference's Scene hex buffers (FEM-AABB/raytracer.h:65-96), one entry per
+// element, coefficients FP32.
+struct HostScene {
+  std::vector<float> corners;     // n*24, XML vertex order
+  std::vector<uint32_t> gmodes;   // n*3 (0,0,0 = trilinear from corners)
+  std::vector<uint32_t> fmodes;   // n*3
+  std::vector<int64_t> goff;      // n, -1 = trilinear
+  std::vector<int64_t> foff;      // n, -1 = no field
+  std::vector<float> geom;
+  std::vector<float> field;
+  int64_t size() const { return static_cast<int64_t>(goff.size()); }
+};
+
+// GLL nodes on [-1,1], ascending, computed in FP64.
+std::vector<double> gll_nodes(int n);
+// Modified-A mode i and its derivative at x, FP64.
+double mod_a(int i, double x);
+double mod_a_prime(int i, double x);
+// Inverse of the n x n matrix V[row][col] = phi_col(nodes[row]) (FP64).
+bool modal_vandermonde_inverse(const std::vector<double>& nodes, std::vector<double>& inv);
+// Tensor-product modal fit of nodal values (i fastest) on GLL nodes.
+void tensor_modal_fit(int n, const std::vector<double>& vinv, const double* nodal, double* modal);
+
+// Seeded synthetic scene generation (appends to hs).
+int generate_synthetic(const ho_synth_params& p, HostScene& hs, std::string& err);
+
+// Largest modes count over geometry and field (trilinear counts as 2).
+int scene_max_modes(const HostScene& hs);
+// Pack the scene into per-element records of 4*N^3 floats (x, y, z geometry
+// blocks then the field block), zero-padded to N modes per direction.
+// Trilinear elements become their exact N = 2 modal form. flags[e] bit 0:
+// has field; bit 1: trilinear (box rule of FEM-AABB/high_order.h:59-76);
+// own[e]: the element's own geometry modes (box sample count).
+void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vector<uint32_t>& flags,
+                  std::vector<int32_t>& own);
+
+// 1-D change of basis Modified-A -> Bernstein on [a,b] for n modes:
+// phi_i(x) = sum_k M[i*n+k] * B_k((x-a)/(b-a)).
+void modal_to_bernstein(int n, double a, double b, std::vector<double>& M);
+
+// PCG-XSL-RR 128/64 generator (published PCG64 algorithm).
+struct Pcg64 {
+  unsigned __int128 state, inc;
+  Pcg64(uint64_t seed, uint64_t stream);
+  uint64_t next();
+  double uniform();  // [0,1), 53 bits
+};
+
+int load_xml_fld(const std::string& xml, const std::string& fld, HostScene& hs, std::string& err);
+
+}  // namespace ho
+
+struct ho_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int mode = HO_MODE_PLAIN;
+  ho::HostScene hs;
+  bool built = false;
+
+  // device scene
+  int N = 0;
+  int64_t n_elem = 0;
+  float* d_rec = nullptr;         // n_elem * 4 * N^3
+  float* d_box = nullptr;         // n_elem * 6 padded sampled boxes
+  float* d_hull = nullptr;        // n_elem * 6 Bernstein hull boxes
+  float* d_fbox = nullptr;        // n_elem * 36 face hull boxes
+  uint32_t* d_flags = nullptr;    // n_elem
+  int32_t* d_own = nullptr;       // n_elem
+  ho::BNode* d_nodes = nullptr;   // max(1, n_elem - 1)
+  int64_t n_nodes = 0;
+  int bvh_depth = 0;
+  float bounds[6] = {0, 0, 0, 0, 0, 0};
+  int64_t device_bytes = 0;
+
+  ho::DevStats* d_stats = nullptr;
+  ho_stats last{};
+
+  // render scratch
+  ho_hit* d_hits = nullptr;
+  size_t hits_cap = 0;
+  uint8_t* d_rgb = nullptr;
+  size_t rgb_cap = 0;
+  float* d_rays = nullptr;
+  size_t rays_cap = 0;
+  void* h_pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+
+namespace ho {
+// Kernel launchers (ho_build.cu / ho_trace.cu). Return cudaError_t as int.
+int launch_setup(ho_context* c);
+int build_lbvh(ho_context* c);
+struct TraceArgs {
+  // camera mode (rays == nullptr): pixel-centre rays of a pinhole camera
+  float origin[3], llc[3], horiz[3], vert[3];
+  int width = 0, height = 0;
+  const float* rays = nullptr;  // explicit rays: n*6 floats on the device
+  int64_t n_rays = 0;
+  float iso[8];
+  int n_iso = 0;
+  uint32_t iso_on_mask = 0;     // bit i: isovalue i enabled
+  ho_hit* hits = nullptr;       // optional
+  uint8_t* rgb = nullptr;       // optional (camera mode)
+};
+int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s);
+}  // namespace ho

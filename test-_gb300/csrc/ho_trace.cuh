@@ -1,0 +1,305 @@
+// Ray queries against the curved-hex scene (plain mode).
+//
+// One thread per (ray, isovalue) query; for camera rays a warp covers an
+// 8x4 pixel tile so the lanes of a warp mostly visit the same elements and
+// their coefficient loads coalesce into broadcasts.
+//
+// Candidate order. The reference visits the elements whose padded box the
+// ray meets in BVH stack order, clipping each candidate's segment to the
+// closest hit found so far (FEM-AABB/raytracer.cu:111-358). Here candidates
+// are visited in ascending (box entry t, element index) order with the same
+// clipping: the traversal keeps the K smallest candidate keys above the last
+// visited key in registers, visits them, and walks the tree again only when
+// more than K candidates were in range (HO_FLAG_OVERFLOW), so every ray sees
+// exactly the ordered candidate sequence whatever the tree shape.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ho_device.cuh"
+#include "ho_host.h"
+
+namespace ho {
+
+constexpr int kCandK = 8;
+constexpr int kStack = 64;
+constexpr int kTraceBlock = 128;
+
+struct CamArgs {
+  float3 origin, llc, horiz, vert;
+  int width, height;
+};
+
+struct TraceParams {
+  const BNode* __restrict__ nodes;
+  const float* __restrict__ rec;
+  const float* __restrict__ fbox;
+  const float* __restrict__ box;
+  const uint32_t* __restrict__ flags;
+  const float* __restrict__ rays;  // explicit rays or nullptr
+  int64_t n_rays;
+  CamArgs cam;
+  float iso[8];
+  int n_iso;
+  uint32_t iso_on_mask;
+  ho_hit* __restrict__ hits;
+  uint8_t* __restrict__ rgb;
+  DevStats* stats;
+};
+
+__device__ __forceinline__ bool key_less(float ta, int ea, float tb, int eb) {
+  return ta < tb || (ta == tb && ea < eb);
+}
+
+// Insert (t, e) into the ascending register buffer; the largest falls out.
+__device__ __forceinline__ void kbuf_insert(float (&bt)[kCandK], int (&be)[kCandK], float t, int e) {
+#pragma unroll
+  for (int j = 0; j < kCandK; ++j) {
+    const bool sw = key_less(t, e, bt[j], be[j]);
+    const float tt = sw ? bt[j] : t;
+    const int ee = sw ? be[j] : e;
+    bt[j] = sw ? t : bt[j];
+    be[j] = sw ? e : be[j];
+    t = tt;
+    e = ee;
+  }
+}
+
+__device__ __forceinline__ void load_child(const BNode* __restrict__ nodes, int node, int c, float (&lo)[3],
+                                           float (&hi)[3], int& idx, uint32_t& aux) {
+  const float4* p = reinterpret_cast<const float4*>(&nodes[node].c[c]);
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  lo[0] = a.x; lo[1] = a.y; lo[2] = a.z;
+  idx = __float_as_int(a.w);
+  hi[0] = b.x; hi[1] = b.y; hi[2] = b.z;
+  aux = __float_as_uint(b.w);
+}
+
+// Collect the K smallest candidate keys > (kt, ke) with entry <= tmax.
+// Returns false on traversal-stack overflow (status set by the caller).
+static __device__ bool collect(const TraceParams& P, float3 o, float3 d, float tmax, float kt, int ke, float (&bt)[kCandK],
+                        int (&be)[kCandK], bool& overflow, Work& w) {
+#pragma unroll
+  for (int j = 0; j < kCandK; ++j) {
+    bt[j] = FLT_MAX;
+    be[j] = INT_MAX;
+  }
+  overflow = false;
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const int node = stack[--sp];
+    ++w.nodes;
+    float te[2];
+    int id[2];
+    bool hit[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      float lo[3], hi[3];
+      uint32_t aux;
+      load_child(P.nodes, node, c, lo, hi, id[c], aux);
+      hit[c] = false;
+      te[c] = FLT_MAX;
+      if (id[c] == kEmptyChild) continue;
+      float a0, a1;
+      // the current bound: the closest hit so far, tightened by the K-th key
+      const float bound = fminf(tmax, bt[kCandK - 1]);
+      if (!ray_box(o, d, lo, hi, 0.001f, bound, a0, a1)) continue;
+      if (a1 < kt) continue;  // everything inside enters before the last visited key
+      if (id[c] < 0) {
+        const int e = ~id[c];
+        if (!key_less(kt, ke, a0, e)) continue;  // already visited
+        if (a0 > tmax) continue;
+        if (!key_less(a0, e, bt[kCandK - 1], be[kCandK - 1])) {
+          overflow = true;
+          continue;
+        }
+        if (be[kCandK - 1] != INT_MAX) overflow = true;  // the largest falls out
+        kbuf_insert(bt, be, a0, e);
+      } else {
+        hit[c] = true;
+        te[c] = a0;
+      }
+    }
+    if (hit[0] && hit[1]) {
+      if (sp + 2 > kStack) return false;
+      const int nearc = te[0] <= te[1] ? 0 : 1;
+      stack[sp++] = id[1 - nearc];
+      stack[sp++] = id[nearc];
+    } else if (hit[0] || hit[1]) {
+      if (sp + 1 > kStack) return false;
+      stack[sp++] = hit[0] ? id[0] : id[1];
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool active) {
+  // warp-aggregated counters
+  uint32_t v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled, w.nodes,
+                          w.accepted, w.rejected, w.restarts};
+#pragma unroll
+  for (int s = 0; s < ST_COUNT; ++s) {
+    unsigned long long x = v[s];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(&st->c[s], x);
+  }
+}
+
+// Primary-ray shading: Lambert headlight on hits (blue on face 0 as
+// raytracer.cu:247-248 assigns material 1 there, grey otherwise), sky
+// gradient on misses (raytracer.cu:398-402), gamma 2 and 8-bit quantisation
+// (raytracer.cu:462-475).
+__device__ __forceinline__ void shade(const HitState& h, float3 d, uint8_t* out) {
+  float c[3];
+  if (h.kind == HO_HIT_MISS) {
+    const float a = 0.5f * (d.y + 1.0f);
+    c[0] = (1.0f - a) * 1.0f + a * 0.5f;
+    c[1] = (1.0f - a) * 1.0f + a * 0.7f;
+    c[2] = (1.0f - a) * 1.0f + a * 1.0f;
+  } else {
+    const bool blue = h.kind == HO_HIT_FACE && h.face == 0;
+    float lam = -(h.n.x * d.x + h.n.y * d.y + h.n.z * d.z);
+    lam = lam > 0.f ? lam : 0.f;
+    const float k = 0.2f + 0.8f * lam;
+    c[0] = (blue ? 0.1f : 0.5f) * k;
+    c[1] = (blue ? 0.2f : 0.5f) * k;
+    c[2] = (blue ? 0.8f : 0.5f) * k;
+  }
+#pragma unroll
+  for (int q = 0; q < 3; ++q) out[q] = static_cast<uint8_t>(255.99f * fminf(1.0f, sqrtf(c[q])));
+}
+
+template <int N>
+__global__ void __launch_bounds__(kTraceBlock) trace_kernel(TraceParams P, int64_t n_queries) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x) >> 5;
+  int64_t q;
+  float3 o, d;
+  int iso_idx;
+  bool active;
+  int64_t pix = 0;
+  if (P.rays == nullptr) {
+    const int tx_n = (P.cam.width + 7) >> 3, ty_n = (P.cam.height + 3) >> 2;
+    const int64_t tiles = static_cast<int64_t>(tx_n) * ty_n;
+    iso_idx = static_cast<int>(wid / tiles);
+    const int64_t tile = wid - static_cast<int64_t>(iso_idx) * tiles;
+    const int x = static_cast<int>(tile % tx_n) * 8 + (lane & 7);
+    const int y = static_cast<int>(tile / tx_n) * 4 + (lane >> 3);
+    active = iso_idx < P.n_iso && x < P.cam.width && y < P.cam.height;
+    pix = static_cast<int64_t>(y) * P.cam.width + x;
+    q = static_cast<int64_t>(iso_idx) * P.cam.width * P.cam.height + pix;
+    const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(P.cam.width);
+    const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(P.cam.height);
+    o = P.cam.origin;
+    d = make_float3(P.cam.llc.x + s * P.cam.horiz.x + t * P.cam.vert.x - o.x,
+                    P.cam.llc.y + s * P.cam.horiz.y + t * P.cam.vert.y - o.y,
+                    P.cam.llc.z + s * P.cam.horiz.z + t * P.cam.vert.z - o.z);
+    d = normalize3(d);
+  } else {
+    q = static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x;
+    active = q < n_queries;
+    iso_idx = active ? static_cast<int>(q / P.n_rays) : 0;
+    const int64_t r = active ? q - static_cast<int64_t>(iso_idx) * P.n_rays : 0;
+    const float* rp = P.rays + 6 * r;
+    o = active ? make_float3(rp[0], rp[1], rp[2]) : make_float3(0.f, 0.f, 0.f);
+    d = active ? make_float3(rp[3], rp[4], rp[5]) : make_float3(0.f, 0.f, 1.f);
+  }
+  Work w;
+  HitState best;
+  best.t = FLT_MAX;
+  best.elem = -1;
+  best.face = -1;
+  best.kind = HO_HIT_MISS;
+  best.xi = make_float3(0.f, 0.f, 0.f);
+  best.n = best.xi;
+  best.u = 0.f;
+  best.flags = 0;
+  if (active) {
+    const float iso = P.iso[iso_idx];
+    const bool iso_on = (P.iso_on_mask >> iso_idx) & 1u;
+    constexpr int64_t S = static_cast<int64_t>(N) * N * N;
+    float kt = -FLT_MAX;
+    int ke = -1;
+    for (;;) {
+      float bt[kCandK];
+      int be[kCandK];
+      bool overflow;
+      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, w)) {
+        atomicOr(&P.stats->status, kStatusStackOverflow);
+        break;
+      }
+      bool done = false;
+#pragma unroll 1
+      for (int j = 0; j < kCandK; ++j) {
+        // the buffer is sorted; read entry j through a static-index select
+        // chain so the buffer stays in registers
+        float ct = bt[0];
+        int ce = be[0];
+#pragma unroll
+        for (int m = 1; m < kCandK; ++m)
+          if (j == m) {
+            ct = bt[m];
+            ce = be[m];
+          }
+        if (ce == INT_MAX || ct > best.t) {
+          done = true;
+          break;
+        }
+        // segment of the padded box clipped to the closest hit so far
+        const float* b = P.box + 6 * static_cast<int64_t>(ce);
+        const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
+        const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
+        float te, tx;
+        if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
+          Elem<N> el;
+          el.c = P.rec + static_cast<int64_t>(ce) * 4 * S;
+          el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
+          visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
+                             best, w);
+        }
+        kt = ct;
+        ke = ce;
+      }
+      if (done || !overflow) break;
+      ++w.restarts;
+      best.flags |= HO_FLAG_OVERFLOW;
+    }
+  }
+  flush_work(P.stats, w, active);
+  if (!active) return;
+  if (P.hits) {
+    ho_hit h;
+    h.t = best.t;
+    h.elem = best.elem;
+    h.face = static_cast<int16_t>(best.face);
+    h.kind = static_cast<int16_t>(best.kind);
+    h.xi[0] = best.xi.x; h.xi[1] = best.xi.y; h.xi[2] = best.xi.z;
+    h.n[0] = best.n.x; h.n[1] = best.n.y; h.n[2] = best.n.z;
+    h.u = best.u;
+    h.flags = best.flags;
+    h.iters = w.newton + w.face;
+    P.hits[q] = h;
+  }
+  if (P.rgb && P.rays == nullptr) shade(best, d, P.rgb + 3 * q);
+}
+template <int N>
+cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s) {
+  const int64_t blocks = (n_threads + kTraceBlock - 1) / kTraceBlock;
+  trace_kernel<N><<<static_cast<unsigned>(blocks), kTraceBlock, 0, s>>>(P, n_queries);
+  return cudaGetLastError();
+}
+
+// explicit instantiations live in ho_trace_n*.cu
+extern template cudaError_t launch_n<2>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<3>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<4>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<5>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<6>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<7>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<8>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+
+}  // namespace ho

@@ -1,0 +1,6 @@
+// Instantiation of the trace kernel for 3 modes per direction.
+#include "ho_trace.cuh"
+
+namespace ho {
+template cudaError_t launch_n<3>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+}  // namespace ho

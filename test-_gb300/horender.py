@@ -1,0 +1,280 @@
+"""Python binding of libhorender.so (the C ABI in include/horender.h).
+
+This is the interface tests and benchmarks drive; it adds no computation of
+its own. It mirrors the reference's host API shape: load a scene (or add
+hexes / generate a seeded one), build the BVH, render(camera, isovalues) ->
+images, intersect(rays) -> hits, save_ppm.
+
+There is no fallback: if the compiled library is missing, importing this
+module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libhorender.so"
+
+HO_OK = 0
+ERRORS = {-1: "HO_ERR_ARG", -2: "HO_ERR_CUDA", -3: "HO_ERR_STATE", -4: "HO_ERR_IO", -5: "HO_ERR_PARSE",
+          -6: "HO_ERR_NOMEM", -7: "HO_ERR_RANGE", -8: "HO_ERR_DEVICE"}
+MODE_PLAIN, MODE_LEARNED, MODE_BATCHED = 0, 1, 2
+HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
+FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW = 1, 2, 4
+
+HIT_DTYPE = np.dtype([("t", "<f4"), ("elem", "<i4"), ("face", "<i2"), ("kind", "<i2"), ("xi", "<f4", 3),
+                      ("n", "<f4", 3), ("u", "<f4"), ("flags", "<u4"), ("iters", "<u4")])
+assert HIT_DTYPE.itemsize == 48
+
+
+class HoError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Camera(C.Structure):
+    _fields_ = [("lookfrom", C.c_float * 3), ("lookat", C.c_float * 3), ("vup", C.c_float * 3),
+                ("vfov_deg", C.c_float), ("focus_dist", C.c_float)]
+
+
+class _Synth(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("order_min", C.c_int32),
+                ("order_max", C.c_int32), ("curve_amp", C.c_double), ("n_gauss", C.c_int32),
+                ("seed", C.c_uint64)]
+
+
+class _Info(C.Structure):
+    _fields_ = [("n_elem", C.c_int64), ("n_nodes", C.c_int64), ("max_modes", C.c_int32),
+                ("bvh_depth", C.c_int32), ("device_bytes", C.c_int64), ("bounds", C.c_float * 6)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("rays", "candidates", "geom_evals", "map_evals", "field_evals",
+                                          "newton_iters", "face_iters", "faces_culled", "node_visits",
+                                          "mlp_accepted", "mlp_rejected", "restarts")] + [
+        ("max_modes", C.c_int32), ("status", C.c_int32)]
+
+
+def _load():
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build() (no CPU fallback exists)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, i32, i64, f32 = C.c_void_p, C.c_int, C.c_int64, C.c_float
+    L.ho_create.argtypes = [i32, C.POINTER(vp)]
+    L.ho_destroy.argtypes = [vp]
+    L.ho_destroy.restype = None
+    L.ho_last_error.argtypes = [vp]
+    L.ho_last_error.restype = C.c_char_p
+    L.ho_load_xml_fld.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.ho_add_hexes.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, i64, vp]
+    L.ho_generate_synthetic.argtypes = [vp, C.POINTER(_Synth)]
+    L.ho_get_scene.argtypes = [vp] + [vp] * 10
+    L.ho_build_bvh.argtypes = [vp]
+    L.ho_scene_info_get.argtypes = [vp, C.POINTER(_Info)]
+    L.ho_get_boxes.argtypes = [vp, vp]
+    L.ho_get_hull_boxes.argtypes = [vp, vp, vp]
+    L.ho_render.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp]
+    L.ho_render_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp, vp]
+    L.ho_intersect.argtypes = [vp, i64, vp, f32, i32, vp]
+    L.ho_intersect_device.argtypes = [vp, i64, vp, f32, i32, vp, vp]
+    L.ho_set_mode.argtypes = [vp, i32]
+    L.ho_get_stats.argtypes = [vp, C.POINTER(_Stats)]
+    L.ho_save_ppm.argtypes = [vp, i32, i32, C.c_char_p]
+    return L
+
+
+lib = _load()
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+@dataclass
+class Camera:
+    """Pinhole camera (FEM-AABB/raytracer.h:31-48 with aperture 0)."""
+    lookfrom: tuple
+    lookat: tuple
+    vup: tuple = (0.0, 1.0, 0.0)
+    vfov_deg: float = 60.0
+    focus_dist: float = 0.0
+
+    def _c(self) -> _Camera:
+        c = _Camera()
+        c.lookfrom[:] = [float(x) for x in self.lookfrom]
+        c.lookat[:] = [float(x) for x in self.lookat]
+        c.vup[:] = [float(x) for x in self.vup]
+        c.vfov_deg = float(self.vfov_deg)
+        c.focus_dist = float(self.focus_dist)
+        return c
+
+
+@dataclass
+class Workload:
+    """A named synthetic workload: scene + view + isovalues."""
+    name: str
+    nx: int
+    order_min: int
+    order_max: int
+    curve_amp: float
+    n_gauss: int
+    seed: int
+    width: int
+    height: int
+    isovalues: list = field(default_factory=list)
+    camera: Camera = field(default_factory=lambda: Camera((2.5, 2.0, 1.8), (0.5, 0.5, 0.5), (0, 1, 0), 60.0))
+
+    def synth(self) -> dict:
+        return dict(nx=self.nx, ny=self.nx, nz=self.nx, order_min=self.order_min, order_max=self.order_max,
+                    curve_amp=self.curve_amp, n_gauss=self.n_gauss, seed=self.seed)
+
+
+# Benchmark workloads (seeded synthetic stand-ins for the reference's meshes).
+WORKLOADS = {
+    "hex4_p4": Workload("hex4_p4", 4, 4, 4, 0.05, 8, 1, 256, 256, [0.2]),
+    "hex32_p6": Workload("hex32_p6", 32, 6, 6, 0.08, 64, 2, 1920, 1080, [-0.3, 0.0, 0.3]),
+    "hex48_mixed": Workload("hex48_mixed", 48, 2, 8, 0.1, 64, 3, 1024, 1024, [-0.2, 0.1, 0.3]),
+    "hex64_p5": Workload("hex64_p5", 64, 5, 5, 0.12, 64, 4, 3840, 2160, [0.1]),
+}
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        rc = lib.ho_create(int(device), C.byref(h))
+        if rc != HO_OK:
+            raise HoError(rc, "ho_create failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib.ho_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc: int):
+        if rc != HO_OK:
+            raise HoError(rc, lib.ho_last_error(self.h).decode())
+
+    # ---- scene ---------------------------------------------------------------
+    def add_hexes(self, corners, geom_modes, geom, geom_offsets, field_modes, field, field_offsets):
+        corners = np.ascontiguousarray(corners, np.float32)
+        gm = np.ascontiguousarray(geom_modes, np.uint32)
+        geom = np.ascontiguousarray(geom, np.float32)
+        go = np.ascontiguousarray(geom_offsets, np.int64)
+        fm = np.ascontiguousarray(field_modes, np.uint32)
+        field = np.ascontiguousarray(field, np.float32)
+        fo = np.ascontiguousarray(field_offsets, np.int64)
+        n = go.shape[0]
+        self._ck(lib.ho_add_hexes(self.h, n, _p(corners), _p(gm), _p(geom), geom.size, _p(go), _p(fm), _p(field),
+                                  field.size, _p(fo)))
+
+    def generate_synthetic(self, nx, ny, nz, order_min, order_max, curve_amp, n_gauss, seed):
+        s = _Synth(nx, ny, nz, order_min, order_max, curve_amp, n_gauss, seed)
+        self._ck(lib.ho_generate_synthetic(self.h, C.byref(s)))
+
+    def load_xml_fld(self, xml: str, fld: str):
+        self._ck(lib.ho_load_xml_fld(self.h, str(xml).encode(), str(fld).encode()))
+
+    def get_scene(self) -> dict:
+        n, gl, fl = C.c_int64(), C.c_int64(), C.c_int64()
+        self._ck(lib.ho_get_scene(self.h, C.byref(n), None, None, None, C.byref(gl), None, None, None, C.byref(fl),
+                                  None))
+        n = n.value
+        out = dict(corners=np.zeros((n, 8, 3), np.float32), geom_modes=np.zeros((n, 3), np.uint32),
+                   geom=np.zeros(gl.value, np.float32), geom_offsets=np.zeros(n, np.int64),
+                   field_modes=np.zeros((n, 3), np.uint32), field=np.zeros(fl.value, np.float32),
+                   field_offsets=np.zeros(n, np.int64))
+        self._ck(lib.ho_get_scene(self.h, None, _p(out["corners"]), _p(out["geom_modes"]), _p(out["geom"]), None,
+                                  _p(out["geom_offsets"]), _p(out["field_modes"]), _p(out["field"]), None,
+                                  _p(out["field_offsets"])))
+        return out
+
+    def build_bvh(self):
+        self._ck(lib.ho_build_bvh(self.h))
+
+    def info(self) -> dict:
+        i = _Info()
+        self._ck(lib.ho_scene_info_get(self.h, C.byref(i)))
+        return dict(n_elem=i.n_elem, n_nodes=i.n_nodes, max_modes=i.max_modes, bvh_depth=i.bvh_depth,
+                    device_bytes=i.device_bytes, bounds=list(i.bounds))
+
+    def boxes(self) -> np.ndarray:
+        n = self.info()["n_elem"]
+        out = np.zeros((n, 6), np.float32)
+        self._ck(lib.ho_get_boxes(self.h, _p(out)))
+        return out
+
+    def hull_boxes(self):
+        n = self.info()["n_elem"]
+        hull = np.zeros((n, 6), np.float32)
+        faces = np.zeros((n, 6, 6), np.float32)
+        self._ck(lib.ho_get_hull_boxes(self.h, _p(hull), _p(faces)))
+        return hull, faces
+
+    def set_mode(self, mode: int):
+        self._ck(lib.ho_set_mode(self.h, int(mode)))
+
+    # ---- queries ---------------------------------------------------------------
+    def render(self, camera: Camera, isovalues, width: int, height: int, iso_zero_disables: bool = True,
+               want_rgb: bool = True, want_hits: bool = False):
+        iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
+        n = iso.size
+        rgb = np.zeros((n, height, width, 3), np.uint8) if want_rgb else None
+        hits = np.zeros((n, height, width), HIT_DTYPE) if want_hits else None
+        cam = camera._c()
+        self._ck(lib.ho_render(self.h, C.byref(cam), _p(iso), n, width, height, int(iso_zero_disables),
+                               _p(rgb) if rgb is not None else None, _p(hits) if hits is not None else None))
+        return rgb, hits
+
+    def render_device(self, camera: Camera, isovalues, width, height, rgb_ptr, hits_ptr, stream_ptr,
+                      iso_zero_disables: bool = True):
+        iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
+        cam = camera._c()
+        self._ck(lib.ho_render_device(self.h, C.byref(cam), _p(iso), iso.size, width, height,
+                                      int(iso_zero_disables), rgb_ptr, hits_ptr, stream_ptr))
+
+    def intersect(self, rays: np.ndarray, iso: float, iso_enabled: bool = True) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        out = np.zeros(rays.shape[0], HIT_DTYPE)
+        self._ck(lib.ho_intersect(self.h, rays.shape[0], _p(rays), float(iso), int(iso_enabled), _p(out)))
+        return out
+
+    def intersect_device(self, n: int, rays_ptr: int, iso: float, iso_enabled: bool, out_ptr: int, stream_ptr):
+        self._ck(lib.ho_intersect_device(self.h, int(n), rays_ptr, float(iso), int(iso_enabled), out_ptr,
+                                         stream_ptr))
+
+    def stats(self) -> dict:
+        s = _Stats()
+        self._ck(lib.ho_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+def save_ppm(rgb: np.ndarray, path: str):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    h, w = rgb.shape[:2]
+    rc = lib.ho_save_ppm(_p(rgb), w, h, str(path).encode())
+    if rc != HO_OK:
+        raise HoError(rc, f"cannot write {path}")
+
+
+def workload_context(name: str, device: int = 0, build: bool = True) -> tuple[Context, Workload]:
+    w = WORKLOADS[name]
+    ctx = Context(device)
+    ctx.generate_synthetic(**w.synth())
+    if build:
+        ctx.build_bvh()
+    return ctx, w

@@ -1,0 +1,349 @@
+"""ctypes bindings for the CPU oracle (oracle/_build/libhorender_oracle.so)
+and, where it was built, for the reference shim (oracle/_ref/libref.so).
+
+Test infrastructure: only tests, ``__graft_entry__.smoke()`` and bench.py's
+CPU-baseline arm use this module, always as the checker.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[1]
+ORACLE_SO = ROOT / "oracle" / "_build" / "libhorender_oracle.so"
+REF_SO = ROOT / "oracle" / "_ref" / "libref.so"
+
+HIT_DTYPE = np.dtype(
+    [("t", "f8"), ("elem", "i4"), ("face", "i4"), ("kind", "i4"), ("pad", "i4"),
+     ("xi", "f8", 3), ("n", "f8", 3), ("u", "f8")]
+)
+
+KIND_MISS, KIND_FACE, KIND_ISO = 0, 1, 2
+
+
+class _SceneDesc(C.Structure):
+    _fields_ = [
+        ("n_elem", C.c_int32),
+        ("geom_modes", C.c_void_p),
+        ("geom_offset", C.c_void_p),
+        ("geom", C.c_void_p),
+        ("field_modes", C.c_void_p),
+        ("field_offset", C.c_void_p),
+        ("field", C.c_void_p),
+        ("verts", C.c_void_p),
+    ]
+
+
+class _Counters(C.Structure):
+    _fields_ = [("newton_iters", C.c_uint64), ("face_iters", C.c_uint64),
+                ("newton_solves", C.c_uint64), ("candidates", C.c_uint64)]
+
+
+def build_oracle() -> Path:
+    """Compile the oracle with its Makefile (quick; no GPU needed)."""
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+    return ORACLE_SO
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not ORACLE_SO.exists():
+            build_oracle()
+        L = C.CDLL(str(ORACLE_SO))
+        vp, i32, i64, f32 = C.c_void_p, C.c_int, C.c_int64, C.c_float
+        L.hor_scene_create.restype = vp
+        L.hor_scene_create.argtypes = [C.POINTER(_SceneDesc)]
+        L.hor_scene_destroy.argtypes = [vp]
+        L.hor_scene_boxes.argtypes = [vp, i32, vp]
+        L.hor_trace.argtypes = [vp, i32, vp, i64, f32, i32, i32, vp, C.POINTER(_Counters)]
+        L.hor_map_point.argtypes = [vp, i32, i32, vp, i64, vp]
+        L.hor_eval_point.argtypes = [vp, i32, i32, vp, i64, vp]
+        L.hor_inverse_map.argtypes = [vp, i32, i32, vp, i64, vp]
+        L.hor_find_iso.argtypes = [vp, i32, i32, vp, vp, i64, f32, vp]
+        L.hor_hit_hex.argtypes = [vp, i32, i32, vp, vp, i64, vp]
+        L.hor_basis.argtypes = [i32, C.c_uint, C.c_double, vp]
+        L.hor_camera_rays.argtypes = [vp, vp, vp, f32, i32, i32, vp]
+        L.hor_shade.argtypes = [vp, vp, i64, vp]
+        L.hor_trace_replay.argtypes = [vp, i32, vp, i64, f32, i32, vp, i32, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class SceneArrays:
+    """Flat scene arrays shared by the oracle, the reference shim and the
+    product's C-ABI: per element geometry/field modes (n x 3 uint32), offsets
+    (int64, -1 = absent) into flat fp32 coefficient arrays, corner vertices
+    (n x 8 x 3 fp32, XML order)."""
+
+    def __init__(self, geom_modes, geom_offset, geom, field_modes, field_offset, field, verts):
+        self.geom_modes = np.ascontiguousarray(geom_modes, dtype=np.uint32).reshape(-1, 3)
+        self.geom_offset = np.ascontiguousarray(geom_offset, dtype=np.int64)
+        self.geom = np.ascontiguousarray(geom, dtype=np.float32)
+        self.field_modes = np.ascontiguousarray(field_modes, dtype=np.uint32).reshape(-1, 3)
+        self.field_offset = np.ascontiguousarray(field_offset, dtype=np.int64)
+        self.field = np.ascontiguousarray(field, dtype=np.float32)
+        if self.field.size == 0:
+            self.field = np.zeros(1, np.float32)
+        if self.geom.size == 0:
+            self.geom = np.zeros(1, np.float32)
+        self.verts = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 8, 3)
+
+    @property
+    def n(self) -> int:
+        return int(self.geom_modes.shape[0])
+
+    def save(self, path):
+        np.savez_compressed(path, geom_modes=self.geom_modes, geom_offset=self.geom_offset, geom=self.geom,
+                            field_modes=self.field_modes, field_offset=self.field_offset, field=self.field,
+                            verts=self.verts)
+
+    @staticmethod
+    def load(path) -> "SceneArrays":
+        z = np.load(path)
+        return SceneArrays(z["geom_modes"], z["geom_offset"], z["geom"], z["field_modes"], z["field_offset"],
+                           z["field"], z["verts"])
+
+
+class OracleScene:
+    def __init__(self, arrs: SceneArrays):
+        self.arrs = arrs
+        d = _SceneDesc(arrs.n, _p(arrs.geom_modes).value, _p(arrs.geom_offset).value, _p(arrs.geom).value,
+                       _p(arrs.field_modes).value, _p(arrs.field_offset).value, _p(arrs.field).value,
+                       _p(arrs.verts).value)
+        self.h = lib().hor_scene_create(C.byref(d))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().hor_scene_destroy(self.h)
+            self.h = None
+
+    def boxes(self, precision=64) -> np.ndarray:
+        out = np.zeros((self.arrs.n, 6), np.float64)
+        lib().hor_scene_boxes(self.h, precision, _p(out))
+        return out
+
+    def trace(self, rays: np.ndarray, iso: float, iso_on: bool = True, precision: int = 64,
+              threads: int | None = None):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = np.zeros(rays.shape[0], HIT_DTYPE)
+        cnt = _Counters()
+        nt = threads or os.cpu_count() or 1
+        lib().hor_trace(self.h, precision, _p(rays), rays.shape[0], float(iso), int(iso_on), nt, _p(out),
+                        C.byref(cnt))
+        return out, {k: getattr(cnt, k) for k, _ in _Counters._fields_}
+
+    def trace_replay(self, rays, iso, iso_on, order, order_n, precision=32):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        order = np.ascontiguousarray(order, np.int32)
+        order_n = np.ascontiguousarray(order_n, np.int32)
+        out = np.zeros(rays.shape[0], HIT_DTYPE)
+        lib().hor_trace_replay(self.h, precision, _p(rays), rays.shape[0], float(iso), int(iso_on), _p(order),
+                               order.shape[1], _p(order_n), _p(out))
+        return out
+
+    def map_point(self, elem, xi, precision=64):
+        xi = np.ascontiguousarray(xi, np.float64).reshape(-1, 3)
+        out = np.zeros_like(xi)
+        lib().hor_map_point(self.h, precision, elem, _p(xi), xi.shape[0], _p(out))
+        return out
+
+    def eval_point(self, elem, xi, precision=64):
+        xi = np.ascontiguousarray(xi, np.float64).reshape(-1, 3)
+        out = np.zeros((xi.shape[0], 13))
+        lib().hor_eval_point(self.h, precision, elem, _p(xi), xi.shape[0], _p(out))
+        return out
+
+    def inverse_map(self, elem, x, precision=64):
+        x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+        out = np.zeros((x.shape[0], 4))
+        lib().hor_inverse_map(self.h, precision, elem, _p(x), x.shape[0], _p(out))
+        return out
+
+    def find_iso(self, elem, rays, seg, iso, precision=64):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        seg = np.ascontiguousarray(seg, np.float64).reshape(-1, 2)
+        out = np.zeros((rays.shape[0], 8))
+        lib().hor_find_iso(self.h, precision, elem, _p(rays), _p(seg), rays.shape[0], float(iso), _p(out))
+        return out
+
+    def hit_hex(self, elem, rays, seg, precision=64):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        seg = np.ascontiguousarray(seg, np.float64).reshape(-1, 2)
+        out = np.zeros((rays.shape[0], 6))
+        lib().hor_hit_hex(self.h, precision, elem, _p(rays), _p(seg), rays.shape[0], _p(out))
+        return out
+
+
+def basis(nmodes: int, x: float, precision=64) -> np.ndarray:
+    out = np.zeros((nmodes, 2))
+    lib().hor_basis(precision, nmodes, float(x), _p(out))
+    return out
+
+
+def camera_rays(lookfrom, lookat, vup, vfov, W, H) -> np.ndarray:
+    f = np.asarray(lookfrom, np.float32)
+    a = np.asarray(lookat, np.float32)
+    u = np.asarray(vup, np.float32)
+    out = np.zeros((H * W, 6), np.float32)
+    lib().hor_camera_rays(_p(f), _p(a), _p(u), float(vfov), W, H, _p(out))
+    return out
+
+
+def shade(rays: np.ndarray, hits: np.ndarray) -> np.ndarray:
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    hits = np.ascontiguousarray(hits, HIT_DTYPE)
+    out = np.zeros((rays.shape[0], 3), np.uint8)
+    lib().hor_shade(_p(rays), _p(hits), rays.shape[0], _p(out))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# reference shim (only where oracle/_ref was built from the reference sources)
+# ---------------------------------------------------------------------------
+_ref = None
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        L = C.CDLL(str(REF_SO))
+        vp, i32, i64, f32 = C.c_void_p, C.c_int, C.c_int64, C.c_float
+        L.ref_scene_create.restype = vp
+        L.ref_scene_create.argtypes = [i32, vp, vp, vp, i64, vp, vp, vp, i64, vp]
+        L.ref_scene_load.restype = vp
+        L.ref_scene_load.argtypes = [C.c_char_p, C.c_char_p]
+        L.ref_scene_destroy.argtypes = [vp]
+        L.ref_scene_count.argtypes = [vp]
+        L.ref_scene_elem.argtypes = [vp, i32, vp, vp, vp, vp]
+        L.ref_scene_geom.restype = i64
+        L.ref_scene_geom.argtypes = [vp, vp]
+        L.ref_scene_field.restype = i64
+        L.ref_scene_field.argtypes = [vp, vp]
+        L.ref_basis.argtypes = [C.c_uint, f32, vp]
+        L.ref_box.argtypes = [vp, i32, i32, vp]
+        L.ref_map_point.argtypes = [vp, i32, vp, i64, vp]
+        L.ref_eval_point.argtypes = [vp, i32, vp, i64, vp]
+        L.ref_inverse_map.argtypes = [vp, i32, vp, i64, vp]
+        L.ref_find_iso.argtypes = [vp, i32, vp, vp, i64, f32, vp]
+        L.ref_hit_hex.argtypes = [vp, i32, vp, vp, i64, vp]
+        L.ref_trace.argtypes = [vp, vp, i64, f32, vp]
+        L.ref_trace_order.argtypes = [vp, vp, i64, f32, vp, vp, i32, vp]
+        _ref = L
+    return _ref
+
+
+class RefScene:
+    def __init__(self, arrs: SceneArrays | None = None, xml: str | None = None, fld: str | None = None):
+        L = ref()
+        if xml is not None:
+            self.h = L.ref_scene_load(xml.encode(), fld.encode())
+            if not self.h:
+                raise RuntimeError("reference loader failed")
+        else:
+            self.arrs = arrs
+            self.h = L.ref_scene_create(arrs.n, _p(arrs.geom_modes), _p(arrs.geom_offset), _p(arrs.geom),
+                                        arrs.geom.size, _p(arrs.field_modes), _p(arrs.field_offset),
+                                        _p(arrs.field), arrs.field.size, _p(arrs.verts))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref().ref_scene_destroy(self.h)
+            self.h = None
+
+    def arrays(self) -> SceneArrays:
+        L = ref()
+        n = L.ref_scene_count(self.h)
+        gm = np.zeros((n, 3), np.uint32)
+        fm = np.zeros((n, 3), np.uint32)
+        go = np.zeros(n, np.int64)
+        fo = np.zeros(n, np.int64)
+        verts = np.zeros((n, 8, 3), np.float32)
+        modes6 = np.zeros(6, np.uint32)
+        offs = np.zeros(2, np.int64)
+        v24 = np.zeros(24, np.float32)
+        box = np.zeros(6, np.float32)
+        for i in range(n):
+            L.ref_scene_elem(self.h, i, _p(modes6), _p(offs), _p(v24), _p(box))
+            gm[i] = modes6[:3]
+            fm[i] = modes6[3:]
+            go[i], fo[i] = offs
+            verts[i] = v24.reshape(8, 3)
+        ng = L.ref_scene_geom(self.h, None)
+        geom = np.zeros(ng, np.float32)
+        L.ref_scene_geom(self.h, _p(geom))
+        nf = L.ref_scene_field(self.h, None)
+        field = np.zeros(nf, np.float32)
+        L.ref_scene_field(self.h, _p(field))
+        return SceneArrays(gm, go, geom, fm, fo, field, verts)
+
+    def box(self, elem, samples):
+        out = np.zeros(6, np.float32)
+        ref().ref_box(self.h, elem, samples, _p(out))
+        return out
+
+    def map_point(self, elem, xi):
+        xi = np.ascontiguousarray(xi, np.float32).reshape(-1, 3)
+        out = np.zeros_like(xi)
+        ref().ref_map_point(self.h, elem, _p(xi), xi.shape[0], _p(out))
+        return out
+
+    def eval_point(self, elem, xi):
+        xi = np.ascontiguousarray(xi, np.float32).reshape(-1, 3)
+        out = np.zeros((xi.shape[0], 13), np.float32)
+        ref().ref_eval_point(self.h, elem, _p(xi), xi.shape[0], _p(out))
+        return out
+
+    def inverse_map(self, elem, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 3)
+        out = np.zeros((x.shape[0], 4), np.float32)
+        ref().ref_inverse_map(self.h, elem, _p(x), x.shape[0], _p(out))
+        return out
+
+    def find_iso(self, elem, rays, seg, iso):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        seg = np.ascontiguousarray(seg, np.float32).reshape(-1, 2)
+        out = np.zeros((rays.shape[0], 8), np.float32)
+        ref().ref_find_iso(self.h, elem, _p(rays), _p(seg), rays.shape[0], float(iso), _p(out))
+        return out
+
+    def hit_hex(self, elem, rays, seg):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        seg = np.ascontiguousarray(seg, np.float32).reshape(-1, 2)
+        out = np.zeros((rays.shape[0], 6), np.float32)
+        ref().ref_hit_hex(self.h, elem, _p(rays), _p(seg), rays.shape[0], _p(out))
+        return out
+
+    def trace(self, rays, iso, order_cap: int = 0):
+        """Reference traversal; returns (n x 12 results) or, with order_cap > 0,
+        (results, visit order n x order_cap, visit counts)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        out = np.zeros((rays.shape[0], 12), np.float32)
+        if order_cap <= 0:
+            ref().ref_trace(self.h, _p(rays), rays.shape[0], float(iso), _p(out))
+            return out
+        order = np.zeros((rays.shape[0], order_cap), np.int32)
+        cnt = np.zeros(rays.shape[0], np.int32)
+        ref().ref_trace_order(self.h, _p(rays), rays.shape[0], float(iso), _p(out), _p(order), order_cap, _p(cnt))
+        return out, order, cnt
+
+
+def ref_basis(nmodes: int, x: float) -> np.ndarray:
+    out = np.zeros((nmodes, 2), np.float32)
+    ref().ref_basis(nmodes, float(x), _p(out))
+    return out
