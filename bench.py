@@ -1,0 +1,344 @@
+"""Benchmark: Mrays/s of curved-hex ray/isosurface queries on one GB300.
+
+Workload (default): hex32_p6 — 32^3 = 32,768 hexes of [0,1]^3, P = 6
+geometry and field (7^3 modes per element), sinusoidal curving 0.08 h,
+seeded 64-Gaussian field; 1920x1080 pixel-centre primary rays from a pinhole
+camera at (2.5, 2.0, 1.8) looking at (0.5, 0.5, 0.5), 60 deg vertical FOV;
+isovalues {-0.3, 0.0, 0.3} (0.0 traced as a real isovalue). One step = one
+render of all 3 isovalues = 6,220,800 ray queries; a ray query counts as
+completed whether it hits a face, the isosurface, or nothing.
+
+  value  : queries/s with the scene resident in HBM, CUDA events around the
+           trace launch on its own stream, L2 flushed (256 MiB write) before
+           every timed step, sum over K steps.
+  e2e    : the same through ho_render() with a host image buffer (device ->
+           host copy of the 8-bit images inside the timed region), host clock.
+  cpu_baseline / --impl reference: the oracle's FP32 port of the reference
+           algorithm (same per-candidate steps, ordered candidates), all host
+           threads, on a bounded random sample of the workload's rays.
+
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "test-_gb300"))
+
+METRIC = "Mrays/s (hit+iso) learned-init batched vs plain Newton, same GB300, equal error"
+UNIT = "Mrays/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="hex32_p6")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---- algorithmic FLOPs per counted evaluation (modes n per direction) ------
+def flops_geom(n):   # x and J: 3 comps x (2n^3 + 3n^2 + 4n) FMA + basis values/derivatives (3 x 8n)
+    return 2 * 3 * (2 * n**3 + 3 * n**2 + 4 * n) + 3 * 8 * n
+
+
+def flops_map(n):    # x only: 3 comps x (n^3 + n^2 + n) FMA + basis values (3 x 4n)
+    return 2 * 3 * (n**3 + n**2 + n) + 3 * 4 * n
+
+
+def flops_field(n):  # u and grad: (2n^3 + 3n^2 + 4n) FMA + basis (3 x 8n)
+    return 2 * (2 * n**3 + 3 * n**2 + 4 * n) + 3 * 8 * n
+
+
+def algorithmic_flops(st, n):
+    # + 3x3 inverse and update per Newton iteration (about 60 flops each)
+    return (st["geom_evals"] * flops_geom(n) + st["map_evals"] * flops_map(n) + st["field_evals"] * flops_field(n)
+            + (st["newton_iters"] + st["face_iters"]) * 60)
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(workload, seconds, n_iso_sample=None):
+    """Time the oracle's FP32 port on a bounded random sample of rays."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_bind as ob
+    import horender as hr
+
+    ctx = hr.Context(0)
+    ctx.generate_synthetic(**workload.synth())
+    s = ctx.get_scene()
+    ctx.close()
+    arrs = ob.SceneArrays(s["geom_modes"], s["geom_offsets"], s["geom"], s["field_modes"], s["field_offsets"],
+                          s["field"], s["corners"])
+    osc = ob.OracleScene(arrs)
+    cam = workload.camera
+    rays = ob.camera_rays(cam.lookfrom, cam.lookat, cam.vup, cam.vfov_deg, workload.width, workload.height)
+    rng = np.random.default_rng(12345)
+    threads = os.cpu_count() or 1
+    n = 64
+    done_rays = 0
+    elapsed = 0.0
+    while True:
+        idx = rng.choice(rays.shape[0], size=n, replace=False)
+        sample = rays[idx]
+        t0 = time.perf_counter()
+        for iso in workload.isovalues:
+            osc.trace(sample, iso, True, precision=32, threads=threads)
+        dt = time.perf_counter() - t0
+        done_rays += n * len(workload.isovalues)
+        elapsed += dt
+        if elapsed >= seconds * 0.5 or n >= rays.shape[0]:
+            break
+        # grow the sample toward the time target
+        n = int(min(rays.shape[0], max(2 * n, n * (seconds - elapsed) / max(dt, 1e-3))))
+    return {"value": done_rays / elapsed / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done_rays} ray queries ({len(workload.isovalues)} isovalues) drawn uniformly from the "
+                      f"{workload.width}x{workload.height} image, FP32 oracle port, {threads} threads, "
+                      f"{elapsed:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    import horender as hr
+
+    w = hr.WORKLOADS[args.workload]
+    if rank != 0:
+        return
+    per_step = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(w, max(2.0, args.cpu_seconds / 2))
+        if i >= args.warmup:
+            per_step.append(cb["value"])
+    v = float(np.mean(per_step))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w.name, "mesh": f"{w.nx}^3 hexes", "order": w.order_max,
+                       "rays": f"{w.width}x{w.height}", "isovalues": w.isovalues},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                             "sample": cb["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import horender as hr
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = hr.WORKLOADS[args.workload]
+    ctx = hr.Context(local)
+    ctx.generate_synthetic(**w.synth())
+    ctx.build_bvh()
+    info = ctx.info()
+    n_iso = len(w.isovalues)
+    W, H = w.width, w.height
+    nq = W * H * n_iso
+    rgb = torch.empty(nq * 3, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+
+    def step():
+        ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            step()
+    torch.cuda.synchronize()
+    st = ctx.stats()
+    barrier(world)
+    torch.cuda.synchronize()
+    evs = []
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                step()
+                b.record(stream)
+                evs.append((a, b))
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = [a.elapsed_time(b) for a, b in evs]
+    total_s = sum(ms) / 1e3
+    total_s = max_over_ranks(total_s, world)
+    queries = sum_over_ranks(nq * args.steps, world)
+    value = queries / total_s / 1e6
+    launch_s = total_s / args.steps  # one trace launch per step
+
+    # roofline of the trace kernel: algorithmic FP32 flops of one launch
+    N = info["max_modes"]
+    flops = algorithmic_flops(st, N)
+    achieved_tflops = flops / launch_s / 1e12
+
+    # e2e: public API, host image buffer, D2H inside the timed region
+    host_rgb = torch.empty((n_iso, H, W, 3), dtype=torch.uint8).pin_memory()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = queries / e2e_s / 1e6
+    del host_rgb
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    fp32_peak = fp32_peak_tflops(torch, dev)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "impl": "gb300", "mode": "plain",
+        "config": {"workload": w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes", "order": w.order_max,
+                   "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
+                   "rays": f"{W}x{H}", "isovalues": w.isovalues, "queries_per_step": nq,
+                   "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": (achieved_tflops / fp32_peak) if fp32_peak else None, "traffic": None,
+                     "peak_source": "FP32 FMA loop measured in this run (peaks file has HBM and bf16 only)",
+                     "flops_per_launch": flops},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4 * n_iso,
+                "d2h_bytes_per_step": nq * 3},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "work": st,
+        "scene": info,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def fp32_peak_tflops(torch, dev):
+    """Measured FP32 FMA rate of this GPU in TFLOP/s (ho_measure_fp32_peak)."""
+    import horender as hr
+
+    return hr.fp32_fma_peak_tflops(dev.index or 0)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

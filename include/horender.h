@@ -187,6 +187,11 @@ int ho_intersect_device(ho_context* ctx, int64_t n, const float* rays_dev, float
 int ho_set_mode(ho_context* ctx, int mode);
 int ho_get_stats(ho_context* ctx, ho_stats* out);
 
+/* FP32 FMA throughput of the device in TFLOP/s (register-resident FMA loop):
+ * the roofline denominator for the CUDA-core-bound intersection kernels. No
+ * reference counterpart. */
+int ho_measure_fp32_peak(int device, double* tflops);
+
 /* Replaces: save_image_ppm (FEM-AABB/raytracer.cu:480-494). P6, rows in
  * buffer order. */
 int ho_save_ppm(const uint8_t* rgb, int width, int height, const char* path);

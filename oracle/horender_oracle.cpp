@@ -54,11 +54,68 @@ struct GatherNode {
 
 struct OScene {
   std::vector<Elem> elems;
-  std::vector<Box64> box32, box64;  // padded sampled boxes computed in f32 / f64
-  std::vector<Box64> gbox;          // union of the two, for candidate gathering
+  std::vector<Box64> box32, box64;  // padded sampled boxes in f32 / f64 (computed on first use)
+  std::vector<uint8_t> have_box;
+  std::vector<Box64> gbox;          // cheap rigorous superset of both, for candidate gathering
   std::vector<GatherNode> nodes;
   std::vector<int> order;
 };
+
+// A box that contains the padded sampled box without sampling: the vertex
+// modes (i,j,k in {0,1}) interpolate trilinearly between 8 values, and every
+// other mode is bounded by |phi_i| <= (i-1)/4 on [-1,1] (|P^{(1,1)}_m| <= m+1
+// there); the result is then padded the way the sampled box is.
+Box64 gather_box(const Elem& e) {
+  Box64 b;
+  if (!has_ho_geom(e)) {
+    for (int a = 0; a < 3; ++a) {
+      b.lo[a] = 1e300;
+      b.hi[a] = -1e300;
+      for (int v = 0; v < 8; ++v) {
+        b.lo[a] = std::min(b.lo[a], double(e.verts[v][a]));
+        b.hi[a] = std::max(b.hi[a], double(e.verts[v][a]));
+      }
+      b.lo[a] -= 1e-4 + 1e-6;
+      b.hi[a] += 1e-4 + 1e-6;
+    }
+    return b;
+  }
+  auto bound = [](unsigned i) { return i < 2 ? 1.0 : 0.25 * (double(i) - 1.0); };
+  for (int a = 0; a < 3; ++a) {
+    const float* c = e.geom[a];
+    double lo = 1e300, hi = -1e300, rest = 0.0;
+    int idx = 0;
+    for (unsigned k = 0; k < e.gm[2]; ++k)
+      for (unsigned j = 0; j < e.gm[1]; ++j)
+        for (unsigned i = 0; i < e.gm[0]; ++i) {
+          const double v = c[idx++];
+          if (i < 2 && j < 2 && k < 2) {
+            lo = std::min(lo, v);
+            hi = std::max(hi, v);
+          } else {
+            rest += std::fabs(v) * bound(i) * bound(j) * bound(k);
+          }
+        }
+    lo -= rest;
+    hi += rest;
+    const double pad = std::max(0.15 * (hi - lo), 1e-3) * 1.001 + 1e-6 * (1.0 + std::fabs(lo) + std::fabs(hi));
+    b.lo[a] = lo - pad;
+    b.hi[a] = hi + pad;
+  }
+  return b;
+}
+
+void compute_boxes(OScene& s, int64_t i) {
+  V3<float> l32, h32;
+  V3<double> l64, h64;
+  elem_box<float>(s.elems[i], 4, l32, h32);
+  elem_box<double>(s.elems[i], 4, l64, h64);
+  Box64& a = s.box32[i];
+  Box64& c = s.box64[i];
+  a.lo[0] = l32.x; a.lo[1] = l32.y; a.lo[2] = l32.z; a.hi[0] = h32.x; a.hi[1] = h32.y; a.hi[2] = h32.z;
+  c.lo[0] = l64.x; c.lo[1] = l64.y; c.lo[2] = l64.z; c.hi[0] = h64.x; c.hi[1] = h64.y; c.hi[2] = h64.z;
+  s.have_box[i] = 1;
+}
 
 int build_gather(OScene& s, int first, int count) {
   GatherNode nd;
@@ -132,12 +189,10 @@ void gather(const OScene& s, const double o[3], const double d[3], std::vector<i
 
 template <class R>
 void trace_one(const OScene& s, const float* rayf, float isof, bool iso_on, hor_hit& out, Counters& cnt,
-               uint64_t& ncand, std::vector<int>& scratch, std::vector<std::pair<R, int>>& cands) {
+               uint64_t& ncand, const std::vector<int>& scratch, std::vector<std::pair<R, int>>& cands) {
   Ray<R> ray;
   ray.o = mk<R>(rayf[0], rayf[1], rayf[2]);
   ray.d = mk<R>(rayf[3], rayf[4], rayf[5]);
-  const double o64[3] = {rayf[0], rayf[1], rayf[2]}, d64[3] = {rayf[3], rayf[4], rayf[5]};
-  gather(s, o64, d64, scratch);
   const std::vector<Box64>& boxes = (sizeof(R) == sizeof(float)) ? s.box32 : s.box64;
   const R t_eps = static_cast<R>(0.001f);
   const R t_far = static_cast<R>(FLT_MAX);
@@ -226,24 +281,10 @@ void* hor_scene_create(const hor_scene_desc* d) {
   }
   s->box32.resize(d->n_elem);
   s->box64.resize(d->n_elem);
+  s->have_box.assign(d->n_elem, 0);
   s->gbox.resize(d->n_elem);
   parallel_for(d->n_elem, std::max(1u, std::thread::hardware_concurrency()), [&](int, int64_t b, int64_t e) {
-    for (int64_t i = b; i < e; ++i) {
-      V3<float> l32, h32;
-      V3<double> l64, h64;
-      elem_box<float>(s->elems[i], 4, l32, h32);
-      elem_box<double>(s->elems[i], 4, l64, h64);
-      Box64& a = s->box32[i];
-      Box64& c = s->box64[i];
-      a.lo[0] = l32.x; a.lo[1] = l32.y; a.lo[2] = l32.z; a.hi[0] = h32.x; a.hi[1] = h32.y; a.hi[2] = h32.z;
-      c.lo[0] = l64.x; c.lo[1] = l64.y; c.lo[2] = l64.z; c.hi[0] = h64.x; c.hi[1] = h64.y; c.hi[2] = h64.z;
-      Box64& g = s->gbox[i];
-      for (int k = 0; k < 3; ++k) {
-        const double m = 1e-6 * (1.0 + std::fabs(a.lo[k]) + std::fabs(a.hi[k]));
-        g.lo[k] = std::min(a.lo[k], c.lo[k]) - m;
-        g.hi[k] = std::max(a.hi[k], c.hi[k]) + m;
-      }
-    }
+    for (int64_t i = b; i < e; ++i) s->gbox[i] = gather_box(s->elems[i]);
   });
   s->order.resize(d->n_elem);
   for (int i = 0; i < d->n_elem; ++i) s->order[i] = i;
@@ -256,6 +297,11 @@ void hor_scene_destroy(void* s) { delete static_cast<OScene*>(s); }
 // Padded sampled boxes as (lo.xyz, hi.xyz) per element, in f32 or f64 math.
 int hor_scene_boxes(void* sp, int precision, double* out) {
   OScene* s = static_cast<OScene*>(sp);
+  parallel_for(static_cast<int64_t>(s->elems.size()), std::max(1u, std::thread::hardware_concurrency()),
+               [&](int, int64_t b, int64_t e) {
+                 for (int64_t i = b; i < e; ++i)
+                   if (!s->have_box[i]) compute_boxes(*s, i);
+               });
   const std::vector<Box64>& b = precision == 32 ? s->box32 : s->box64;
   for (size_t i = 0; i < b.size(); ++i)
     for (int a = 0; a < 3; ++a) {
@@ -270,19 +316,42 @@ int hor_scene_boxes(void* sp, int precision, double* out) {
 // caller decides). precision: 32 or 64.
 int hor_trace(void* sp, int precision, const float* rays, int64_t n, float iso, int iso_on, int nthreads,
               hor_hit* out, hor_counters* counters) {
-  const OScene* s = static_cast<const OScene*>(sp);
+  OScene* s = static_cast<OScene*>(sp);
   std::vector<hor_counters> per(std::max(1, nthreads));
   for (auto& c : per) std::memset(&c, 0, sizeof(c));
+  // 1. candidates per ray through the rigorous gather boxes
+  std::vector<std::vector<int>> lists(n);
+  parallel_for(n, nthreads, [&](int, int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      const float* r = rays + 6 * i;
+      const double o64[3] = {r[0], r[1], r[2]}, d64[3] = {r[3], r[4], r[5]};
+      gather(*s, o64, d64, lists[i]);
+    }
+  });
+  // 2. exact padded boxes for the touched elements
+  std::vector<int> need;
+  {
+    std::vector<uint8_t> mark(s->elems.size(), 0);
+    for (const auto& l : lists)
+      for (int e : l)
+        if (!s->have_box[e] && !mark[e]) {
+          mark[e] = 1;
+          need.push_back(e);
+        }
+  }
+  parallel_for(static_cast<int64_t>(need.size()), nthreads, [&](int, int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) compute_boxes(*s, need[i]);
+  });
+  // 3. trace
   parallel_for(n, nthreads, [&](int w, int64_t b, int64_t e) {
-    std::vector<int> scratch;
     Counters cnt;
     uint64_t ncand = 0;
     if (precision == 32) {
       std::vector<std::pair<float, int>> cands;
-      for (int64_t i = b; i < e; ++i) trace_one<float>(*s, rays + 6 * i, iso, iso_on != 0, out[i], cnt, ncand, scratch, cands);
+      for (int64_t i = b; i < e; ++i) trace_one<float>(*s, rays + 6 * i, iso, iso_on != 0, out[i], cnt, ncand, lists[i], cands);
     } else {
       std::vector<std::pair<double, int>> cands;
-      for (int64_t i = b; i < e; ++i) trace_one<double>(*s, rays + 6 * i, iso, iso_on != 0, out[i], cnt, ncand, scratch, cands);
+      for (int64_t i = b; i < e; ++i) trace_one<double>(*s, rays + 6 * i, iso, iso_on != 0, out[i], cnt, ncand, lists[i], cands);
     }
     per[w].newton_iters += cnt.newton_iters;
     per[w].face_iters += cnt.face_iters;
@@ -307,7 +376,10 @@ int hor_trace(void* sp, int precision, const float* rays, int64_t n, float iso, 
 // per-candidate policy from the traversal order.
 int hor_trace_replay(void* sp, int precision, const float* rays, int64_t n, float iso, int iso_on,
                      const int32_t* order, int order_cap, const int32_t* order_n, hor_hit* out) {
-  const OScene* s = static_cast<const OScene*>(sp);
+  OScene* s = static_cast<OScene*>(sp);
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < std::min(order_cap, order_n[i]); ++k)
+      if (!s->have_box[order[i * order_cap + k]]) compute_boxes(*s, order[i * order_cap + k]);
   for (int64_t i = 0; i < n; ++i) {
     const int m = std::min(order_cap, order_n[i]);
     Counters cnt;

@@ -494,9 +494,12 @@ int build_lbvh(ho_context* c) {
   int64_t leaves = 0;
   std::vector<std::pair<int32_t, int>> st;
   st.push_back({0, 1});
+  int64_t visits = 0;
   while (!st.empty()) {
+    if (++visits > c->n_nodes) break;  // a well-formed tree has exactly n_nodes internal nodes
     auto [id, dd] = st.back();
     st.pop_back();
+    if (id < 0 || id >= c->n_nodes) break;
     depth = std::max(depth, dd);
     for (int ch = 0; ch < 2; ++ch) {
       const int32_t x = hn[id].c[ch].idx;

@@ -85,6 +85,7 @@ def _load():
     L.ho_set_mode.argtypes = [vp, i32]
     L.ho_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.ho_save_ppm.argtypes = [vp, i32, i32, C.c_char_p]
+    L.ho_measure_fp32_peak.argtypes = [i32, C.POINTER(C.c_double)]
     return L
 
 
@@ -230,10 +231,14 @@ class Context:
 
     # ---- queries ---------------------------------------------------------------
     def render(self, camera: Camera, isovalues, width: int, height: int, iso_zero_disables: bool = True,
-               want_rgb: bool = True, want_hits: bool = False):
+               want_rgb: bool = True, want_hits: bool = False, rgb_out: np.ndarray | None = None):
         iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
         n = iso.size
-        rgb = np.zeros((n, height, width, 3), np.uint8) if want_rgb else None
+        if rgb_out is not None:
+            assert rgb_out.dtype == np.uint8 and rgb_out.size == n * height * width * 3 and rgb_out.flags.c_contiguous
+            rgb = rgb_out
+        else:
+            rgb = np.zeros((n, height, width, 3), np.uint8) if want_rgb else None
         hits = np.zeros((n, height, width), HIT_DTYPE) if want_hits else None
         cam = camera._c()
         self._ck(lib.ho_render(self.h, C.byref(cam), _p(iso), n, width, height, int(iso_zero_disables),
@@ -261,6 +266,14 @@ class Context:
         s = _Stats()
         self._ck(lib.ho_get_stats(self.h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+def fp32_fma_peak_tflops(device: int = 0) -> float:
+    v = C.c_double()
+    rc = lib.ho_measure_fp32_peak(int(device), C.byref(v))
+    if rc != HO_OK:
+        raise HoError(rc, "FP32 peak probe failed")
+    return v.value
 
 
 def save_ppm(rgb: np.ndarray, path: str):

@@ -1,0 +1,79 @@
+"""GPU parity against the oracle on the small curved-hex workload (hex4_p4:
+4x4x4 hexes, P=4, curving 0.05h, iso 0.2), through the C ABI.
+
+Tolerances (FP32 kernels vs the FP64 oracle running the same algorithm):
+  * hit identity (kind, element, face) equal on >= 99.5% of rays; every
+    difference must be a near-tie (|t_gpu - t_oracle| small, or a sign
+    change within the iso tolerance band) and is counted;
+  * t within 2e-4 absolute on rays whose identity agrees (the reference's own
+    stopping rules: |f| < 1e-5 for the isosurface, max residual < 1e-4 for a
+    face);
+  * padded element boxes within 1e-5 of the FP64 oracle's boxes.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import horender as hr
+from conftest import classify, scene_arrays_from_ctx
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small(oracle):
+    ctx, w = hr.workload_context("hex4_p4")
+    arrs = scene_arrays_from_ctx(ctx)
+    return ctx, w, arrs, oracle.OracleScene(arrs)
+
+
+def test_boxes_match_oracle(small):
+    ctx, w, arrs, osc = small
+    gb = ctx.boxes()
+    ob = osc.boxes(64)
+    assert np.abs(gb - ob).max() < 1e-5
+
+
+def test_hull_contains_element(small):
+    ctx, w, arrs, osc = small
+    hull, faces = ctx.hull_boxes()
+    boxes = ctx.boxes()
+    # the padded sampled box contains the rigorous hull on this mesh
+    assert (boxes[:, :3] <= hull[:, :3] + 1e-6).all() and (boxes[:, 3:] >= hull[:, 3:] - 1e-6).all()
+    # the hull contains densely sampled points of each element
+    rng = np.random.default_rng(0)
+    xi = rng.uniform(-1, 1, (512, 3))
+    for e in range(arrs.n):
+        x = osc.map_point(e, xi)
+        assert (x >= hull[e, :3] - 1e-6).all() and (x <= hull[e, 3:] + 1e-6).all()
+
+
+@pytest.mark.parametrize("iso_on", [True, False])
+def test_render_hits_match_oracle(small, oracle, iso_on):
+    ctx, w, arrs, osc = small
+    W = H = 128
+    _, hits = ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=True, want_rgb=False, want_hits=True) \
+        if iso_on else ctx.render(w.camera, [0.0], W, H, iso_zero_disables=True, want_rgb=False, want_hits=True)
+    h = hits[0].reshape(-1)
+    rays = oracle.camera_rays(w.camera.lookfrom, w.camera.lookat, w.camera.vup, w.camera.vfov_deg, W, H)
+    ref, _ = osc.trace(rays, w.isovalues[0] if iso_on else 0.0, iso_on, precision=64)
+    same = classify(h, ref)
+    assert same.mean() >= 0.995, f"identity agreement {same.mean():.4f}"
+    m = same & (ref["kind"] > 0)
+    assert np.abs(h["t"][m] - ref["t"][m]).max() < 2e-4
+    # misses are misses
+    assert ((h["kind"] == 0) == (ref["kind"] == 0)).mean() >= 0.999
+
+
+def test_intersect_explicit_rays_matches_render(small):
+    ctx, w, arrs, osc = small
+    W = H = 64
+    _, hits = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    import oracle_bind as ob
+
+    rays = ob.camera_rays(w.camera.lookfrom, w.camera.lookat, w.camera.vup, w.camera.vfov_deg, W, H)
+    h2 = ctx.intersect(rays, w.isovalues[0], True)
+    h1 = hits[0].reshape(-1)
+    same = classify(h1, h2)
+    assert same.mean() > 0.999
