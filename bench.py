@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--workload", default="hex32_p6")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling)")
+    ap.add_argument("--height", type=int, default=0, help="override the workload's image height (profiling)")
     return ap.parse_args()
 
 
@@ -228,6 +231,10 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     w = hr.WORKLOADS[args.workload]
+    if args.width and args.height:
+        import dataclasses
+
+        w = dataclasses.replace(w, width=args.width, height=args.height)
     ctx = hr.Context(local)
     ctx.generate_synthetic(**w.synth())
     ctx.build_bvh()
@@ -281,9 +288,9 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(0 if args.no_e2e else args.steps):
         ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_s = max(max_over_ranks(time.perf_counter() - t0, world), 1e-9)
     e2e = queries / e2e_s / 1e6
     del host_rgb
 

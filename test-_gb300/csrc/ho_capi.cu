@@ -157,6 +157,8 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_hits);
     cudaFree(c->d_rgb);
     cudaFree(c->d_rays);
+    cudaFree(c->d_work);
+    cudaFree(c->d_qctr);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     cudaStreamDestroy(c->stream);
   }

@@ -100,21 +100,40 @@ __device__ __forceinline__ void basis_val_der(float x, float (&a)[N], float (&d)
 
 // ---------------------------------------------------------------------------
 // Sum-factorised tensor contractions. Coefficient index ((k*N)+j)*N+i,
-// i fastest (HexElement.cu:14-26). One component.
+// i fastest (HexElement.cu:14-26). One component per call.
+//
+// Code size matters more than call overhead here: a fully unrolled N^3
+// contraction is thousands of instructions, and inlining it at every call
+// site overflows the instruction cache. So the i and j loops are unrolled
+// (basis values in registers), the k loop is rolled (its basis values come
+// from the caller's per-lane local array), and the routines are out of line.
 // ---------------------------------------------------------------------------
-
-// value and the three reference-space partials
 template <int N>
-__device__ __forceinline__ void contract_vd(const float* __restrict__ c, const float (&ar)[N], const float (&dr)[N],
-                                            const float (&as)[N], const float (&ds)[N], const float (&at)[N],
-                                            const float (&dt)[N], float& v, float& vr, float& vs, float& vt) {
-  v = vr = vs = vt = 0.0f;
+struct Basis {
+  float ar[N], dr[N], as[N], ds[N], at[N], dt[N];
+};
+
+// value and the three reference-space partials: out = {v, dv/dr, dv/ds, dv/dt}
+template <int N>
+__device__ __noinline__ void contract_vd(const float* __restrict__ c, const Basis<N>* __restrict__ B,
+                                         float* __restrict__ out) {
+  float ar[N], dr[N], as[N], ds[N];
 #pragma unroll
+  for (int i = 0; i < N; ++i) {
+    ar[i] = B->ar[i];
+    dr[i] = B->dr[i];
+    as[i] = B->as[i];
+    ds[i] = B->ds[i];
+  }
+  float v = 0.f, vr = 0.f, vs = 0.f, vt = 0.f;
+#pragma unroll 1
   for (int k = 0; k < N; ++k) {
+    const float tk = B->at[k], dtk = B->dt[k];
+    const float* ck = c + k * N * N;
     float q0 = 0.f, q1 = 0.f, q2 = 0.f;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const float* row = c + (k * N + j) * N;
+      const float* row = ck + j * N;
       float s0 = 0.f, s1 = 0.f;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
@@ -126,30 +145,41 @@ __device__ __forceinline__ void contract_vd(const float* __restrict__ c, const f
       q1 = fmaf(s1, as[j], q1);
       q2 = fmaf(s0, ds[j], q2);
     }
-    v = fmaf(q0, at[k], v);
-    vr = fmaf(q1, at[k], vr);
-    vs = fmaf(q2, at[k], vs);
-    vt = fmaf(q0, dt[k], vt);
+    v = fmaf(q0, tk, v);
+    vr = fmaf(q1, tk, vr);
+    vs = fmaf(q2, tk, vs);
+    vt = fmaf(q0, dtk, vt);
   }
+  out[0] = v;
+  out[1] = vr;
+  out[2] = vs;
+  out[3] = vt;
 }
 
 // value only
 template <int N>
-__device__ __forceinline__ float contract_v(const float* __restrict__ c, const float (&ar)[N], const float (&as)[N],
-                                            const float (&at)[N]) {
-  float v = 0.0f;
+__device__ __noinline__ float contract_v(const float* __restrict__ c, const Basis<N>* __restrict__ B) {
+  float ar[N], as[N];
 #pragma unroll
+  for (int i = 0; i < N; ++i) {
+    ar[i] = B->ar[i];
+    as[i] = B->as[i];
+  }
+  float v = 0.0f;
+#pragma unroll 1
   for (int k = 0; k < N; ++k) {
+    const float tk = B->at[k];
+    const float* ck = c + k * N * N;
     float q0 = 0.f;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const float* row = c + (k * N + j) * N;
+      const float* row = ck + j * N;
       float s0 = 0.f;
 #pragma unroll
       for (int i = 0; i < N; ++i) s0 = fmaf(__ldg(row + i), ar[i], s0);
       q0 = fmaf(s0, as[j], q0);
     }
-    v = fmaf(q0, at[k], v);
+    v = fmaf(q0, tk, v);
   }
   return v;
 }
@@ -163,50 +193,79 @@ struct Elem {
   __device__ __forceinline__ const float* fld() const { return c + 3 * N * N * N; }
 };
 
-// x(xi) and J (row-major J[row=x,y,z][col=r,s,t]) in one pass.
+// x(xi) and J (row-major J[row=x,y,z][col=r,s,t]).
+template <int N>
+__device__ __noinline__ void geom_eval_raw(const float* __restrict__ c, float3 xi, float* __restrict__ xJ) {
+  Basis<N> B;
+  basis_val_der<N>(xi.x, B.ar, B.dr);
+  basis_val_der<N>(xi.y, B.as, B.ds);
+  basis_val_der<N>(xi.z, B.at, B.dt);
+  constexpr int S = N * N * N;
+#pragma unroll 1
+  for (int comp = 0; comp < 3; ++comp) contract_vd<N>(c + comp * S, &B, xJ + 4 * comp);
+}
+
 template <int N>
 __device__ __forceinline__ void geom_eval(const Elem<N>& e, float3 xi, float3& x, float (&J)[9], Work& w) {
-  float ar[N], dr[N], as[N], ds[N], at[N], dt[N];
-  basis_val_der<N>(xi.x, ar, dr);
-  basis_val_der<N>(xi.y, as, ds);
-  basis_val_der<N>(xi.z, at, dt);
-  constexpr int S = N * N * N;
-  contract_vd<N>(e.c, ar, dr, as, ds, at, dt, x.x, J[0], J[1], J[2]);
-  contract_vd<N>(e.c + S, ar, dr, as, ds, at, dt, x.y, J[3], J[4], J[5]);
-  contract_vd<N>(e.c + 2 * S, ar, dr, as, ds, at, dt, x.z, J[6], J[7], J[8]);
+  float r[12];
+  geom_eval_raw<N>(e.c, xi, r);
+  x = make_float3(r[0], r[4], r[8]);
+  J[0] = r[1]; J[1] = r[2]; J[2] = r[3];
+  J[3] = r[5]; J[4] = r[6]; J[5] = r[7];
+  J[6] = r[9]; J[7] = r[10]; J[8] = r[11];
   ++w.geom;
 }
 
 template <int N>
-__device__ __forceinline__ float3 geom_map(const Elem<N>& e, float3 xi, Work& w) {
-  float ar[N], as[N], at[N];
-  basis_val<N>(xi.x, ar);
-  basis_val<N>(xi.y, as);
-  basis_val<N>(xi.z, at);
+__device__ __noinline__ float3 geom_map_raw(const float* __restrict__ c, float3 xi) {
+  Basis<N> B;
+  basis_val<N>(xi.x, B.ar);
+  basis_val<N>(xi.y, B.as);
+  basis_val<N>(xi.z, B.at);
   constexpr int S = N * N * N;
+  const float x = contract_v<N>(c, &B);
+  const float y = contract_v<N>(c + S, &B);
+  const float z = contract_v<N>(c + 2 * S, &B);
+  return make_float3(x, y, z);
+}
+
+template <int N>
+__device__ __forceinline__ float3 geom_map(const Elem<N>& e, float3 xi, Work& w) {
   ++w.map;
-  return make_float3(contract_v<N>(e.c, ar, as, at), contract_v<N>(e.c + S, ar, as, at),
-                     contract_v<N>(e.c + 2 * S, ar, as, at));
+  return geom_map_raw<N>(e.c, xi);
 }
 
 // u(xi) and grad_xi u
 template <int N>
+__device__ __noinline__ void field_eval_raw(const float* __restrict__ c, float3 xi, float* __restrict__ ug) {
+  Basis<N> B;
+  basis_val_der<N>(xi.x, B.ar, B.dr);
+  basis_val_der<N>(xi.y, B.as, B.ds);
+  basis_val_der<N>(xi.z, B.at, B.dt);
+  contract_vd<N>(c, &B, ug);
+}
+
+template <int N>
 __device__ __forceinline__ void field_eval(const Elem<N>& e, float3 xi, float& u, float3& g, Work& w) {
-  float ar[N], dr[N], as[N], ds[N], at[N], dt[N];
-  basis_val_der<N>(xi.x, ar, dr);
-  basis_val_der<N>(xi.y, as, ds);
-  basis_val_der<N>(xi.z, at, dt);
-  contract_vd<N>(e.fld(), ar, dr, as, ds, at, dt, u, g.x, g.y, g.z);
+  float r[4];
+  field_eval_raw<N>(e.fld(), xi, r);
+  u = r[0];
+  g = make_float3(r[1], r[2], r[3]);
   ++w.field;
 }
 
 template <int N>
+__device__ __noinline__ float field_value_raw(const float* __restrict__ c, float3 xi) {
+  Basis<N> B;
+  basis_val<N>(xi.x, B.ar);
+  basis_val<N>(xi.y, B.as);
+  basis_val<N>(xi.z, B.at);
+  return contract_v<N>(c, &B);
+}
+
+template <int N>
 __device__ __forceinline__ float field_value(const Elem<N>& e, float3 xi) {
-  float ar[N], as[N], at[N];
-  basis_val<N>(xi.x, ar);
-  basis_val<N>(xi.y, as);
-  basis_val<N>(xi.z, at);
-  return contract_v<N>(e.fld(), ar, as, at);
+  return field_value_raw<N>(e.fld(), xi);
 }
 
 // Adjugate / determinant inverse, no singular guard (HexElement.cu:208-225).
@@ -280,9 +339,48 @@ __device__ __forceinline__ bool sample_along(const Elem<N>& e, float3 o, float3 
   return true;
 }
 
-// First sign change over 17 uniform samples of [t0,t1], then at most 20
-// safeguarded Newton/bisection steps, done when |f| < 1e-5
-// (RayIsosurface.cu:67-188).
+// At most 20 safeguarded Newton/bisection steps on a bracket [lt, rt] whose
+// left sample is ls; done when |f| < 1e-5, else the midpoint with the left
+// sample's xi and gradient (RayIsosurface.cu:121-177).
+template <int N>
+__device__ __forceinline__ bool refine_bracket(const Elem<N>& e, float3 o, float3 d, float iso, float lt, float rt,
+                                               Sample ls, float& th, float3& xh, float3& gh, Work& w) {
+  for (int it = 0; it < 20; ++it) {
+    const float mt = 0.5f * (lt + rt);
+    Sample ms;
+    if (!sample_along<N>(e, o, d, mt, iso, ms, w)) return false;
+    float ct = mt;
+    if (fabsf(ms.df) > 1e-8f) {
+      const float nt = mt - ms.f / ms.df;
+      if (nt > lt && nt < rt) ct = nt;
+    }
+    Sample cs;
+    if (!sample_along<N>(e, o, d, ct, iso, cs, w)) {
+      ct = mt;  // keep the failed solve's xi, as the reference does
+      cs.f = ms.f;
+      cs.g = ms.g;
+    }
+    if (fabsf(cs.f) < 1e-5f) {
+      th = ct;
+      xh = cs.xi;
+      gh = cs.g;
+      return true;
+    }
+    if (ls.f * cs.f <= 0.0f) {
+      rt = ct;
+    } else {
+      lt = ct;
+      ls = cs;
+    }
+  }
+  th = 0.5f * (lt + rt);
+  xh = ls.xi;
+  gh = ls.g;
+  return true;
+}
+
+// First sign change over 17 uniform samples of [t0,t1], then the bracket
+// refinement (RayIsosurface.cu:67-188). One thread.
 template <int N>
 __device__ bool find_iso(const Elem<N>& e, float3 o, float3 d, float t0, float t1, float iso, float& th, float3& xh,
                          float3& gh, Work& w) {
@@ -302,46 +400,53 @@ __device__ bool find_iso(const Elem<N>& e, float3 o, float3 d, float t0, float t
       sp = s;
       continue;
     }
-    if (sp.f * s.f <= 0.0f) {
-      float lt = tp, rt = t;
-      Sample ls = sp;
-      for (int it = 0; it < 20; ++it) {
-        const float mt = 0.5f * (lt + rt);
-        Sample ms;
-        if (!sample_along<N>(e, o, d, mt, iso, ms, w)) return false;
-        float ct = mt;
-        if (fabsf(ms.df) > 1e-8f) {
-          const float nt = mt - ms.f / ms.df;
-          if (nt > lt && nt < rt) ct = nt;
-        }
-        Sample cs;
-        if (!sample_along<N>(e, o, d, ct, iso, cs, w)) {
-          ct = mt;  // keep the failed solve's xi, as the reference does
-          cs.f = ms.f;
-          cs.g = ms.g;
-        }
-        if (fabsf(cs.f) < 1e-5f) {
-          th = ct;
-          xh = cs.xi;
-          gh = cs.g;
-          return true;
-        }
-        if (ls.f * cs.f <= 0.0f) {
-          rt = ct;
-        } else {
-          lt = ct;
-          ls = cs;
-        }
-      }
-      th = 0.5f * (lt + rt);
-      xh = ls.xi;
-      gh = ls.g;
-      return true;
-    }
+    if (sp.f * s.f <= 0.0f) return refine_bracket<N>(e, o, d, iso, tp, t, sp, th, xh, gh, w);
     tp = t;
     sp = s;
   }
   return false;
+}
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float3 shfl3(float3 v, int src) {
+  return make_float3(__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src));
+}
+
+// Warp version: the 17 samples are independent inverse-map solves, so lane i
+// solves sample i; the first sample i (in order) that succeeded and whose
+// previous successful sample has f(prev)*f(i) <= 0 is found with ballots —
+// the same bracket the sequential scan stops at. The refinement is then run
+// by every lane on identical data (uniform control flow); its work is
+// counted in wu, which only lane 0 reports. Call with all 32 lanes.
+template <int N>
+__device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, float t1, float iso, float& th,
+                              float3& xh, float3& gh, Work& w, Work& wu) {
+  const int lane = threadIdx.x & 31;
+  Sample s;
+  s.f = 0.f;
+  s.df = 0.f;
+  s.xi = make_float3(0.f, 0.f, 0.f);
+  s.g = s.xi;
+  const float t = t0 + (t1 - t0) * (float(lane) / 16.0f);
+  bool ok = false;
+  if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w);
+  const unsigned okm = __ballot_sync(kFull, ok);
+  const unsigned below = okm & ((1u << lane) - 1u);
+  const int prev = below ? 31 - __clz(below) : lane;
+  const float pf = __shfl_sync(kFull, s.f, prev);
+  const bool sc = ok && below != 0u && pf * s.f <= 0.0f;
+  const unsigned scm = __ballot_sync(kFull, sc);
+  if (scm == 0u) return false;
+  const int ri = __ffs(scm) - 1;
+  const int li = 31 - __clz(okm & ((1u << ri) - 1u));
+  const float lt = __shfl_sync(kFull, t, li), rt = __shfl_sync(kFull, t, ri);
+  Sample ls;
+  ls.f = __shfl_sync(kFull, s.f, li);
+  ls.df = __shfl_sync(kFull, s.df, li);
+  ls.xi = shfl3(s.xi, li);
+  ls.g = shfl3(s.g, li);
+  return refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu);
 }
 
 // Slab test clipped to [tmin, tmax] (high_order.h:115-152).
@@ -388,64 +493,71 @@ __device__ __forceinline__ void setc(float3& v, int a, float s) {
   else v.z = s;
 }
 
-// Ray against one curved face: (u,v,tau) Newton from the 9 seeds
-// {-0.8,0,0.8}^2, at most 50 iterations, accept when max|X-Y| < 1e-4 with
-// u,v in [-1.001,1.001] and tau in [tmin,tmax]; step clamp 0.25,
-// divergence break after 5 iterations (high_order.h:189-304).
+// One seed of the ray / curved-face Newton in (u,v,tau): at most 50
+// iterations, accept when max|X-Y| < 1e-4 with u,v in [-1.001,1.001] and tau
+// in [tmin,tmax]; step clamp 0.25, divergence break after 5 iterations
+// (high_order.h:213-300).
 template <int N>
-__device__ bool hit_face(const Elem<N>& e, float3 o, float3 d, int f, float tmin, float tmax, float& th, float3& xh,
-                         Work& w) {
+__device__ bool face_seed(const Elem<N>& e, float3 o, float3 d, int f, int si, int sj, float tmin, float tmax,
+                          float& th, float3& xh, Work& w) {
   int fixed, ua, va;
   float val;
   face_param(f, fixed, val, ua, va);
   const float dd = d.x * d.x + d.y * d.y + d.z * d.z;
-  for (int sj = 0; sj < 3; ++sj) {
-    for (int si = 0; si < 3; ++si) {
-      float3 p = make_float3(0.f, 0.f, 0.f);
-      setc(p, fixed, val);
-      setc(p, ua, si == 0 ? -0.8f : (si == 1 ? 0.0f : 0.8f));
-      setc(p, va, sj == 0 ? -0.8f : (sj == 1 ? 0.0f : 0.8f));
-      const float3 x0 = geom_map<N>(e, p, w);
-      const float3 df = make_float3(x0.x - o.x, x0.y - o.y, x0.z - o.z);
-      float tau = dd > 0.f ? (df.x * d.x + df.y * d.y + df.z * d.z) / dd : 0.f;
-      tau = fminf(fmaxf(tau, tmin), tmax);
-      float prev = FLT_MAX;
-      for (int it = 0; it < 50; ++it) {
-        ++w.face;
-        float3 X;
-        float J[9];
-        geom_eval<N>(e, p, X, J, w);
-        const float rx = X.x - (o.x + tau * d.x), ry = X.y - (o.y + tau * d.y), rz = X.z - (o.z + tau * d.z);
-        const float m = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));
-        if (m < 1e-4f) {
-          const float pu = getc(p, ua), pv = getc(p, va);
-          if (pu >= -1.001f && pu <= 1.001f && pv >= -1.001f && pv <= 1.001f && tau >= tmin && tau <= tmax) {
-            th = tau;
-            xh = p;
-            return true;
-          }
-          break;
-        }
-        if (it > 5 && m > prev * 1.5f) break;
-        prev = m;
-        const float A[9] = {J[ua], J[va], -d.x, J[3 + ua], J[3 + va], -d.y, J[6 + ua], J[6 + va], -d.z};
-        float K[9];
-        invert3(A, K);
-        const float du = -(K[0] * rx + K[1] * ry + K[2] * rz);
-        const float dv = -(K[3] * rx + K[4] * ry + K[5] * rz);
-        const float dtau = -(K[6] * rx + K[7] * ry + K[8] * rz);
-        const float mx = fmaxf(fabsf(du), fmaxf(fabsf(dv), fabsf(dtau)));
-        const float sc = mx > 0.25f ? 0.25f / mx : 1.0f;
-        float nu = getc(p, ua) + du * sc, nv = getc(p, va) + dv * sc;
-        tau = fminf(fmaxf(tau + dtau * sc, tmin), tmax);
-        nu = fminf(fmaxf(nu, -1.5f), 1.5f);
-        nv = fminf(fmaxf(nv, -1.5f), 1.5f);  // fminf/fmaxf drop a NaN, as on the host
-        setc(p, ua, nu);
-        setc(p, va, nv);
-        setc(p, fixed, val);
+  float3 p = make_float3(0.f, 0.f, 0.f);
+  setc(p, fixed, val);
+  setc(p, ua, si == 0 ? -0.8f : (si == 1 ? 0.0f : 0.8f));
+  setc(p, va, sj == 0 ? -0.8f : (sj == 1 ? 0.0f : 0.8f));
+  const float3 x0 = geom_map<N>(e, p, w);
+  const float3 df = make_float3(x0.x - o.x, x0.y - o.y, x0.z - o.z);
+  float tau = dd > 0.f ? (df.x * d.x + df.y * d.y + df.z * d.z) / dd : 0.f;
+  tau = fminf(fmaxf(tau, tmin), tmax);
+  float prev = FLT_MAX;
+  for (int it = 0; it < 50; ++it) {
+    ++w.face;
+    float3 X;
+    float J[9];
+    geom_eval<N>(e, p, X, J, w);
+    const float rx = X.x - (o.x + tau * d.x), ry = X.y - (o.y + tau * d.y), rz = X.z - (o.z + tau * d.z);
+    const float m = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));
+    if (m < 1e-4f) {
+      const float pu = getc(p, ua), pv = getc(p, va);
+      if (pu >= -1.001f && pu <= 1.001f && pv >= -1.001f && pv <= 1.001f && tau >= tmin && tau <= tmax) {
+        th = tau;
+        xh = p;
+        return true;
       }
+      return false;
     }
+    if (it > 5 && m > prev * 1.5f) return false;
+    prev = m;
+    const float A[9] = {J[ua], J[va], -d.x, J[3 + ua], J[3 + va], -d.y, J[6 + ua], J[6 + va], -d.z};
+    float K[9];
+    invert3(A, K);
+    const float du = -(K[0] * rx + K[1] * ry + K[2] * rz);
+    const float dv = -(K[3] * rx + K[4] * ry + K[5] * rz);
+    const float dtau = -(K[6] * rx + K[7] * ry + K[8] * rz);
+    const float mx = fmaxf(fabsf(du), fmaxf(fabsf(dv), fabsf(dtau)));
+    const float sc = mx > 0.25f ? 0.25f / mx : 1.0f;
+    float nu = getc(p, ua) + du * sc, nv = getc(p, va) + dv * sc;
+    tau = fminf(fmaxf(tau + dtau * sc, tmin), tmax);
+    nu = fminf(fmaxf(nu, -1.5f), 1.5f);  // fminf/fmaxf drop a NaN, as on the host
+    nv = fminf(fmaxf(nv, -1.5f), 1.5f);
+    setc(p, ua, nu);
+    setc(p, va, nv);
+    setc(p, fixed, val);
   }
+  return false;
+}
+
+// Ray against one curved face: the 9 seeds {-0.8,0,0.8}^2 in order (v outer,
+// u inner); the first seed accepted answers (high_order.h:189-304).
+template <int N>
+__device__ bool hit_face(const Elem<N>& e, float3 o, float3 d, int f, float tmin, float tmax, float& th, float3& xh,
+                         Work& w) {
+  for (int sj = 0; sj < 3; ++sj)
+    for (int si = 0; si < 3; ++si)
+      if (face_seed<N>(e, o, d, f, si, sj, tmin, tmax, th, xh, w)) return true;
   return false;
 }
 
@@ -530,6 +642,119 @@ __device__ void visit_candidate(const Elem<N>& e, const float* __restrict__ fbox
       float3 x;
       float J[9];
       geom_eval<N>(e, xi, x, J, w);
+      const float3 dr = make_float3(J[0], J[3], J[6]), ds = make_float3(J[1], J[4], J[7]),
+                   dt = make_float3(J[2], J[5], J[8]);
+      float3 n;
+      if (fabsf(xi.x) > 0.9f) n = cross3(ds, dt);
+      else if (fabsf(xi.y) > 0.9f) n = cross3(dr, dt);
+      else n = cross3(dr, ds);
+      n = normalize3(n);
+      if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+      best.t = th;
+      best.elem = eidx;
+      best.face = face;
+      best.kind = HO_HIT_FACE;
+      best.xi = xi;
+      best.n = n;
+      best.u = e.has_field ? field_value<N>(e, xi) : 0.f;
+    }
+  }
+}
+
+// Face test of one face against [tmin,tmax] through its hull box (exact cull).
+__device__ __forceinline__ bool face_may_hit(const float* __restrict__ fbox, int f, float3 o, float3 d, float tmin,
+                                             float tmax) {
+  const float* b = fbox + 6 * f;
+  const float lo[3] = {__ldg(b + 0), __ldg(b + 1), __ldg(b + 2)};
+  const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
+  float a0, a1;
+  return ray_box(o, d, lo, hi, tmin, tmax, a0, a1);
+}
+
+// Warp version of hit_hex: the (face, seed) Newton solves of the faces that
+// survive the cull are independent, so they are spread over the lanes (at
+// most 6 x 9 = 54, two per lane). For each face the lowest seed index that
+// was accepted answers — the seed the sequential loop would stop at — and
+// faces are then compared in index order as the reference does.
+template <int N>
+__device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, float3 o, float3 d, float tmin,
+                             float tmax, float& th, float3& xh, int& face, Work& w, Work& wu) {
+  const int lane = threadIdx.x & 31;
+  unsigned packed = 0;
+  int na = 0;
+  for (int f = 0; f < 6; ++f) {
+    if (face_may_hit(fbox, f, o, d, tmin, tmax)) {
+      packed |= static_cast<unsigned>(f) << (3 * na);
+      ++na;
+    } else {
+      ++wu.culled;
+    }
+  }
+  if (na == 0) return false;
+  const int T = na * 9;
+  bool ok[2] = {false, false};
+  float tv[2] = {0.f, 0.f};
+  float3 xv[2] = {make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int k = lane + 32 * r;
+    if (k < T) {
+      const int slot = k / 9, sd = k - 9 * slot;
+      const int f = (packed >> (3 * slot)) & 7u;
+      ok[r] = face_seed<N>(e, o, d, f, sd % 3, sd / 3, tmin, tmax, tv[r], xv[r], w);
+    }
+  }
+  bool any = false;
+  float best = tmax;
+  for (int a = 0; a < na; ++a) {
+    const int k0 = lane, k1 = lane + 32;
+    const unsigned b0 = __ballot_sync(kFull, ok[0] && k0 / 9 == a);
+    const unsigned b1 = __ballot_sync(kFull, ok[1] && k1 < T && k1 / 9 == a);
+    if ((b0 | b1) == 0u) continue;
+    const bool second = b0 == 0u;
+    const int src = second ? __ffs(b1) - 1 : __ffs(b0) - 1;
+    const float tA = __shfl_sync(kFull, tv[0], src), tB = __shfl_sync(kFull, tv[1], src);
+    const float3 xA = shfl3(xv[0], src), xB = shfl3(xv[1], src);
+    const float tf = second ? tB : tA;
+    const float3 xf = second ? xB : xA;
+    if (tf > tmin && tf < best) {
+      best = tf;
+      xh = xf;
+      face = (packed >> (3 * a)) & 7u;
+      any = true;
+    }
+  }
+  if (any) th = best;
+  return any;
+}
+
+// Warp version of visit_candidate: every lane holds the same `best`.
+template <int N>
+__device__ void visit_warp(const Elem<N>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d, float te,
+                           float tx, float iso, bool iso_on, HitState& best, Work& w, Work& wu) {
+  ++wu.cand;
+  float th;
+  float3 xi, g;
+  if (iso_on && e.has_field && find_iso_warp<N>(e, o, d, te, tx, iso, th, xi, g, w, wu)) {
+    if (th > 0.001f && th < best.t) {
+      float3 n = normalize3(g);
+      if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+      best.t = th;
+      best.elem = eidx;
+      best.face = -1;
+      best.kind = HO_HIT_ISO;
+      best.xi = xi;
+      best.n = n;
+      best.u = field_value<N>(e, xi);
+    }
+    return;
+  }
+  int face = -1;
+  if (hit_hex_warp<N>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu)) {
+    if (th > 0.001f && th < best.t) {
+      float3 x;
+      float J[9];
+      geom_eval<N>(e, xi, x, J, wu);
       const float3 dr = make_float3(J[0], J[3], J[6]), ds = make_float3(J[1], J[4], J[7]),
                    dt = make_float3(J[2], J[5], J[8]);
       float3 n;

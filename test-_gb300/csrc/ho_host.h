@@ -99,6 +99,9 @@ struct ho_context {
   size_t rgb_cap = 0;
   float* d_rays = nullptr;
   size_t rays_cap = 0;
+  int32_t* d_work = nullptr;      // query queue of the intersect pass
+  size_t work_cap = 0;
+  unsigned* d_qctr = nullptr;     // [0] queue length, [1] next item
   void* h_pinned = nullptr;
   size_t pinned_cap = 0;
 };

@@ -5,6 +5,56 @@
 
 namespace ho {
 
+// Does the ray meet any padded element box in [0.001, inf)? (early exit)
+static __device__ bool any_candidate(const BNode* __restrict__ nodes, float3 o, float3 d, Work& w) {
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp > 0) {
+    const int node = stack[--sp];
+    ++w.nodes;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      float lo[3], hi[3];
+      int id;
+      uint32_t aux;
+      load_child(nodes, node, c, lo, hi, id, aux);
+      if (id == kEmptyChild) continue;
+      float a0, a1;
+      if (!ray_box(o, d, lo, hi, 0.001f, FLT_MAX, a0, a1)) continue;
+      if (id < 0) return true;
+      if (sp >= kStack) return true;  // let the intersect kernel see (and report) it
+      stack[sp++] = id;
+    }
+  }
+  return false;
+}
+
+// Pass 1, one thread per query: rays that meet no padded box are finished
+// here (miss); the rest are appended to the work queue.
+__global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_queries) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  Work w;
+  bool need = false;
+  float3 o = make_float3(0.f, 0.f, 0.f), d = make_float3(0.f, 0.f, 1.f);
+  if (q < n_queries) {
+    int iso_idx;
+    query_ray(P, q, o, d, iso_idx);
+    need = any_candidate(P.nodes, o, d, w);
+    if (!need) write_result(P, q, d, miss_state(), 0);
+  }
+  const unsigned m = __ballot_sync(kFull, need);
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(P.qcount, static_cast<unsigned>(__popc(m)));
+    base = __shfl_sync(kFull, base, leader);
+    if (need) P.work[base + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(q);
+  }
+  flush_work(P.stats, w, q < n_queries);
+}
+
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   TraceParams P;
   P.nodes = c->d_nodes;
@@ -36,6 +86,30 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
     n_threads = tiles * 32 * a.n_iso;
   }
   if (n_threads == 0) return 0;
+  if (static_cast<size_t>(n_queries) > c->work_cap || !c->d_work) {
+    cudaFree(c->d_work);
+    c->d_work = nullptr;
+    c->work_cap = 0;
+    cudaError_t e = cudaMalloc(&c->d_work, static_cast<size_t>(n_queries) * sizeof(int32_t));
+    if (e != cudaSuccess) return int(e);
+    c->work_cap = static_cast<size_t>(n_queries);
+  }
+  if (!c->d_qctr) {
+    cudaError_t e = cudaMalloc(&c->d_qctr, 2 * sizeof(unsigned));
+    if (e != cudaSuccess) return int(e);
+  }
+  {
+    cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return int(e);
+  }
+  P.work = c->d_work;
+  P.qcount = c->d_qctr;
+  P.qnext = c->d_qctr + 1;
+  classify_kernel<<<static_cast<unsigned>((n_queries + 255) / 256), 256, 0, s>>>(P, n_queries);
+  {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return int(e);
+  }
   cudaError_t e;
   switch (c->N) {
     case 2: e = launch_n<2>(P, n_queries, n_threads, s); break;

@@ -23,7 +23,7 @@ namespace ho {
 
 constexpr int kCandK = 8;
 constexpr int kStack = 64;
-constexpr int kTraceBlock = 128;
+constexpr int kTraceBlock = 128;  // intersect pass: 4 warps, one query each
 
 struct CamArgs {
   float3 origin, llc, horiz, vert;
@@ -45,6 +45,9 @@ struct TraceParams {
   ho_hit* __restrict__ hits;
   uint8_t* __restrict__ rgb;
   DevStats* stats;
+  int32_t* work;      // queue of query indices that meet at least one box
+  unsigned* qcount;   // queue length (written by the classify pass)
+  unsigned* qnext;    // next queue item to take (intersect pass)
 };
 
 __device__ __forceinline__ bool key_less(float ta, int ea, float tb, int eb) {
@@ -172,25 +175,13 @@ __device__ __forceinline__ void shade(const HitState& h, float3 d, uint8_t* out)
   for (int q = 0; q < 3; ++q) out[q] = static_cast<uint8_t>(255.99f * fminf(1.0f, sqrtf(c[q])));
 }
 
-template <int N>
-__global__ void __launch_bounds__(kTraceBlock) trace_kernel(TraceParams P, int64_t n_queries) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wid = (static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x) >> 5;
-  int64_t q;
-  float3 o, d;
-  int iso_idx;
-  bool active;
-  int64_t pix = 0;
+// Rays as the kernels see them: query q -> (origin, direction, isovalue index).
+__device__ __forceinline__ void query_ray(const TraceParams& P, int64_t q, float3& o, float3& d, int& iso_idx) {
   if (P.rays == nullptr) {
-    const int tx_n = (P.cam.width + 7) >> 3, ty_n = (P.cam.height + 3) >> 2;
-    const int64_t tiles = static_cast<int64_t>(tx_n) * ty_n;
-    iso_idx = static_cast<int>(wid / tiles);
-    const int64_t tile = wid - static_cast<int64_t>(iso_idx) * tiles;
-    const int x = static_cast<int>(tile % tx_n) * 8 + (lane & 7);
-    const int y = static_cast<int>(tile / tx_n) * 4 + (lane >> 3);
-    active = iso_idx < P.n_iso && x < P.cam.width && y < P.cam.height;
-    pix = static_cast<int64_t>(y) * P.cam.width + x;
-    q = static_cast<int64_t>(iso_idx) * P.cam.width * P.cam.height + pix;
+    const int64_t npix = static_cast<int64_t>(P.cam.width) * P.cam.height;
+    iso_idx = static_cast<int>(q / npix);
+    const int64_t pix = q - static_cast<int64_t>(iso_idx) * npix;
+    const int x = static_cast<int>(pix % P.cam.width), y = static_cast<int>(pix / P.cam.width);
     const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(P.cam.width);
     const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(P.cam.height);
     o = P.cam.origin;
@@ -199,43 +190,78 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(TraceParams P, int64
                     P.cam.llc.z + s * P.cam.horiz.z + t * P.cam.vert.z - o.z);
     d = normalize3(d);
   } else {
-    q = static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x;
-    active = q < n_queries;
-    iso_idx = active ? static_cast<int>(q / P.n_rays) : 0;
-    const int64_t r = active ? q - static_cast<int64_t>(iso_idx) * P.n_rays : 0;
-    const float* rp = P.rays + 6 * r;
-    o = active ? make_float3(rp[0], rp[1], rp[2]) : make_float3(0.f, 0.f, 0.f);
-    d = active ? make_float3(rp[3], rp[4], rp[5]) : make_float3(0.f, 0.f, 1.f);
+    iso_idx = static_cast<int>(q / P.n_rays);
+    const float* rp = P.rays + 6 * (q - static_cast<int64_t>(iso_idx) * P.n_rays);
+    o = make_float3(rp[0], rp[1], rp[2]);
+    d = make_float3(rp[3], rp[4], rp[5]);
   }
-  Work w;
-  HitState best;
-  best.t = FLT_MAX;
-  best.elem = -1;
-  best.face = -1;
-  best.kind = HO_HIT_MISS;
-  best.xi = make_float3(0.f, 0.f, 0.f);
-  best.n = best.xi;
-  best.u = 0.f;
-  best.flags = 0;
-  if (active) {
+}
+
+__device__ __forceinline__ void write_result(const TraceParams& P, int64_t q, float3 d, const HitState& best,
+                                             uint32_t iters) {
+  if (P.hits) {
+    ho_hit h;
+    h.t = best.t;
+    h.elem = best.elem;
+    h.face = static_cast<int16_t>(best.face);
+    h.kind = static_cast<int16_t>(best.kind);
+    h.xi[0] = best.xi.x; h.xi[1] = best.xi.y; h.xi[2] = best.xi.z;
+    h.n[0] = best.n.x; h.n[1] = best.n.y; h.n[2] = best.n.z;
+    h.u = best.u;
+    h.flags = best.flags;
+    h.iters = iters;
+    P.hits[q] = h;
+  }
+  if (P.rgb && P.rays == nullptr) shade(best, d, P.rgb + 3 * q);
+}
+
+__device__ __forceinline__ HitState miss_state() {
+  HitState b;
+  b.t = FLT_MAX;
+  b.elem = -1;
+  b.face = -1;
+  b.kind = HO_HIT_MISS;
+  b.xi = make_float3(0.f, 0.f, 0.f);
+  b.n = b.xi;
+  b.u = 0.f;
+  b.flags = 0;
+  return b;
+}
+
+// Pass 2, persistent, one warp per queued query: ordered candidates, each
+// visited with its independent Newton solves spread over the lanes.
+template <int N>
+__global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
+  const int lane = threadIdx.x & 31;
+  constexpr int64_t S = static_cast<int64_t>(N) * N * N;
+  Work w, wu;
+  const unsigned n_work = *P.qcount;
+  for (;;) {
+    unsigned item = 0;
+    if (lane == 0) item = atomicAdd(P.qnext, 1u);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= n_work) break;
+    const int64_t q = P.work[item];
+    float3 o, d;
+    int iso_idx;
+    query_ray(P, q, o, d, iso_idx);
     const float iso = P.iso[iso_idx];
     const bool iso_on = (P.iso_on_mask >> iso_idx) & 1u;
-    constexpr int64_t S = static_cast<int64_t>(N) * N * N;
+    HitState best = miss_state();
+    const uint32_t it0 = wu.newton + wu.face + w.newton + w.face;
     float kt = -FLT_MAX;
     int ke = -1;
     for (;;) {
       float bt[kCandK];
       int be[kCandK];
       bool overflow;
-      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, w)) {
-        atomicOr(&P.stats->status, kStatusStackOverflow);
+      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu)) {
+        if (lane == 0) atomicOr(&P.stats->status, kStatusStackOverflow);
         break;
       }
       bool done = false;
 #pragma unroll 1
       for (int j = 0; j < kCandK; ++j) {
-        // the buffer is sorted; read entry j through a static-index select
-        // chain so the buffer stays in registers
         float ct = bt[0];
         int ce = be[0];
 #pragma unroll
@@ -248,7 +274,6 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(TraceParams P, int64
           done = true;
           break;
         }
-        // segment of the padded box clipped to the closest hit so far
         const float* b = P.box + 6 * static_cast<int64_t>(ce);
         const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
         const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
@@ -257,38 +282,42 @@ __global__ void __launch_bounds__(kTraceBlock) trace_kernel(TraceParams P, int64
           Elem<N> el;
           el.c = P.rec + static_cast<int64_t>(ce) * 4 * S;
           el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
-          visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
-                             best, w);
+          visit_warp<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on, best,
+                        w, wu);
         }
         kt = ct;
         ke = ce;
       }
       if (done || !overflow) break;
-      ++w.restarts;
+      ++wu.restarts;
       best.flags |= HO_FLAG_OVERFLOW;
     }
+    // iterations of this query summed over the lanes
+    uint32_t its = w.newton + w.face;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) its += __shfl_xor_sync(kFull, its, off);
+    if (lane == 0) write_result(P, q, d, best, its + wu.newton + wu.face - it0);
   }
-  flush_work(P.stats, w, active);
-  if (!active) return;
-  if (P.hits) {
-    ho_hit h;
-    h.t = best.t;
-    h.elem = best.elem;
-    h.face = static_cast<int16_t>(best.face);
-    h.kind = static_cast<int16_t>(best.kind);
-    h.xi[0] = best.xi.x; h.xi[1] = best.xi.y; h.xi[2] = best.xi.z;
-    h.n[0] = best.n.x; h.n[1] = best.n.y; h.n[2] = best.n.z;
-    h.u = best.u;
-    h.flags = best.flags;
-    h.iters = w.newton + w.face;
-    P.hits[q] = h;
+  if (lane == 0) {
+    w.cand += wu.cand; w.geom += wu.geom; w.map += wu.map; w.field += wu.field; w.newton += wu.newton;
+    w.face += wu.face; w.culled += wu.culled; w.nodes += wu.nodes; w.restarts += wu.restarts;
   }
-  if (P.rgb && P.rays == nullptr) shade(best, d, P.rgb + 3 * q);
+  flush_work(P.stats, w, false);
 }
+
 template <int N>
 cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s) {
-  const int64_t blocks = (n_threads + kTraceBlock - 1) / kTraceBlock;
-  trace_kernel<N><<<static_cast<unsigned>(blocks), kTraceBlock, 0, s>>>(P, n_queries);
+  (void)n_threads;
+  (void)n_queries;
+  static int grid = 0;  // persistent grid: resident blocks per SM x SMs
+  if (grid == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N>, kTraceBlock, 0);
+    grid = sms * (per > 0 ? per : 1);
+  }
+  isect_kernel<N><<<grid, kTraceBlock, 0, s>>>(P);
   return cudaGetLastError();
 }
 
