@@ -117,20 +117,20 @@ inline bool has_ho_geom(const Elem& e) {
 enum Deriv { D_NONE = 0, D_R = 1, D_S = 2, D_T = 3 };
 
 // Triple-loop modal sum with one factor differentiated (HexElement.cu:8-94).
+// The reference calls ModifiedA inside the innermost loop; the 1-D values
+// only depend on (mode, coordinate), so they are computed once per call here
+// — the same values, accumulated in the same order.
 template <class R> R modal3(const float* c, const unsigned m[3], const V3<R>& p, Deriv d) {
   if (!c || m[0] == 0 || m[1] == 0 || m[2] == 0) return R(0);
+  R br[16], bs[16], bt[16];
+  for (unsigned i = 0; i < m[0]; ++i) br[i] = (d == D_R) ? mod_a_prime<R>(i, p.x) : mod_a<R>(i, p.x);
+  for (unsigned j = 0; j < m[1]; ++j) bs[j] = (d == D_S) ? mod_a_prime<R>(j, p.y) : mod_a<R>(j, p.y);
+  for (unsigned k = 0; k < m[2]; ++k) bt[k] = (d == D_T) ? mod_a_prime<R>(k, p.z) : mod_a<R>(k, p.z);
   R acc = R(0);
   int idx = 0;
-  for (unsigned k = 0; k < m[2]; ++k) {
-    const R tk = (d == D_T) ? mod_a_prime<R>(k, p.z) : mod_a<R>(k, p.z);
-    for (unsigned j = 0; j < m[1]; ++j) {
-      const R sj = (d == D_S) ? mod_a_prime<R>(j, p.y) : mod_a<R>(j, p.y);
-      for (unsigned i = 0; i < m[0]; ++i) {
-        const R ri = (d == D_R) ? mod_a_prime<R>(i, p.x) : mod_a<R>(i, p.x);
-        acc += static_cast<R>(c[idx++]) * ri * sj * tk;
-      }
-    }
-  }
+  for (unsigned k = 0; k < m[2]; ++k)
+    for (unsigned j = 0; j < m[1]; ++j)
+      for (unsigned i = 0; i < m[0]; ++i) acc += static_cast<R>(c[idx++]) * br[i] * bs[j] * bt[k];
   return acc;
 }
 
@@ -239,17 +239,21 @@ template <class R> R field_value(const Elem& e, const V3<R>& p) { return modal3<
 template <class R> V3<R> field_grad_ref(const Elem& e, const V3<R>& p) {
   V3<R> g = mk<R>(0, 0, 0);
   const float* c = e.field;
+  R a[3][16], da[3][16];
+  const R q[3] = {p.x, p.y, p.z};
+  for (int ax = 0; ax < 3; ++ax)
+    for (unsigned i = 0; i < e.fm[ax]; ++i) {
+      a[ax][i] = mod_a<R>(i, q[ax]);
+      da[ax][i] = mod_a_prime<R>(i, q[ax]);
+    }
   int idx = 0;
   for (unsigned k = 0; k < e.fm[2]; ++k) {
-    const R tk = mod_a<R>(k, p.z), tkp = mod_a_prime<R>(k, p.z);
     for (unsigned j = 0; j < e.fm[1]; ++j) {
-      const R sj = mod_a<R>(j, p.y), sjp = mod_a_prime<R>(j, p.y);
       for (unsigned i = 0; i < e.fm[0]; ++i) {
-        const R ri = mod_a<R>(i, p.x), rip = mod_a_prime<R>(i, p.x);
         const R cv = static_cast<R>(c[idx++]);
-        g.x += cv * rip * sj * tk;
-        g.y += cv * ri * sjp * tk;
-        g.z += cv * ri * sj * tkp;
+        g.x += cv * da[0][i] * a[1][j] * a[2][k];
+        g.y += cv * a[0][i] * da[1][j] * a[2][k];
+        g.z += cv * a[0][i] * a[1][j] * da[2][k];
       }
     }
   }
