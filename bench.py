@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--mode", default="both", choices=["both", "plain", "learned"],
+                    help="learned: learned-init batched (the headline); plain: the reference algorithm")
+    ap.add_argument("--train-samples", type=int, default=2_000_000)
+    ap.add_argument("--train-steps", type=int, default=1500)
     ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling)")
     ap.add_argument("--height", type=int, default=0, help="override the workload's image height (profiling)")
     return ap.parse_args()
@@ -250,33 +254,48 @@ def run_gpu(args, rank, world):
     def step():
         ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            flush.zero_()
-            step()
-    torch.cuda.synchronize()
-    st = ctx.stats()
-    barrier(world)
-    torch.cuda.synchronize()
-    evs = []
-    with ClockSampler(local) as clk:
+    def timed(mode):
+        ctx.set_mode(mode)
         with torch.cuda.stream(stream):
-            for _ in range(args.steps):
+            for _ in range(args.warmup):
                 flush.zero_()
-                a = torch.cuda.Event(enable_timing=True)
-                b = torch.cuda.Event(enable_timing=True)
-                a.record(stream)
                 step()
-                b.record(stream)
-                evs.append((a, b))
         torch.cuda.synchronize()
-    barrier(world)
-    ms = [a.elapsed_time(b) for a, b in evs]
-    total_s = sum(ms) / 1e3
-    total_s = max_over_ranks(total_s, world)
+        st = ctx.stats()
+        barrier(world)
+        torch.cuda.synchronize()
+        evs = []
+        with ClockSampler(local) as clk:
+            with torch.cuda.stream(stream):
+                for _ in range(args.steps):
+                    flush.zero_()
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    step()
+                    b.record(stream)
+                    evs.append((a, b))
+            torch.cuda.synchronize()
+        barrier(world)
+        total = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / 1e3, world)
+        return total, st, clk
+
+    train = None
+    if args.mode in ("both", "learned"):
+        t0 = time.perf_counter()
+        losses = ctx.train_mlp(n_samples=args.train_samples, steps=args.train_steps, batch=4096, lr=2e-3, seed=1)
+        train = {"samples": args.train_samples, "steps": args.train_steps, "batch": 4096,
+                 "seconds": time.perf_counter() - t0, "loss_first": float(losses[:20].mean()),
+                 "loss_last": float(losses[-50:].mean())}
+    results = {}
+    for mode in (["plain", "learned"] if args.mode == "both" else [args.mode]):
+        results[mode] = timed(hr.MODE_LEARNED if mode == "learned" else hr.MODE_PLAIN)
+    head = "learned" if "learned" in results else "plain"
+    total_s, st, clk = results[head]
     queries = sum_over_ranks(nq * args.steps, world)
     value = queries / total_s / 1e6
-    launch_s = total_s / args.steps  # one trace launch per step
+    launch_s = total_s / args.steps
+    plain_value = queries / results["plain"][0] / 1e6 if "plain" in results else None
 
     # roofline of the trace kernel: algorithmic FP32 flops of one launch
     N = info["max_modes"]
@@ -288,6 +307,7 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
+    ctx.set_mode(hr.MODE_LEARNED if head == "learned" else hr.MODE_PLAIN)
     for _ in range(0 if args.no_e2e else args.steps):
         ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
     e2e_s = max(max_over_ranks(time.perf_counter() - t0, world), 1e-9)
@@ -303,7 +323,12 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "impl": "gb300", "mode": "plain",
+        "impl": "gb300", "mode": "learned-init + batched" if head == "learned" else "plain",
+        "plain": None if plain_value is None else {
+            "value": plain_value, "ms_per_step": results["plain"][0] / args.steps * 1e3,
+            "newton_iters": results["plain"][1]["newton_iters"], "face_iters": results["plain"][1]["face_iters"]},
+        "speedup_vs_plain": None if plain_value is None else value / plain_value,
+        "training": train,
         "config": {"workload": w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes", "order": w.order_max,
                    "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
                    "rays": f"{W}x{H}", "isovalues": w.isovalues, "queries_per_step": nq,
@@ -315,7 +340,7 @@ def run_gpu(args, rank, world):
                      "flops_per_launch": flops},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4 * n_iso,
                 "d2h_bytes_per_step": nq * 3},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (4 if head == "learned" else 2),
         "clocks": clk.summary(),
         "work": st,
         "scene": info,

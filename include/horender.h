@@ -183,8 +183,41 @@ int ho_intersect(ho_context* ctx, int64_t n, const float* rays, float iso, int i
 int ho_intersect_device(ho_context* ctx, int64_t n, const float* rays_dev, float iso, int iso_enabled,
                         ho_hit* out_dev, void* stream);
 
-/* Solver mode (HO_MODE_*). No reference counterpart: the reference has one. */
+/* Solver mode (HO_MODE_*). No reference counterpart: the reference has one.
+ * HO_MODE_LEARNED needs a trained (ho_train_mlp) or loaded (ho_mlp_load)
+ * network. */
 int ho_set_mode(ho_context* ctx, int mode);
+
+/* ---- learned mode (no reference counterpart) ------------------------------
+ * Network 48 -> 128 -> 128 -> 128 -> 8 (GELU), BF16 weights, FP32
+ * accumulation. Flat parameter order: W1[48][128], b1[128], W2[128][128], b2,
+ * W3[128][128], b3, W4[128][8], b4[8] (HO_MLP_PARAMS floats; W[in][out]).
+ * Input of one (ray, element) pair: element descriptor (8 corners and 6
+ * face-centre offsets in the element frame, 42) + entry point into the
+ * element's padded box in that frame (3) + unit direction (3). Outputs:
+ * reference coordinates at the entry (3), their rate of change along the ray
+ * per element size (3), 2 unused. */
+#define HO_MLP_PARAMS 40328
+#define HO_MLP_IN 48
+#define HO_MLP_OUT 8
+int ho_mlp_init(ho_context* ctx, uint64_t seed);
+int ho_mlp_set_params(ho_context* ctx, const float* params);
+int ho_mlp_get_params(ho_context* ctx, float* params);
+/* Y[n][8] = network(X[n][48]) with the inference kernel. */
+int ho_mlp_forward(ho_context* ctx, const float* X, int64_t n, float* Y);
+/* One forward/backward pass of the training kernels on n rows: masked MSE on
+ * outputs 0..5 (mean over valid rows); gradients in the flat order. */
+int ho_mlp_grad(ho_context* ctx, const float* X, const float* T, const uint8_t* valid, int n, float* loss,
+                float* grads);
+/* n training pairs produced by the plain solver on seeded random rays through
+ * random elements of the built scene: X[n][48], T[n][8], valid[n]. */
+int ho_learn_samples(ho_context* ctx, int64_t n, uint64_t seed, float* X, float* T, uint8_t* valid);
+/* Generate n_samples pairs on the device and train (Adam, cosine decay);
+ * losses (optional) receives the per-step batch loss. */
+int ho_train_mlp(ho_context* ctx, int64_t n_samples, int steps, int batch, float lr, uint64_t seed, float* losses);
+/* Checkpoint: FP32 master parameters + their BF16 copy. */
+int ho_mlp_save(ho_context* ctx, const char* path);
+int ho_mlp_load(ho_context* ctx, const char* path);
 int ho_get_stats(ho_context* ctx, ho_stats* out);
 
 /* FP32 FMA throughput of the device in TFLOP/s (register-resident FMA loop):

@@ -14,6 +14,8 @@
 #include <string>
 
 #include "ho_host.h"
+#include "ho_learn.h"
+#include "ho_mlp.h"
 
 using ho::HostScene;
 
@@ -49,6 +51,8 @@ void free_scene(ho_context* c) {
   cudaFree(c->d_flags);
   cudaFree(c->d_own);
   cudaFree(c->d_nodes);
+  cudaFree(c->d_desc);
+  c->d_desc = nullptr;
   c->d_rec = c->d_box = c->d_hull = c->d_fbox = nullptr;
   c->d_flags = nullptr;
   c->d_own = nullptr;
@@ -159,6 +163,10 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_rays);
     cudaFree(c->d_work);
     cudaFree(c->d_qctr);
+    cudaFree(c->d_feat);
+    cudaFree(c->d_pred);
+    cudaFree(c->d_cand);
+    c->mlp.release();
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     cudaStreamDestroy(c->stream);
   }
@@ -289,6 +297,9 @@ int ho_build_bvh(ho_context* c) {
   if (rc) return cuda_fail(c, rc, "setup kernel");
   rc = ho::build_lbvh(c);
   if (rc) return cuda_fail(c, rc, "LBVH build");
+  CK(cudaMalloc(&c->d_desc, ne * ho::kDescFloats * sizeof(float)), "cudaMalloc(descriptors)");
+  rc = ho::launch_desc(c->N, c->d_rec, ne, c->d_desc, c->stream);
+  if (rc) return cuda_fail(c, rc, "descriptor kernel");
   if (c->bvh_depth + 2 > 64) return fail(c, HO_ERR_RANGE, "BVH deeper than the traversal stack");
   CK(cudaStreamSynchronize(c->stream), "sync");
   c->device_bytes = static_cast<int64_t>(rec.size() * sizeof(float)) + ne * (4 + 4 + 24 + 24 + 144) +
@@ -412,9 +423,257 @@ int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso
 
 int ho_set_mode(ho_context* c, int mode) {
   if (!c) return HO_ERR_ARG;
-  if (mode != HO_MODE_PLAIN) return fail(c, HO_ERR_ARG, "mode not available in this build");
-  c->mode = mode;
+  if (mode == HO_MODE_PLAIN) {
+    c->mode = mode;
+    return HO_OK;
+  }
+  if (mode == HO_MODE_LEARNED) {
+    if (!c->mlp.trained) return fail(c, HO_ERR_STATE, "learned mode needs a trained or loaded network");
+    c->mode = mode;
+    return HO_OK;
+  }
+  return fail(c, HO_ERR_ARG, "unknown mode");
+}
+
+// ---- learned mode ----------------------------------------------------------
+namespace {
+const int kLayerIn[4] = {ho::kMlpIn, ho::kMlpHidden, ho::kMlpHidden, ho::kMlpHidden};
+const int kLayerInPad[4] = {ho::kMlpInPad, ho::kMlpHidden, ho::kMlpHidden, ho::kMlpHidden};
+const int kLayerOut[4] = {ho::kMlpHidden, ho::kMlpHidden, ho::kMlpHidden, ho::kMlpOut};
+
+// flat layout W1[48][128] b1 W2[128][128] b2 W3 b3 W4[128][8] b4 -> padded per-layer host arrays
+void unflatten(const float* flat, std::vector<std::vector<float>>& W, std::vector<std::vector<float>>& b) {
+  W.assign(4, {});
+  b.assign(4, {});
+  size_t o = 0;
+  for (int l = 0; l < 4; ++l) {
+    W[l].assign(static_cast<size_t>(kLayerInPad[l]) * kLayerOut[l], 0.f);
+    for (int i = 0; i < kLayerIn[l]; ++i)
+      for (int j = 0; j < kLayerOut[l]; ++j) W[l][static_cast<size_t>(i) * kLayerOut[l] + j] = flat[o++];
+    b[l].assign(flat + o, flat + o + kLayerOut[l]);
+    o += kLayerOut[l];
+  }
+}
+
+void flatten(const std::vector<std::vector<float>>& W, const std::vector<std::vector<float>>& b, float* flat) {
+  size_t o = 0;
+  for (int l = 0; l < 4; ++l) {
+    for (int i = 0; i < kLayerIn[l]; ++i)
+      for (int j = 0; j < kLayerOut[l]; ++j) flat[o++] = W[l][static_cast<size_t>(i) * kLayerOut[l] + j];
+    for (int j = 0; j < kLayerOut[l]; ++j) flat[o++] = b[l][j];
+  }
+}
+
+int upload_params(ho_context* c, const float* flat) {
+  std::vector<std::vector<float>> W, b;
+  unflatten(flat, W, b);
+  const float* Wp[4] = {W[0].data(), W[1].data(), W[2].data(), W[3].data()};
+  const float* bp[4] = {b[0].data(), b[1].data(), b[2].data(), b[3].data()};
+  const int rc = c->mlp.set_params(Wp, bp, c->stream);
+  if (rc) return cuda_fail(c, rc, "network parameters");
+  CK(cudaStreamSynchronize(c->stream), "sync");
   return HO_OK;
+}
+
+int download_params(ho_context* c, float* flat, bool grads) {
+  std::vector<std::vector<float>> W(4), b(4);
+  for (int l = 0; l < 4; ++l) {
+    W[l].resize(static_cast<size_t>(kLayerInPad[l]) * kLayerOut[l]);
+    b[l].resize(kLayerOut[l]);
+    CK(cudaMemcpyAsync(W[l].data(), grads ? c->mlp.gW[l] : c->mlp.W[l], W[l].size() * sizeof(float),
+                       cudaMemcpyDeviceToHost, c->stream), "read parameters");
+    CK(cudaMemcpyAsync(b[l].data(), grads ? c->mlp.gb[l] : c->mlp.b[l], b[l].size() * sizeof(float),
+                       cudaMemcpyDeviceToHost, c->stream), "read parameters");
+  }
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  flatten(W, b, flat);
+  return HO_OK;
+}
+
+void to_bf16_rows(const float* X, int64_t n, std::vector<uint16_t>& out) {
+  out.assign(static_cast<size_t>(n) * ho::kMlpInPad, 0);
+  for (int64_t r = 0; r < n; ++r)
+    for (int j = 0; j < ho::kMlpIn; ++j) {
+      uint32_t u;
+      std::memcpy(&u, &X[r * ho::kMlpIn + j], 4);
+      const uint32_t lsb = (u >> 16) & 1u;  // round to nearest even
+      out[static_cast<size_t>(r) * ho::kMlpInPad + j] = static_cast<uint16_t>((u + 0x7FFFu + lsb) >> 16);
+    }
+}
+}  // namespace
+
+int ho_mlp_init(ho_context* c, uint64_t seed) {
+  if (!c) return HO_ERR_ARG;
+  int rc = ensure_device(c);
+  if (rc) return rc;
+  std::vector<float> flat(ho::kMlpParams, 0.f);
+  ho::Pcg64 g(seed, 11);
+  size_t o = 0;
+  for (int l = 0; l < 4; ++l) {
+    const double lim = std::sqrt(6.0 / (kLayerIn[l] + kLayerOut[l]));  // Glorot uniform
+    for (int i = 0; i < kLayerIn[l] * kLayerOut[l]; ++i) flat[o++] = static_cast<float>((2.0 * g.uniform() - 1.0) * lim);
+    o += kLayerOut[l];  // zero biases
+  }
+  return upload_params(c, flat.data());
+}
+
+int ho_mlp_set_params(ho_context* c, const float* params) {
+  if (!c || !params) return HO_ERR_ARG;
+  int rc = ensure_device(c);
+  if (rc) return rc;
+  rc = upload_params(c, params);
+  if (rc) return rc;
+  c->mlp.trained = true;
+  return HO_OK;
+}
+
+int ho_mlp_get_params(ho_context* c, float* params) {
+  if (!c || !params) return HO_ERR_ARG;
+  if (!c->mlp.ready) return fail(c, HO_ERR_STATE, "no network");
+  return download_params(c, params, false);
+}
+
+int ho_mlp_forward(ho_context* c, const float* X, int64_t n, float* Y) {
+  if (!c || (n > 0 && (!X || !Y))) return HO_ERR_ARG;
+  if (!c->mlp.ready) return fail(c, HO_ERR_STATE, "no network");
+  if (n == 0) return HO_OK;
+  std::vector<uint16_t> xb;
+  to_bf16_rows(X, n, xb);
+  void* dx = nullptr;
+  float* dy = nullptr;
+  CK(cudaMalloc(&dx, xb.size() * 2), "cudaMalloc");
+  CK(cudaMalloc(&dy, static_cast<size_t>(n) * ho::kMlpOut * sizeof(float)), "cudaMalloc");
+  CK(cudaMemcpyAsync(dx, xb.data(), xb.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload");
+  const int rc = ho::mlp_infer(c->mlp.dev(), dx, n, nullptr, 1, dy, c->stream, 152);
+  if (rc) return cuda_fail(c, rc, "network forward");
+  CK(cudaMemcpyAsync(Y, dy, static_cast<size_t>(n) * ho::kMlpOut * sizeof(float), cudaMemcpyDeviceToHost, c->stream),
+     "read");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  cudaFree(dx);
+  cudaFree(dy);
+  return HO_OK;
+}
+
+int ho_mlp_grad(ho_context* c, const float* X, const float* T, const uint8_t* valid, int n, float* loss,
+                float* grads) {
+  if (!c || !X || !T || !valid || n <= 0 || !loss || !grads) return HO_ERR_ARG;
+  if (!c->mlp.ready) return fail(c, HO_ERR_STATE, "no network");
+  std::vector<uint16_t> xb;
+  to_bf16_rows(X, n, xb);
+  void* dx = nullptr;
+  float *dt = nullptr, *dl = nullptr;
+  uint8_t* dv = nullptr;
+  CK(cudaMalloc(&dx, xb.size() * 2), "cudaMalloc");
+  CK(cudaMalloc(&dt, static_cast<size_t>(n) * ho::kMlpOut * sizeof(float)), "cudaMalloc");
+  CK(cudaMalloc(&dv, n), "cudaMalloc");
+  CK(cudaMalloc(&dl, sizeof(float)), "cudaMalloc");
+  CK(cudaMemcpyAsync(dx, xb.data(), xb.size() * 2, cudaMemcpyHostToDevice, c->stream), "upload");
+  CK(cudaMemcpyAsync(dt, T, static_cast<size_t>(n) * ho::kMlpOut * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+     "upload");
+  CK(cudaMemcpyAsync(dv, valid, n, cudaMemcpyHostToDevice, c->stream), "upload");
+  int nv = 0;
+  for (int i = 0; i < n; ++i) nv += valid[i] ? 1 : 0;
+  const int rc = c->mlp.forward_backward(n, dx, dt, dv, nv, dl, c->stream);
+  if (rc) return cuda_fail(c, rc, "network backward");
+  CK(cudaMemcpyAsync(loss, dl, sizeof(float), cudaMemcpyDeviceToHost, c->stream), "read");
+  const int r2 = download_params(c, grads, true);
+  cudaFree(dx);
+  cudaFree(dt);
+  cudaFree(dv);
+  cudaFree(dl);
+  return r2;
+}
+
+int ho_learn_samples(ho_context* c, int64_t n, uint64_t seed, float* X, float* T, uint8_t* valid) {
+  if (!c || n <= 0 || !X || !T || !valid) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  void* dx = nullptr;
+  float* dt = nullptr;
+  uint8_t* dv = nullptr;
+  CK(cudaMalloc(&dx, static_cast<size_t>(n) * ho::kMlpInPad * 2), "cudaMalloc");
+  CK(cudaMalloc(&dt, static_cast<size_t>(n) * ho::kMlpOut * sizeof(float)), "cudaMalloc");
+  CK(cudaMalloc(&dv, n), "cudaMalloc");
+  int rc = ho::launch_datagen(c->N, c->d_rec, c->d_box, c->d_desc, c->n_elem, n, seed, dx, dt, dv, c->stream);
+  if (rc) return cuda_fail(c, rc, "training-pair kernel");
+  std::vector<uint16_t> xb(static_cast<size_t>(n) * ho::kMlpInPad);
+  CK(cudaMemcpyAsync(xb.data(), dx, xb.size() * 2, cudaMemcpyDeviceToHost, c->stream), "read");
+  CK(cudaMemcpyAsync(T, dt, static_cast<size_t>(n) * ho::kMlpOut * sizeof(float), cudaMemcpyDeviceToHost, c->stream),
+     "read");
+  CK(cudaMemcpyAsync(valid, dv, n, cudaMemcpyDeviceToHost, c->stream), "read");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  for (int64_t r = 0; r < n; ++r)
+    for (int j = 0; j < ho::kMlpIn; ++j) {
+      const uint32_t u = static_cast<uint32_t>(xb[static_cast<size_t>(r) * ho::kMlpInPad + j]) << 16;
+      std::memcpy(&X[r * ho::kMlpIn + j], &u, 4);
+    }
+  cudaFree(dx);
+  cudaFree(dt);
+  cudaFree(dv);
+  return HO_OK;
+}
+
+int ho_train_mlp(ho_context* c, int64_t n_samples, int steps, int batch, float lr, uint64_t seed, float* losses) {
+  if (!c || n_samples <= 0 || steps <= 0 || batch <= 0 || batch > 65536) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (!c->mlp.ready) {
+    const int rc = ho_mlp_init(c, seed);
+    if (rc) return rc;
+  }
+  void* dx = nullptr;
+  float* dt = nullptr;
+  uint8_t* dv = nullptr;
+  CK(cudaMalloc(&dx, static_cast<size_t>(n_samples) * ho::kMlpInPad * 2), "cudaMalloc(training inputs)");
+  CK(cudaMalloc(&dt, static_cast<size_t>(n_samples) * ho::kMlpOut * sizeof(float)), "cudaMalloc(training targets)");
+  CK(cudaMalloc(&dv, n_samples), "cudaMalloc");
+  int rc = ho::launch_datagen(c->N, c->d_rec, c->d_box, c->d_desc, c->n_elem, n_samples, seed, dx, dt, dv, c->stream);
+  if (rc) return cuda_fail(c, rc, "training-pair kernel");
+  std::vector<float> hist;
+  rc = c->mlp.train(dx, dt, dv, n_samples, steps, batch, lr, seed, hist, c->stream);
+  cudaFree(dx);
+  cudaFree(dt);
+  cudaFree(dv);
+  if (rc) return cuda_fail(c, rc, "training");
+  if (losses) std::memcpy(losses, hist.data(), hist.size() * sizeof(float));
+  return HO_OK;
+}
+
+// Checkpoint: "HOMLP001", int32 parameter count, FP32 master parameters, then
+// their BF16 copy (round to nearest even) in the same flat order.
+int ho_mlp_save(ho_context* c, const char* path) {
+  if (!c || !path) return HO_ERR_ARG;
+  if (!c->mlp.ready) return fail(c, HO_ERR_STATE, "no network");
+  std::vector<float> flat(ho::kMlpParams);
+  int rc = download_params(c, flat.data(), false);
+  if (rc) return rc;
+  std::vector<uint16_t> hb(flat.size());
+  for (size_t i = 0; i < flat.size(); ++i) {
+    uint32_t u;
+    std::memcpy(&u, &flat[i], 4);
+    hb[i] = static_cast<uint16_t>((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+  }
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(c, HO_ERR_IO, std::string("cannot write ") + path);
+  const int32_t cnt = ho::kMlpParams;
+  bool ok = std::fwrite("HOMLP001", 1, 8, f) == 8 && std::fwrite(&cnt, 4, 1, f) == 1 &&
+            std::fwrite(flat.data(), 4, flat.size(), f) == flat.size() &&
+            std::fwrite(hb.data(), 2, hb.size(), f) == hb.size();
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? HO_OK : fail(c, HO_ERR_IO, std::string("short write to ") + path);
+}
+
+int ho_mlp_load(ho_context* c, const char* path) {
+  if (!c || !path) return HO_ERR_ARG;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(c, HO_ERR_IO, std::string("cannot read ") + path);
+  char magic[8];
+  int32_t cnt = 0;
+  std::vector<float> flat(ho::kMlpParams);
+  const bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "HOMLP001", 8) == 0 &&
+                  std::fread(&cnt, 4, 1, f) == 1 && cnt == ho::kMlpParams &&
+                  std::fread(flat.data(), 4, flat.size(), f) == flat.size();
+  std::fclose(f);
+  if (!ok) return fail(c, HO_ERR_PARSE, std::string("not a network checkpoint: ") + path);
+  return ho_mlp_set_params(c, flat.data());
 }
 
 int ho_get_stats(ho_context* c, ho_stats* out) {

@@ -291,9 +291,9 @@ __device__ __forceinline__ void invert3(const float (&J)[9], float (&K)[9]) {
 // A NaN iterate can never converge, so it stops early with the same answer.
 template <int N>
 __device__ __forceinline__ bool inverse_map(const Elem<N>& e, float3 p, float3& xi, Work& w,
-                                            float3 xi0 = make_float3(0.f, 0.f, 0.f)) {
+                                            float3 xi0 = make_float3(0.f, 0.f, 0.f), int max_it = 50) {
   xi = xi0;
-  for (int it = 0; it < 50; ++it) {
+  for (int it = 0; it < max_it; ++it) {
     ++w.newton;
     float3 x;
     float J[9], K[9];
@@ -322,9 +322,9 @@ struct Sample {
 
 template <int N>
 __device__ __forceinline__ bool sample_along(const Elem<N>& e, float3 o, float3 d, float t, float iso, Sample& s,
-                                             Work& w, float3 xi0 = make_float3(0.f, 0.f, 0.f)) {
+                                             Work& w, float3 xi0 = make_float3(0.f, 0.f, 0.f), int max_it = 50) {
   const float3 p = make_float3(o.x + t * d.x, o.y + t * d.y, o.z + t * d.z);
-  if (!inverse_map<N>(e, p, s.xi, w, xi0)) return false;
+  if (!inverse_map<N>(e, p, s.xi, w, xi0, max_it)) return false;
   float u;
   float3 gr;
   field_eval<N>(e, s.xi, u, gr, w);
@@ -339,23 +339,45 @@ __device__ __forceinline__ bool sample_along(const Elem<N>& e, float3 o, float3 
   return true;
 }
 
+// Learned-mode sample: Newton from a predicted xi with a short iteration cap;
+// if that does not converge the plain cold-start solve answers (the fallback
+// the learned guess never replaces).
+constexpr int kWarmCap = 12;
+template <int N>
+__device__ __forceinline__ bool sample_warm(const Elem<N>& e, float3 o, float3 d, float t, float iso, Sample& s,
+                                            Work& w, bool warm, float3 xi0) {
+  if (warm) {
+    if (sample_along<N>(e, o, d, t, iso, s, w, xi0, kWarmCap)) {
+      ++w.accepted;
+      return true;
+    }
+    ++w.rejected;
+  }
+  return sample_along<N>(e, o, d, t, iso, s, w);
+}
+
+__device__ __forceinline__ float3 lerp3(float3 a, float3 b, float u) {
+  return make_float3(a.x + u * (b.x - a.x), a.y + u * (b.y - a.y), a.z + u * (b.z - a.z));
+}
+
 // At most 20 safeguarded Newton/bisection steps on a bracket [lt, rt] whose
 // left sample is ls; done when |f| < 1e-5, else the midpoint with the left
 // sample's xi and gradient (RayIsosurface.cu:121-177).
 template <int N>
 __device__ __forceinline__ bool refine_bracket(const Elem<N>& e, float3 o, float3 d, float iso, float lt, float rt,
-                                               Sample ls, float& th, float3& xh, float3& gh, Work& w) {
+                                               Sample ls, float& th, float3& xh, float3& gh, Work& w,
+                                               bool warm = false, float3 rxi = make_float3(0.f, 0.f, 0.f)) {
   for (int it = 0; it < 20; ++it) {
     const float mt = 0.5f * (lt + rt);
     Sample ms;
-    if (!sample_along<N>(e, o, d, mt, iso, ms, w)) return false;
+    if (!sample_warm<N>(e, o, d, mt, iso, ms, w, warm, lerp3(ls.xi, rxi, 0.5f))) return false;
     float ct = mt;
     if (fabsf(ms.df) > 1e-8f) {
       const float nt = mt - ms.f / ms.df;
       if (nt > lt && nt < rt) ct = nt;
     }
     Sample cs;
-    if (!sample_along<N>(e, o, d, ct, iso, cs, w)) {
+    if (!sample_warm<N>(e, o, d, ct, iso, cs, w, warm, ms.xi)) {
       ct = mt;  // keep the failed solve's xi, as the reference does
       cs.f = ms.f;
       cs.g = ms.g;
@@ -368,6 +390,7 @@ __device__ __forceinline__ bool refine_bracket(const Elem<N>& e, float3 o, float
     }
     if (ls.f * cs.f <= 0.0f) {
       rt = ct;
+      rxi = cs.xi;
     } else {
       lt = ct;
       ls = cs;
@@ -419,9 +442,21 @@ __device__ __forceinline__ float3 shfl3(float3 v, int src) {
 // the same bracket the sequential scan stops at. The refinement is then run
 // by every lane on identical data (uniform control flow); its work is
 // counted in wu, which only lane 0 reports. Call with all 32 lanes.
+// Learned prediction for one candidate: xi at the segment entry te and
+// d xi / d t there (scaled by the element size: xi(t) ~ xi_in + (t-te)*k*v).
+struct Pred {
+  bool on;
+  float3 xi_in, v;
+  float k, te;
+  __device__ __forceinline__ float3 at(float t) const {
+    const float u = (t - te) * k;
+    return make_float3(xi_in.x + u * v.x, xi_in.y + u * v.y, xi_in.z + u * v.z);
+  }
+};
+
 template <int N>
 __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, float t1, float iso, float& th,
-                              float3& xh, float3& gh, Work& w, Work& wu) {
+                              float3& xh, float3& gh, Work& w, Work& wu, const Pred& pr) {
   const int lane = threadIdx.x & 31;
   Sample s;
   s.f = 0.f;
@@ -430,7 +465,7 @@ __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, fl
   s.g = s.xi;
   const float t = t0 + (t1 - t0) * (float(lane) / 16.0f);
   bool ok = false;
-  if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w);
+  if (lane <= 16) ok = sample_warm<N>(e, o, d, t, iso, s, w, pr.on, pr.on ? pr.at(t) : s.xi);
   const unsigned okm = __ballot_sync(kFull, ok);
   const unsigned below = okm & ((1u << lane) - 1u);
   const int prev = below ? 31 - __clz(below) : lane;
@@ -446,7 +481,8 @@ __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, fl
   ls.df = __shfl_sync(kFull, s.df, li);
   ls.xi = shfl3(s.xi, li);
   ls.g = shfl3(s.g, li);
-  return refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu);
+  const float3 rxi = shfl3(s.xi, ri);
+  return refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, pr.on, rxi);
 }
 
 // Slab test clipped to [tmin, tmax] (high_order.h:115-152).
@@ -498,6 +534,10 @@ __device__ __forceinline__ void setc(float3& v, int a, float s) {
 // in [tmin,tmax]; step clamp 0.25, divergence break after 5 iterations
 // (high_order.h:213-300).
 template <int N>
+__device__ bool face_newton(const Elem<N>& e, float3 o, float3 d, int f, float3 p, float tau, float tmin, float tmax,
+                            float& th, float3& xh, Work& w, int max_it);
+
+template <int N>
 __device__ bool face_seed(const Elem<N>& e, float3 o, float3 d, int f, int si, int sj, float tmin, float tmax,
                           float& th, float3& xh, Work& w) {
   int fixed, ua, va;
@@ -512,8 +552,18 @@ __device__ bool face_seed(const Elem<N>& e, float3 o, float3 d, int f, int si, i
   const float3 df = make_float3(x0.x - o.x, x0.y - o.y, x0.z - o.z);
   float tau = dd > 0.f ? (df.x * d.x + df.y * d.y + df.z * d.z) / dd : 0.f;
   tau = fminf(fmaxf(tau, tmin), tmax);
+  return face_newton<N>(e, o, d, f, p, tau, tmin, tmax, th, xh, w, 50);
+}
+
+// The (u,v,tau) Newton of one seed from a given start point.
+template <int N>
+__device__ bool face_newton(const Elem<N>& e, float3 o, float3 d, int f, float3 p, float tau, float tmin, float tmax,
+                            float& th, float3& xh, Work& w, int max_it) {
+  int fixed, ua, va;
+  float val;
+  face_param(f, fixed, val, ua, va);
   float prev = FLT_MAX;
-  for (int it = 0; it < 50; ++it) {
+  for (int it = 0; it < max_it; ++it) {
     ++w.face;
     float3 X;
     float J[9];
@@ -676,21 +726,77 @@ __device__ __forceinline__ bool face_may_hit(const float* __restrict__ fbox, int
 // most 6 x 9 = 54, two per lane). For each face the lowest seed index that
 // was accepted answers — the seed the sequential loop would stop at — and
 // faces are then compared in index order as the reference does.
+// Where the predicted xi-line enters [-1,1]^3: face, start point, t.
+__device__ __forceinline__ bool predicted_entry(const Pred& pr, float tmin, float tmax, int& face, float3& p,
+                                                float& tau) {
+  const float a[3] = {pr.xi_in.x, pr.xi_in.y, pr.xi_in.z};
+  const float v[3] = {pr.v.x * pr.k, pr.v.y * pr.k, pr.v.z * pr.k};
+  float enter = -FLT_MAX, leave = FLT_MAX;
+  int ax = -1;
+  float side = 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    if (fabsf(v[c]) < 1e-12f) {
+      if (fabsf(a[c]) > 1.f) return false;
+      continue;
+    }
+    const float t0 = pr.te + (-1.f - a[c]) / v[c], t1 = pr.te + (1.f - a[c]) / v[c];
+    const float lo = fminf(t0, t1), hi = fmaxf(t0, t1);
+    if (lo > enter) {
+      enter = lo;
+      ax = c;
+      side = (t0 < t1) ? -1.f : 1.f;
+    }
+    leave = fminf(leave, hi);
+  }
+  if (ax < 0 || enter > leave || enter > tmax || leave < tmin) return false;
+  // face table (high_order.h:164-184): (axis, side) -> face index
+  face = ax == 2 ? (side < 0.f ? 0 : 5) : (ax == 1 ? (side < 0.f ? 1 : 3) : (side < 0.f ? 4 : 2));
+  tau = fminf(fmaxf(enter, tmin), tmax);
+  p = pr.at(tau);
+  setc(p, ax, side);
+  return true;
+}
+
 template <int N>
 __device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, float3 o, float3 d, float tmin,
-                             float tmax, float& th, float3& xh, int& face, Work& w, Work& wu) {
+                             float tmax, float& th, float3& xh, int& face, Work& w, Work& wu, const Pred& pr) {
   const int lane = threadIdx.x & 31;
   unsigned packed = 0;
   int na = 0;
+  // learned: one Newton solve from the predicted element entry; faces whose
+  // hull box misses [tmin, t_learned] cannot hold a nearer hit and are skipped
+  int lf = -1;
+  float lt = 0.f;
+  float3 lx = make_float3(0.f, 0.f, 0.f);
+  if (pr.on) {
+    float3 p0;
+    float tau0;
+    int f0;
+    if (predicted_entry(pr, tmin, tmax, f0, p0, tau0) &&
+        face_newton<N>(e, o, d, f0, p0, tau0, tmin, tmax, lt, lx, wu, kWarmCap)) {
+      lf = f0;
+      ++wu.accepted;
+    } else {
+      ++wu.rejected;
+    }
+  }
+  const float cull_hi = lf >= 0 ? lt : tmax;
   for (int f = 0; f < 6; ++f) {
-    if (face_may_hit(fbox, f, o, d, tmin, tmax)) {
+    if (f != lf && face_may_hit(fbox, f, o, d, tmin, cull_hi)) {
       packed |= static_cast<unsigned>(f) << (3 * na);
       ++na;
-    } else {
+    } else if (f != lf) {
       ++wu.culled;
     }
   }
-  if (na == 0) return false;
+  if (na == 0) {
+    if (lf < 0 || !(lt > tmin && lt < tmax)) return false;
+    th = lt;
+    xh = lx;
+    face = lf;
+    return true;
+  }
   const int T = na * 9;
   bool ok[2] = {false, false};
   float tv[2] = {0.f, 0.f};
@@ -706,21 +812,31 @@ __device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, f
   }
   bool any = false;
   float best = tmax;
-  for (int a = 0; a < na; ++a) {
-    const int k0 = lane, k1 = lane + 32;
-    const unsigned b0 = __ballot_sync(kFull, ok[0] && k0 / 9 == a);
-    const unsigned b1 = __ballot_sync(kFull, ok[1] && k1 < T && k1 / 9 == a);
-    if ((b0 | b1) == 0u) continue;
-    const bool second = b0 == 0u;
-    const int src = second ? __ffs(b1) - 1 : __ffs(b0) - 1;
-    const float tA = __shfl_sync(kFull, tv[0], src), tB = __shfl_sync(kFull, tv[1], src);
-    const float3 xA = shfl3(xv[0], src), xB = shfl3(xv[1], src);
-    const float tf = second ? tB : tA;
-    const float3 xf = second ? xB : xA;
+  int a = 0;  // next surviving slot, in increasing face order
+  for (int f = 0; f < 6; ++f) {
+    float tf;
+    float3 xf;
+    if (f == lf) {
+      tf = lt;
+      xf = lx;
+    } else {
+      if (a >= na || static_cast<int>((packed >> (3 * a)) & 7u) != f) continue;
+      const int k0 = lane, k1 = lane + 32;
+      const unsigned b0 = __ballot_sync(kFull, ok[0] && k0 / 9 == a);
+      const unsigned b1 = __ballot_sync(kFull, ok[1] && k1 < T && k1 / 9 == a);
+      ++a;
+      if ((b0 | b1) == 0u) continue;
+      const bool second = b0 == 0u;
+      const int src = second ? __ffs(b1) - 1 : __ffs(b0) - 1;
+      const float tA = __shfl_sync(kFull, tv[0], src), tB = __shfl_sync(kFull, tv[1], src);
+      const float3 xA = shfl3(xv[0], src), xB = shfl3(xv[1], src);
+      tf = second ? tB : tA;
+      xf = second ? xB : xA;
+    }
     if (tf > tmin && tf < best) {
       best = tf;
       xh = xf;
-      face = (packed >> (3 * a)) & 7u;
+      face = f;
       any = true;
     }
   }
@@ -731,11 +847,11 @@ __device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, f
 // Warp version of visit_candidate: every lane holds the same `best`.
 template <int N>
 __device__ void visit_warp(const Elem<N>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d, float te,
-                           float tx, float iso, bool iso_on, HitState& best, Work& w, Work& wu) {
+                           float tx, float iso, bool iso_on, HitState& best, Work& w, Work& wu, const Pred& pr) {
   ++wu.cand;
   float th;
   float3 xi, g;
-  if (iso_on && e.has_field && find_iso_warp<N>(e, o, d, te, tx, iso, th, xi, g, w, wu)) {
+  if (iso_on && e.has_field && find_iso_warp<N>(e, o, d, te, tx, iso, th, xi, g, w, wu, pr)) {
     if (th > 0.001f && th < best.t) {
       float3 n = normalize3(g);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
@@ -750,7 +866,7 @@ __device__ void visit_warp(const Elem<N>& e, const float* __restrict__ fbox, int
     return;
   }
   int face = -1;
-  if (hit_hex_warp<N>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu)) {
+  if (hit_hex_warp<N>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu, pr)) {
     if (th > 0.001f && th < best.t) {
       float3 x;
       float J[9];

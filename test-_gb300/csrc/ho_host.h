@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "ho_layout.h"
+#include "ho_mlp.h"
 #include "horender.h"
 
 namespace ho {
@@ -99,6 +100,13 @@ struct ho_context {
   size_t rgb_cap = 0;
   float* d_rays = nullptr;
   size_t rays_cap = 0;
+  // learned mode
+  ho::Mlp mlp;
+  float* d_desc = nullptr;        // n_elem * 48 element descriptors
+  void* d_feat = nullptr;         // network inputs, [queue item][kPredK][64] BF16
+  float* d_pred = nullptr;        // network outputs, [queue item][kPredK][8]
+  int32_t* d_cand = nullptr;      // elements the predictions belong to
+  size_t pred_cap = 0;
   int32_t* d_work = nullptr;      // query queue of the intersect pass
   size_t work_cap = 0;
   unsigned* d_qctr = nullptr;     // [0] queue length, [1] next item

@@ -1,0 +1,35 @@
+// Learned mode: element descriptors, network inputs, training-pair generation.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ho_mlp.h"
+
+namespace ho {
+
+constexpr int kDescFloats = 48;  // see ho_learn.cu
+constexpr int kPredK = 4;        // candidates per queued ray that get a prediction
+
+// Network input of one (ray, element) pair, BF16 x 64 (48 used).
+__device__ __forceinline__ void write_features(const float* __restrict__ desc, float3 o, float3 d, float te,
+                                               __nv_bfloat16* __restrict__ row) {
+  const float k = desc[45];
+  const float px = (o.x + te * d.x - desc[42]) * k, py = (o.y + te * d.y - desc[43]) * k,
+              pz = (o.z + te * d.z - desc[44]) * k;
+  for (int j = 0; j < 42; j += 2)
+    *reinterpret_cast<__nv_bfloat162*>(row + j) = __floats2bfloat162_rn(desc[j], desc[j + 1]);
+  *reinterpret_cast<__nv_bfloat162*>(row + 42) = __floats2bfloat162_rn(px, py);
+  *reinterpret_cast<__nv_bfloat162*>(row + 44) = __floats2bfloat162_rn(pz, d.x);
+  *reinterpret_cast<__nv_bfloat162*>(row + 46) = __floats2bfloat162_rn(d.y, d.z);
+  const __nv_bfloat162 z = __floats2bfloat162_rn(0.f, 0.f);
+  for (int j = 48; j < kMlpInPad; j += 2) *reinterpret_cast<__nv_bfloat162*>(row + j) = z;
+}
+
+int launch_desc(int N, const float* rec, int64_t n, float* desc, cudaStream_t s);
+int launch_datagen(int N, const float* rec, const float* box, const float* desc, int64_t n_elem, int64_t n,
+                   uint64_t seed, void* X, float* T, uint8_t* V, cudaStream_t s);
+
+}  // namespace ho

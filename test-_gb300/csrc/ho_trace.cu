@@ -55,6 +55,37 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
   flush_work(P.stats, w, q < n_queries);
 }
 
+// Learned mode, after classify: the first kPredK ordered candidates of each
+// queued ray (the same as the intersect pass's first candidates: nothing is
+// hit yet) and the network input of each (ray, candidate) pair.
+__global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16* __restrict__ X,
+                                                   int32_t* __restrict__ cand_e) {
+  const unsigned n_work = *P.qcount;
+  Work w;
+  for (int64_t item = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; item < n_work;
+       item += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t q = P.work[item];
+    float3 o, d;
+    int iso_idx;
+    query_ray(P, q, o, d, iso_idx);
+    float bt[kCandK];
+    int be[kCandK];
+    bool overflow;
+    const bool ok = collect(P, o, d, FLT_MAX, -FLT_MAX, -1, bt, be, overflow, w);
+#pragma unroll
+    for (int j = 0; j < kPredK; ++j) {
+      const int e = (ok && be[j] != INT_MAX) ? be[j] : -1;
+      cand_e[item * kPredK + j] = e;
+      __nv_bfloat16* row = X + (item * kPredK + j) * kMlpInPad;
+      if (e >= 0) {
+        write_features(P.desc + static_cast<int64_t>(e) * kDescFloats, o, d, bt[j], row);
+      } else {
+        for (int c = 0; c < kMlpInPad; ++c) row[c] = __float2bfloat16(0.f);
+      }
+    }
+  }
+}
+
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   TraceParams P;
   P.nodes = c->d_nodes;
@@ -110,16 +141,47 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return int(e);
   }
+  const bool learned = c->mode == HO_MODE_LEARNED && c->mlp.trained;
+  P.desc = c->d_desc;
+  P.cand_e = nullptr;
+  P.pred = nullptr;
+  if (learned) {
+    const size_t rows = static_cast<size_t>(n_queries) * kPredK;
+    if (rows > c->pred_cap) {
+      cudaFree(c->d_feat);
+      cudaFree(c->d_pred);
+      cudaFree(c->d_cand);
+      c->d_feat = nullptr;
+      c->d_pred = nullptr;
+      c->d_cand = nullptr;
+      c->pred_cap = 0;
+      cudaError_t e = cudaMalloc(&c->d_feat, rows * kMlpInPad * sizeof(__nv_bfloat16));
+      if (e == cudaSuccess) e = cudaMalloc(&c->d_pred, rows * kMlpOut * sizeof(float));
+      if (e == cudaSuccess) e = cudaMalloc(&c->d_cand, rows * sizeof(int32_t));
+      if (e != cudaSuccess) return int(e);
+      c->pred_cap = rows;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cand_kernel<<<sms * 8, 128, 0, s>>>(P, static_cast<__nv_bfloat16*>(c->d_feat), c->d_cand);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return int(e);
+    const int rc = mlp_infer(c->mlp.dev(), c->d_feat, 0, c->d_qctr, kPredK, c->d_pred, s, sms);
+    if (rc) return rc;
+    P.cand_e = c->d_cand;
+    P.pred = c->d_pred;
+  }
   cudaError_t e;
   switch (c->N) {
-    case 2: e = launch_n<2>(P, n_queries, n_threads, s); break;
-    case 3: e = launch_n<3>(P, n_queries, n_threads, s); break;
-    case 4: e = launch_n<4>(P, n_queries, n_threads, s); break;
-    case 5: e = launch_n<5>(P, n_queries, n_threads, s); break;
-    case 6: e = launch_n<6>(P, n_queries, n_threads, s); break;
-    case 7: e = launch_n<7>(P, n_queries, n_threads, s); break;
-    case 8: e = launch_n<8>(P, n_queries, n_threads, s); break;
-    case 9: e = launch_n<9>(P, n_queries, n_threads, s); break;
+    case 2: e = launch_n<2>(P, n_queries, n_threads, s, learned); break;
+    case 3: e = launch_n<3>(P, n_queries, n_threads, s, learned); break;
+    case 4: e = launch_n<4>(P, n_queries, n_threads, s, learned); break;
+    case 5: e = launch_n<5>(P, n_queries, n_threads, s, learned); break;
+    case 6: e = launch_n<6>(P, n_queries, n_threads, s, learned); break;
+    case 7: e = launch_n<7>(P, n_queries, n_threads, s, learned); break;
+    case 8: e = launch_n<8>(P, n_queries, n_threads, s, learned); break;
+    case 9: e = launch_n<9>(P, n_queries, n_threads, s, learned); break;
     default: return int(cudaErrorInvalidValue);
   }
   return int(e);

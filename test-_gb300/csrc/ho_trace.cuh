@@ -18,6 +18,7 @@
 
 #include "ho_device.cuh"
 #include "ho_host.h"
+#include "ho_learn.h"
 
 namespace ho {
 
@@ -48,6 +49,10 @@ struct TraceParams {
   int32_t* work;      // queue of query indices that meet at least one box
   unsigned* qcount;   // queue length (written by the classify pass)
   unsigned* qnext;    // next queue item to take (intersect pass)
+  // learned mode
+  const float* desc;      // element descriptors (scale k at [45])
+  const int32_t* cand_e;  // [item][kPredK] candidate elements the predictions belong to
+  const float* pred;      // [item][kPredK][8] network outputs
 };
 
 __device__ __forceinline__ bool key_less(float ta, int ea, float tb, int eb) {
@@ -230,7 +235,7 @@ __device__ __forceinline__ HitState miss_state() {
 
 // Pass 2, persistent, one warp per queued query: ordered candidates, each
 // visited with its independent Newton solves spread over the lanes.
-template <int N>
+template <int N, bool LEARNED>
 __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
   const int lane = threadIdx.x & 31;
   constexpr int64_t S = static_cast<int64_t>(N) * N * N;
@@ -251,6 +256,7 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
     const uint32_t it0 = wu.newton + wu.face + w.newton + w.face;
     float kt = -FLT_MAX;
     int ke = -1;
+    int pass = 0;
     for (;;) {
       float bt[kCandK];
       int be[kCandK];
@@ -282,14 +288,25 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
           Elem<N> el;
           el.c = P.rec + static_cast<int64_t>(ce) * 4 * S;
           el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
+          Pred pr;
+          pr.on = false;
+          if (LEARNED && pass == 0 && j < kPredK && P.cand_e[static_cast<int64_t>(item) * kPredK + j] == ce) {
+            const float* y = P.pred + (static_cast<int64_t>(item) * kPredK + j) * kMlpOut;
+            pr.on = true;
+            pr.xi_in = make_float3(y[0], y[1], y[2]);
+            pr.v = make_float3(y[3], y[4], y[5]);
+            pr.k = __ldg(P.desc + static_cast<int64_t>(ce) * kDescFloats + 45);
+            pr.te = te;
+          }
           visit_warp<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on, best,
-                        w, wu);
+                        w, wu, pr);
         }
         kt = ct;
         ke = ce;
       }
       if (done || !overflow) break;
       ++wu.restarts;
+      ++pass;
       best.flags |= HO_FLAG_OVERFLOW;
     }
     // iterations of this query summed over the lanes
@@ -301,34 +318,38 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
   if (lane == 0) {
     w.cand += wu.cand; w.geom += wu.geom; w.map += wu.map; w.field += wu.field; w.newton += wu.newton;
     w.face += wu.face; w.culled += wu.culled; w.nodes += wu.nodes; w.restarts += wu.restarts;
+    w.accepted += wu.accepted; w.rejected += wu.rejected;
   }
   flush_work(P.stats, w, false);
 }
 
 template <int N>
-cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s) {
+cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned) {
   (void)n_threads;
   (void)n_queries;
-  static int grid = 0;  // persistent grid: resident blocks per SM x SMs
-  if (grid == 0) {
+  static int grid[2] = {0, 0};  // persistent grid: resident blocks per SM x SMs
+  int& g = grid[learned ? 1 : 0];
+  if (g == 0) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N>, kTraceBlock, 0);
-    grid = sms * (per > 0 ? per : 1);
+    if (learned) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, true>, kTraceBlock, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, false>, kTraceBlock, 0);
+    g = sms * (per > 0 ? per : 1);
   }
-  isect_kernel<N><<<grid, kTraceBlock, 0, s>>>(P);
+  if (learned) isect_kernel<N, true><<<g, kTraceBlock, 0, s>>>(P);
+  else isect_kernel<N, false><<<g, kTraceBlock, 0, s>>>(P);
   return cudaGetLastError();
 }
 
 // explicit instantiations live in ho_trace_n*.cu
-extern template cudaError_t launch_n<2>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<3>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<4>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<5>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<6>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<7>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<8>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
-extern template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s);
+extern template cudaError_t launch_n<2>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<3>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<4>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<5>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<6>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<7>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<8>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
 
 }  // namespace ho

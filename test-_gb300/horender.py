@@ -23,6 +23,7 @@ HO_OK = 0
 ERRORS = {-1: "HO_ERR_ARG", -2: "HO_ERR_CUDA", -3: "HO_ERR_STATE", -4: "HO_ERR_IO", -5: "HO_ERR_PARSE",
           -6: "HO_ERR_NOMEM", -7: "HO_ERR_RANGE", -8: "HO_ERR_DEVICE"}
 MODE_PLAIN, MODE_LEARNED, MODE_BATCHED = 0, 1, 2
+MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
 FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW = 1, 2, 4
 
@@ -86,6 +87,15 @@ def _load():
     L.ho_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.ho_save_ppm.argtypes = [vp, i32, i32, C.c_char_p]
     L.ho_measure_fp32_peak.argtypes = [i32, C.POINTER(C.c_double)]
+    L.ho_mlp_init.argtypes = [vp, C.c_uint64]
+    L.ho_mlp_set_params.argtypes = [vp, vp]
+    L.ho_mlp_get_params.argtypes = [vp, vp]
+    L.ho_mlp_forward.argtypes = [vp, vp, i64, vp]
+    L.ho_mlp_grad.argtypes = [vp, vp, vp, vp, i32, vp, vp]
+    L.ho_learn_samples.argtypes = [vp, i64, C.c_uint64, vp, vp, vp]
+    L.ho_train_mlp.argtypes = [vp, i64, i32, i32, f32, C.c_uint64, vp]
+    L.ho_mlp_save.argtypes = [vp, C.c_char_p]
+    L.ho_mlp_load.argtypes = [vp, C.c_char_p]
     return L
 
 
@@ -261,6 +271,53 @@ class Context:
     def intersect_device(self, n: int, rays_ptr: int, iso: float, iso_enabled: bool, out_ptr: int, stream_ptr):
         self._ck(lib.ho_intersect_device(self.h, int(n), rays_ptr, float(iso), int(iso_enabled), out_ptr,
                                          stream_ptr))
+
+    # ---- learned mode ----------------------------------------------------------
+    def mlp_init(self, seed: int = 0):
+        self._ck(lib.ho_mlp_init(self.h, int(seed)))
+
+    def mlp_params(self) -> np.ndarray:
+        out = np.zeros(MLP_PARAMS, np.float32)
+        self._ck(lib.ho_mlp_get_params(self.h, _p(out)))
+        return out
+
+    def mlp_set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == MLP_PARAMS
+        self._ck(lib.ho_mlp_set_params(self.h, _p(p)))
+
+    def mlp_forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, MLP_IN)
+        Y = np.zeros((X.shape[0], MLP_OUT), np.float32)
+        self._ck(lib.ho_mlp_forward(self.h, _p(X), X.shape[0], _p(Y)))
+        return Y
+
+    def mlp_grad(self, X, T, valid):
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, MLP_IN)
+        T = np.ascontiguousarray(T, np.float32).reshape(-1, MLP_OUT)
+        valid = np.ascontiguousarray(valid, np.uint8)
+        loss = np.zeros(1, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        self._ck(lib.ho_mlp_grad(self.h, _p(X), _p(T), _p(valid), X.shape[0], _p(loss), _p(g)))
+        return float(loss[0]), g
+
+    def learn_samples(self, n: int, seed: int = 0):
+        X = np.zeros((n, MLP_IN), np.float32)
+        T = np.zeros((n, MLP_OUT), np.float32)
+        V = np.zeros(n, np.uint8)
+        self._ck(lib.ho_learn_samples(self.h, n, int(seed), _p(X), _p(T), _p(V)))
+        return X, T, V
+
+    def train_mlp(self, n_samples=2_000_000, steps=1500, batch=4096, lr=2e-3, seed=0) -> np.ndarray:
+        losses = np.zeros(steps, np.float32)
+        self._ck(lib.ho_train_mlp(self.h, int(n_samples), int(steps), int(batch), float(lr), int(seed), _p(losses)))
+        return losses
+
+    def mlp_save(self, path: str):
+        self._ck(lib.ho_mlp_save(self.h, str(path).encode()))
+
+    def mlp_load(self, path: str):
+        self._ck(lib.ho_mlp_load(self.h, str(path).encode()))
 
     def stats(self) -> dict:
         s = _Stats()

@@ -6,7 +6,8 @@ except on rays where the reference's answer depends on its BVH visit order
 (the oracle's ascending-entry order gives a different answer there too,
 and the fixture's recorded reference order reproduces the reference's);
 those rays are counted, not failed. Against the ordered oracle the GPU must
-agree on >= 99.5% of rays (the rest are FP32 near-ties, counted), with t
+agree on >= 99.5% of rays, or all but 2 on small samples (the rest are FP32
+near-ties, counted), with t
 within 2e-4 where the identities agree.
 """
 from __future__ import annotations
@@ -39,8 +40,10 @@ def _compare(ctx, osc, rays, iso, ref_tr, label):
     unexplained = ~g_ref & ~order_dep
     print(f"{label}: rays {rays.shape[0]}, gpu==ref {g_ref.mean():.4f}, order-dependent {order_dep.sum()}, "
           f"gpu!=ref otherwise {unexplained.sum()}, gpu==oracle {g_o.mean():.4f}")
-    assert g_o.mean() >= 0.995
-    assert unexplained.mean() <= 0.005
+    n = rays.shape[0]
+    allowed = max(2, int(0.005 * n))  # FP32 near-ties (sample-size floor of 2 rays)
+    assert (~g_o).sum() <= allowed
+    assert unexplained.sum() <= allowed
     m = g_ref & (rk > 0)
     if m.any():
         assert np.abs(g["t"][m] - ref_tr[m, 3]).max() < 2e-4
