@@ -49,10 +49,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--mode", default="both", choices=["both", "plain", "learned"],
-                    help="learned: learned-init batched (the headline); plain: the reference algorithm")
+    ap.add_argument("--mode", default="all", choices=["all", "plain", "batched", "learned"],
+                    help="learned: learned-init + batched (the headline); batched: the same kernels with cold "
+                         "starts; plain: one thread per ray, the reference algorithm's structure")
     ap.add_argument("--train-samples", type=int, default=2_000_000)
-    ap.add_argument("--train-steps", type=int, default=1500)
+    ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling)")
     ap.add_argument("--height", type=int, default=0, help="override the workload's image height (profiling)")
     return ap.parse_args()
@@ -281,21 +282,30 @@ def run_gpu(args, rank, world):
         return total, st, clk
 
     train = None
-    if args.mode in ("both", "learned"):
+    if args.mode in ("all", "learned"):
         t0 = time.perf_counter()
         losses = ctx.train_mlp(n_samples=args.train_samples, steps=args.train_steps, batch=4096, lr=2e-3, seed=1)
+        torch.cuda.synchronize()
         train = {"samples": args.train_samples, "steps": args.train_steps, "batch": 4096,
                  "seconds": time.perf_counter() - t0, "loss_first": float(losses[:20].mean()),
                  "loss_last": float(losses[-50:].mean())}
     results = {}
-    for mode in (["plain", "learned"] if args.mode == "both" else [args.mode]):
-        results[mode] = timed(hr.MODE_LEARNED if mode == "learned" else hr.MODE_PLAIN)
-    head = "learned" if "learned" in results else "plain"
+    codes = {"plain": hr.MODE_PLAIN, "batched": hr.MODE_BATCHED, "learned": hr.MODE_LEARNED}
+    for mode in (["plain", "batched", "learned"] if args.mode == "all" else [args.mode]):
+        results[mode] = timed(codes[mode])
+    head = "learned" if "learned" in results else ("batched" if "batched" in results else "plain")
     total_s, st, clk = results[head]
     queries = sum_over_ranks(nq * args.steps, world)
     value = queries / total_s / 1e6
     launch_s = total_s / args.steps
     plain_value = queries / results["plain"][0] / 1e6 if "plain" in results else None
+
+    def mode_summary(m):
+        if m not in results:
+            return None
+        t, stt, _ = results[m]
+        return {"value": queries / t / 1e6, "ms_per_step": t / args.steps * 1e3, "newton_iters": stt["newton_iters"],
+                "face_iters": stt["face_iters"], "geom_evals": stt["geom_evals"]}
 
     # roofline of the trace kernel: algorithmic FP32 flops of one launch
     N = info["max_modes"]
@@ -307,7 +317,7 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    ctx.set_mode(hr.MODE_LEARNED if head == "learned" else hr.MODE_PLAIN)
+    ctx.set_mode(codes[head])
     for _ in range(0 if args.no_e2e else args.steps):
         ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
     e2e_s = max(max_over_ranks(time.perf_counter() - t0, world), 1e-9)
@@ -323,11 +333,13 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "impl": "gb300", "mode": "learned-init + batched" if head == "learned" else "plain",
-        "plain": None if plain_value is None else {
-            "value": plain_value, "ms_per_step": results["plain"][0] / args.steps * 1e3,
-            "newton_iters": results["plain"][1]["newton_iters"], "face_iters": results["plain"][1]["face_iters"]},
+        "impl": "gb300", "mode": {"learned": "learned-init + batched", "batched": "batched (cold-start Newton)",
+                                  "plain": "plain (thread per ray, cold-start Newton)"}[head],
+        "plain": mode_summary("plain"),
+        "batched": mode_summary("batched"),
         "speedup_vs_plain": None if plain_value is None else value / plain_value,
+        "speedup_vs_batched": (value / mode_summary("batched")["value"]) if "batched" in results and head != "batched"
+        else None,
         "training": train,
         "config": {"workload": w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes", "order": w.order_max,
                    "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
@@ -340,7 +352,7 @@ def run_gpu(args, rank, world):
                      "flops_per_launch": flops},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4 * n_iso,
                 "d2h_bytes_per_step": nq * 3},
-        "gpu_launches": args.steps * (4 if head == "learned" else 2),
+        "gpu_launches": args.steps * {"learned": 4, "batched": 2, "plain": 1}[head],
         "clocks": clk.summary(),
         "work": st,
         "scene": info,

@@ -30,10 +30,13 @@ extern "C" {
 #define HO_ERR_RANGE (-7)    /* size beyond a documented limit                  */
 #define HO_ERR_DEVICE (-8)   /* a kernel reported an internal error status      */
 
-/* Solver modes (ho_set_mode). */
-#define HO_MODE_PLAIN 0      /* reference algorithm: cold-start Newton, 17-sample iso scan */
-#define HO_MODE_LEARNED 1    /* MLP initial guess + bracket, plain fallback and judge     */
-#define HO_MODE_BATCHED 2    /* element-binned wavefront, one persistent launch           */
+/* Solver modes (ho_set_mode). All three compute the reference's algorithm
+ * (same tolerances, same per-candidate policy); they differ in how the work
+ * is mapped to the GPU and where Newton starts. */
+#define HO_MODE_PLAIN 0      /* one thread per ray, sequential cold-start Newton (the reference's structure) */
+#define HO_MODE_LEARNED 1    /* BATCHED + network-predicted Newton starts; plain cold start as fallback     */
+#define HO_MODE_BATCHED 2    /* default: miss-culling pass + device queue + persistent warp per ray, the
+                                independent Newton solves of a candidate spread over the lanes               */
 
 /* Hit kinds. */
 #define HO_HIT_MISS 0

@@ -423,7 +423,7 @@ int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso
 
 int ho_set_mode(ho_context* c, int mode) {
   if (!c) return HO_ERR_ARG;
-  if (mode == HO_MODE_PLAIN) {
+  if (mode == HO_MODE_PLAIN || mode == HO_MODE_BATCHED) {
     c->mode = mode;
     return HO_OK;
   }

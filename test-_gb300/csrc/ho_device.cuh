@@ -342,7 +342,7 @@ __device__ __forceinline__ bool sample_along(const Elem<N>& e, float3 o, float3 
 // Learned-mode sample: Newton from a predicted xi with a short iteration cap;
 // if that does not converge the plain cold-start solve answers (the fallback
 // the learned guess never replaces).
-constexpr int kWarmCap = 12;
+constexpr int kWarmCap = 4;
 template <int N>
 __device__ __forceinline__ bool sample_warm(const Elem<N>& e, float3 o, float3 d, float t, float iso, Sample& s,
                                             Work& w, bool warm, float3 xi0) {

@@ -71,7 +71,7 @@ struct ho_context {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  int mode = HO_MODE_PLAIN;
+  int mode = HO_MODE_BATCHED;
   ho::HostScene hs;
   bool built = false;
 

@@ -15,6 +15,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -76,14 +77,17 @@ __global__ void __launch_bounds__(128) gemm_bf16(int M, int N, int K, const bf16
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
   const bf16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < K; k0 += kGK) {
+  // split-K: block z takes K range [kb, ke); partial sums are added atomically
+  const int kchunk = (K + gridDim.z - 1) / gridDim.z;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  for (int k0 = kb; k0 < ke; k0 += kGK) {
     for (int q = threadIdx.x; q < kGT * kGK; q += 128) {
       const int r = q / kGK, kk = q % kGK;
       const int m = m0 + r, k = k0 + kk, n = n0 + r;
-      As[r][kk] = (m < M && k < K) ? (TA ? A[static_cast<int64_t>(k) * lda + m] : A[static_cast<int64_t>(m) * lda + k])
-                                   : zero;
-      Bs[r][kk] = (n < N && k < K) ? (TB ? B[static_cast<int64_t>(n) * ldb + k] : B[static_cast<int64_t>(k) * ldb + n])
-                                   : zero;
+      As[r][kk] = (m < M && k < ke) ? (TA ? A[static_cast<int64_t>(k) * lda + m] : A[static_cast<int64_t>(m) * lda + k])
+                                    : zero;
+      Bs[r][kk] = (n < N && k < ke) ? (TB ? B[static_cast<int64_t>(n) * ldb + k] : B[static_cast<int64_t>(k) * ldb + n])
+                                    : zero;
     }
     __syncthreads();
     warp_mma<8>(&As[16 * warp][0], kGK + kGPad, &Bs[0][0], kGK + kGPad, kGK, acc);
@@ -100,7 +104,8 @@ __global__ void __launch_bounds__(128) gemm_bf16(int M, int N, int K, const bf16
         const int n = n0 + nt * 8 + 2 * t + c;
         if (m < M && n < N) {
           float* p = C + static_cast<int64_t>(m) * ldc + n;
-          *p = accumulate ? *p + acc[nt][2 * h + c] : acc[nt][2 * h + c];
+          if (gridDim.z > 1) atomicAdd(p, acc[nt][2 * h + c]);
+          else *p = accumulate ? *p + acc[nt][2 * h + c] : acc[nt][2 * h + c];
         }
       }
     }
@@ -110,7 +115,12 @@ __global__ void __launch_bounds__(128) gemm_bf16(int M, int N, int K, const bf16
 template <bool TA, bool TB>
 static void gemm(cudaStream_t s, int M, int N, int K, const bf16* A, int lda, const bf16* B, int ldb, float* C, int ldc,
                  bool accumulate) {
-  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
+  const int tiles = ((N + kGT - 1) / kGT) * ((M + kGT - 1) / kGT);
+  // long reductions over few output tiles (weight gradients) are split over K
+  int split = 1;
+  if (K >= 1024 && tiles < 64) split = std::min(K / 256, 64 / tiles);
+  if (split > 1 && !accumulate) cudaMemsetAsync(C, 0, sizeof(float) * static_cast<size_t>(M) * ldc, s);
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, split);
   gemm_bf16<TA, TB><<<grid, 128, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc, accumulate ? 1 : 0);
 }
 
@@ -157,12 +167,14 @@ __global__ void loss_kernel(const float* __restrict__ Y, const float* __restrict
   dYf[i] = g;
 }
 
+// out[n] += sum over rows of D[m][n]; block b sums rows [256 b, 256 b + 256)
 __global__ void colsum_kernel(const float* __restrict__ D, int M, int N, float* __restrict__ out) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = threadIdx.x;
   if (n >= N) return;
+  const int m0 = blockIdx.x * 256, m1 = min(M, m0 + 256);
   float s = 0.f;
-  for (int m = 0; m < M; ++m) s += D[static_cast<int64_t>(m) * N + n];
-  out[n] += s;
+  for (int m = m0; m < m1; ++m) s += D[static_cast<int64_t>(m) * N + n];
+  atomicAdd(out + n, s);
 }
 
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
@@ -468,7 +480,7 @@ int Mlp::forward_backward(int B, const void* Xb, const float* Tb, const uint8_t*
     MLP_TRY(cudaMemsetAsync(gb[l], 0, kDims[l + 1] * sizeof(float), s));
   }
   gemm<true, false>(s, kMlpHidden, kMlpOut, B, H[2], kMlpHidden, dY, kMlpOut, gW[3], kMlpOut, false);
-  colsum_kernel<<<1, kMlpOut, 0, s>>>(dYf, B, kMlpOut, gb[3]);
+  colsum_kernel<<<(B + 255) / 256, kMlpOut, 0, s>>>(dYf, B, kMlpOut, gb[3]);
   gemm<false, true>(s, B, kMlpHidden, kMlpOut, dY, kMlpOut, static_cast<const bf16*>(Wb[3]), kMlpOut, dH, kMlpHidden, false);
   for (int l = 2; l >= 0; --l) {
     gelu_back_kernel<<<blocks(static_cast<int64_t>(B) * kMlpHidden), th, 0, s>>>(dH, Z[l],
@@ -477,7 +489,7 @@ int Mlp::forward_backward(int B, const void* Xb, const float* Tb, const uint8_t*
     const bf16* a_in = l > 0 ? H[l - 1] : X;
     const int a_dim = l > 0 ? kMlpHidden : kMlpInPad;
     gemm<true, false>(s, a_dim, kMlpHidden, B, a_in, a_dim, dZ, kMlpHidden, gW[l], kMlpHidden, false);
-    colsum_kernel<<<1, kMlpHidden, 0, s>>>(dZf, B, kMlpHidden, gb[l]);
+    colsum_kernel<<<(B + 255) / 256, kMlpHidden, 0, s>>>(dZf, B, kMlpHidden, gb[l]);
     if (l > 0) gemm<false, true>(s, B, kMlpHidden, kMlpHidden, dZ, kMlpHidden, static_cast<const bf16*>(Wb[l]), kMlpHidden, dH, kMlpHidden, false);
   }
   return int(cudaGetLastError());

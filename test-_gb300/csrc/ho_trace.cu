@@ -133,6 +133,24 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 2 * sizeof(unsigned), s);
     if (e != cudaSuccess) return int(e);
   }
+  const int mode = (c->mode == HO_MODE_LEARNED && !c->mlp.trained) ? HO_MODE_BATCHED : c->mode;
+  if (mode == HO_MODE_PLAIN) {
+    // one thread per query: camera queries are laid out as 8x4 pixel tiles per warp
+    if (!a.rays) n_threads = static_cast<int64_t>((a.width + 7) / 8) * ((a.height + 3) / 4) * 32 * a.n_iso;
+    cudaError_t e;
+    switch (c->N) {
+      case 2: e = launch_n<2>(P, n_queries, n_threads, s, mode); break;
+      case 3: e = launch_n<3>(P, n_queries, n_threads, s, mode); break;
+      case 4: e = launch_n<4>(P, n_queries, n_threads, s, mode); break;
+      case 5: e = launch_n<5>(P, n_queries, n_threads, s, mode); break;
+      case 6: e = launch_n<6>(P, n_queries, n_threads, s, mode); break;
+      case 7: e = launch_n<7>(P, n_queries, n_threads, s, mode); break;
+      case 8: e = launch_n<8>(P, n_queries, n_threads, s, mode); break;
+      case 9: e = launch_n<9>(P, n_queries, n_threads, s, mode); break;
+      default: return int(cudaErrorInvalidValue);
+    }
+    return int(e);
+  }
   P.work = c->d_work;
   P.qcount = c->d_qctr;
   P.qnext = c->d_qctr + 1;
@@ -141,7 +159,7 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return int(e);
   }
-  const bool learned = c->mode == HO_MODE_LEARNED && c->mlp.trained;
+  const bool learned = mode == HO_MODE_LEARNED;
   P.desc = c->d_desc;
   P.cand_e = nullptr;
   P.pred = nullptr;
@@ -174,14 +192,14 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   }
   cudaError_t e;
   switch (c->N) {
-    case 2: e = launch_n<2>(P, n_queries, n_threads, s, learned); break;
-    case 3: e = launch_n<3>(P, n_queries, n_threads, s, learned); break;
-    case 4: e = launch_n<4>(P, n_queries, n_threads, s, learned); break;
-    case 5: e = launch_n<5>(P, n_queries, n_threads, s, learned); break;
-    case 6: e = launch_n<6>(P, n_queries, n_threads, s, learned); break;
-    case 7: e = launch_n<7>(P, n_queries, n_threads, s, learned); break;
-    case 8: e = launch_n<8>(P, n_queries, n_threads, s, learned); break;
-    case 9: e = launch_n<9>(P, n_queries, n_threads, s, learned); break;
+    case 2: e = launch_n<2>(P, n_queries, n_threads, s, mode); break;
+    case 3: e = launch_n<3>(P, n_queries, n_threads, s, mode); break;
+    case 4: e = launch_n<4>(P, n_queries, n_threads, s, mode); break;
+    case 5: e = launch_n<5>(P, n_queries, n_threads, s, mode); break;
+    case 6: e = launch_n<6>(P, n_queries, n_threads, s, mode); break;
+    case 7: e = launch_n<7>(P, n_queries, n_threads, s, mode); break;
+    case 8: e = launch_n<8>(P, n_queries, n_threads, s, mode); break;
+    case 9: e = launch_n<9>(P, n_queries, n_threads, s, mode); break;
     default: return int(cudaErrorInvalidValue);
   }
   return int(e);

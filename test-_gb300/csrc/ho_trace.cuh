@@ -323,10 +323,94 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
   flush_work(P.stats, w, false);
 }
 
+// Plain form: the reference's structure on the GPU — one thread per query
+// (camera rays: a warp covers an 8x4 pixel tile), its own ordered candidate
+// loop, each candidate visited with the sequential cold-start algorithm
+// (visit_candidate). No queue, no lane-parallel solves, no prediction.
 template <int N>
-cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned) {
-  (void)n_threads;
-  (void)n_queries;
+__global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64_t n_queries) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x) >> 5;
+  int64_t q;
+  float3 o = make_float3(0.f, 0.f, 0.f), d = make_float3(0.f, 0.f, 1.f);
+  int iso_idx = 0;
+  bool active;
+  if (P.rays == nullptr) {
+    const int tx_n = (P.cam.width + 7) >> 3, ty_n = (P.cam.height + 3) >> 2;
+    const int64_t tiles = static_cast<int64_t>(tx_n) * ty_n;
+    const int it = static_cast<int>(wid / tiles);
+    const int64_t tile = wid - static_cast<int64_t>(it) * tiles;
+    const int x = static_cast<int>(tile % tx_n) * 8 + (lane & 7);
+    const int y = static_cast<int>(tile / tx_n) * 4 + (lane >> 3);
+    active = it < P.n_iso && x < P.cam.width && y < P.cam.height;
+    q = static_cast<int64_t>(it) * P.cam.width * P.cam.height + static_cast<int64_t>(y) * P.cam.width + x;
+  } else {
+    q = static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x;
+    active = q < n_queries;
+  }
+  if (active) query_ray(P, q, o, d, iso_idx);
+  Work w;
+  HitState best = miss_state();
+  if (active) {
+    const float iso = P.iso[iso_idx];
+    const bool iso_on = (P.iso_on_mask >> iso_idx) & 1u;
+    constexpr int64_t S = static_cast<int64_t>(N) * N * N;
+    float kt = -FLT_MAX;
+    int ke = -1;
+    for (;;) {
+      float bt[kCandK];
+      int be[kCandK];
+      bool overflow;
+      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, w)) {
+        atomicOr(&P.stats->status, kStatusStackOverflow);
+        break;
+      }
+      bool done = false;
+#pragma unroll 1
+      for (int j = 0; j < kCandK; ++j) {
+        float ct = bt[0];
+        int ce = be[0];
+#pragma unroll
+        for (int m = 1; m < kCandK; ++m)
+          if (j == m) {
+            ct = bt[m];
+            ce = be[m];
+          }
+        if (ce == INT_MAX || ct > best.t) {
+          done = true;
+          break;
+        }
+        const float* b = P.box + 6 * static_cast<int64_t>(ce);
+        const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
+        const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
+        float te, tx;
+        if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
+          Elem<N> el;
+          el.c = P.rec + static_cast<int64_t>(ce) * 4 * S;
+          el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
+          visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
+                             best, w);
+        }
+        kt = ct;
+        ke = ce;
+      }
+      if (done || !overflow) break;
+      ++w.restarts;
+      best.flags |= HO_FLAG_OVERFLOW;
+    }
+  }
+  flush_work(P.stats, w, active);
+  if (active) write_result(P, q, d, best, w.newton + w.face);
+}
+
+template <int N>
+cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode) {
+  if (mode == HO_MODE_PLAIN) {
+    const int64_t blocks = (n_threads + kTraceBlock - 1) / kTraceBlock;
+    plain_kernel<N><<<static_cast<unsigned>(blocks), kTraceBlock, 0, s>>>(P, n_queries);
+    return cudaGetLastError();
+  }
+  const bool learned = mode == HO_MODE_LEARNED;
   static int grid[2] = {0, 0};  // persistent grid: resident blocks per SM x SMs
   int& g = grid[learned ? 1 : 0];
   if (g == 0) {
@@ -343,13 +427,13 @@ cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads,
 }
 
 // explicit instantiations live in ho_trace_n*.cu
-extern template cudaError_t launch_n<2>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<3>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<4>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<5>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<6>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<7>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<8>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
-extern template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+extern template cudaError_t launch_n<2>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<3>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<4>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<5>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<6>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<7>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<8>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
+extern template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
 
 }  // namespace ho

@@ -2,5 +2,5 @@
 #include "ho_trace.cuh"
 
 namespace ho {
-template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, bool learned);
+template cudaError_t launch_n<9>(const TraceParams& P, int64_t n_queries, int64_t n_threads, cudaStream_t s, int mode);
 }  // namespace ho

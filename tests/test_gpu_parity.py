@@ -66,6 +66,19 @@ def test_render_hits_match_oracle(small, oracle, iso_on):
     assert ((h["kind"] == 0) == (ref["kind"] == 0)).mean() >= 0.999
 
 
+def test_plain_and_batched_modes_agree(small):
+    ctx, w, arrs, osc = small
+    W = H = 96
+    ctx.set_mode(hr.MODE_PLAIN)
+    _, hp = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    sp = ctx.stats()
+    ctx.set_mode(hr.MODE_BATCHED)
+    _, hb = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    same = classify(hp[0].reshape(-1), hb[0].reshape(-1))
+    assert same.mean() >= 0.999
+    assert sp["rays"] == W * H
+
+
 def test_intersect_explicit_rays_matches_render(small):
     ctx, w, arrs, osc = small
     W = H = 64
