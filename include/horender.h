@@ -118,6 +118,9 @@ typedef struct {
   uint64_t restarts;         /* candidate-list overflows                       */
   int32_t max_modes;
   int32_t status;            /* device error status (0 = fine)                 */
+  uint64_t phase_cycles[4];  /* batched/learned: SM cycles spent per warp in
+                                traversal, isosurface scan, bracket refinement,
+                                face search (summed over warps)                */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

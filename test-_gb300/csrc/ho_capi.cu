@@ -122,6 +122,7 @@ int read_stats(ho_context* c) {
   s.mlp_accepted = ds.c[ho::ST_ACCEPT];
   s.mlp_rejected = ds.c[ho::ST_REJECT];
   s.restarts = ds.c[ho::ST_RESTART];
+  for (int k = 0; k < 4; ++k) s.phase_cycles[k] = ds.c[ho::ST_CYC_TRAV + k];
   s.max_modes = c->N;
   s.status = ds.status;
   if (ds.status != 0)

@@ -29,6 +29,9 @@ namespace ho {
 struct Work {
   uint32_t cand = 0, geom = 0, map = 0, field = 0, newton = 0, face = 0, culled = 0, nodes = 0, restarts = 0;
   uint32_t accepted = 0, rejected = 0;
+  // SM cycles by phase (warp kernels, counted on lane 0): traversal, isosurface
+  // scan, bracket refinement, face search
+  unsigned long long cyc[4] = {0, 0, 0, 0};
 };
 
 // ---------------------------------------------------------------------------
@@ -463,9 +466,41 @@ __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, fl
   s.df = 0.f;
   s.xi = make_float3(0.f, 0.f, 0.f);
   s.g = s.xi;
+  const long long c0 = clock64();
   const float t = t0 + (t1 - t0) * (float(lane) / 16.0f);
   bool ok = false;
-  if (lane <= 16) ok = sample_warm<N>(e, o, d, t, iso, s, w, pr.on, pr.on ? pr.at(t) : s.xi);
+  if (!pr.on) {
+    if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w);
+  } else {
+    // learned: Newton from the predicted xi, short cap
+    if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w, pr.at(t), kWarmCap);
+    // a sample that missed the cap restarts from its converged neighbours'
+    // xi (interpolated in t), then, failing that, from the plain cold start
+    const unsigned cm = __ballot_sync(kFull, ok && lane <= 16);
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const unsigned below = cm & lt_mask, above = cm & ~lt_mask & ~(1u << lane) & 0x1FFFFu;
+    const int lb = below ? 31 - __clz(below) : lane, la = above ? __ffs(above) - 1 : lane;
+    const float3 xb = shfl3(s.xi, lb), xa = shfl3(s.xi, la);
+    const float tb = __shfl_sync(kFull, t, lb), ta = __shfl_sync(kFull, t, la);
+    if (lane <= 16) {
+      if (ok) {
+        ++w.accepted;
+      } else {
+        float3 g0 = pr.at(t);
+        if (below && above) g0 = lerp3(xb, xa, (t - tb) / (ta - tb));
+        else if (below) g0 = make_float3(xb.x + (t - tb) * pr.k * pr.v.x, xb.y + (t - tb) * pr.k * pr.v.y,
+                                         xb.z + (t - tb) * pr.k * pr.v.z);
+        else if (above) g0 = make_float3(xa.x + (t - ta) * pr.k * pr.v.x, xa.y + (t - ta) * pr.k * pr.v.y,
+                                         xa.z + (t - ta) * pr.k * pr.v.z);
+        ok = (cm != 0u) && sample_along<N>(e, o, d, t, iso, s, w, g0, kWarmCap);
+        if (!ok) {
+          ++w.rejected;
+          ok = sample_along<N>(e, o, d, t, iso, s, w);
+        }
+      }
+    }
+  }
+  wu.cyc[1] += clock64() - c0;
   const unsigned okm = __ballot_sync(kFull, ok);
   const unsigned below = okm & ((1u << lane) - 1u);
   const int prev = below ? 31 - __clz(below) : lane;
@@ -482,7 +517,10 @@ __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, fl
   ls.xi = shfl3(s.xi, li);
   ls.g = shfl3(s.g, li);
   const float3 rxi = shfl3(s.xi, ri);
-  return refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, pr.on, rxi);
+  const long long c1 = clock64();
+  const bool found = refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, pr.on, rxi);
+  wu.cyc[2] += clock64() - c1;
+  return found;
 }
 
 // Slab test clipped to [tmin, tmax] (high_order.h:115-152).
@@ -866,7 +904,10 @@ __device__ void visit_warp(const Elem<N>& e, const float* __restrict__ fbox, int
     return;
   }
   int face = -1;
-  if (hit_hex_warp<N>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu, pr)) {
+  const long long c0 = clock64();
+  const bool fh = hit_hex_warp<N>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu, pr);
+  wu.cyc[3] += clock64() - c0;
+  if (fh) {
     if (th > 0.001f && th < best.t) {
       float3 x;
       float J[9];

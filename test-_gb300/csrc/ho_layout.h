@@ -47,6 +47,10 @@ enum StatSlot {
   ST_ACCEPT,
   ST_REJECT,
   ST_RESTART,
+  ST_CYC_TRAV,
+  ST_CYC_SCAN,
+  ST_CYC_REFINE,
+  ST_CYC_FACE,
   ST_COUNT
 };
 

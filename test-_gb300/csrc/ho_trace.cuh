@@ -145,8 +145,9 @@ static __device__ bool collect(const TraceParams& P, float3 o, float3 d, float t
 
 __device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool active) {
   // warp-aggregated counters
-  uint32_t v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled, w.nodes,
-                          w.accepted, w.rejected, w.restarts};
+  unsigned long long v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled,
+                                    w.nodes, w.accepted, w.rejected, w.restarts, w.cyc[0], w.cyc[1], w.cyc[2],
+                                    w.cyc[3]};
 #pragma unroll
   for (int s = 0; s < ST_COUNT; ++s) {
     unsigned long long x = v[s];
@@ -261,7 +262,10 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
       float bt[kCandK];
       int be[kCandK];
       bool overflow;
-      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu)) {
+      const long long c0 = clock64();
+      const bool walked = collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu);
+      wu.cyc[0] += clock64() - c0;
+      if (!walked) {
         if (lane == 0) atomicOr(&P.stats->status, kStatusStackOverflow);
         break;
       }
@@ -319,6 +323,7 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
     w.cand += wu.cand; w.geom += wu.geom; w.map += wu.map; w.field += wu.field; w.newton += wu.newton;
     w.face += wu.face; w.culled += wu.culled; w.nodes += wu.nodes; w.restarts += wu.restarts;
     w.accepted += wu.accepted; w.rejected += wu.rejected;
+    for (int k = 0; k < 4; ++k) w.cyc[k] = wu.cyc[k];
   }
   flush_work(P.stats, w, false);
 }

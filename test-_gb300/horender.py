@@ -58,7 +58,7 @@ class _Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("rays", "candidates", "geom_evals", "map_evals", "field_evals",
                                           "newton_iters", "face_iters", "faces_culled", "node_visits",
                                           "mlp_accepted", "mlp_rejected", "restarts")] + [
-        ("max_modes", C.c_int32), ("status", C.c_int32)]
+        ("max_modes", C.c_int32), ("status", C.c_int32), ("phase_cycles", C.c_uint64 * 4)]
 
 
 def _load():
@@ -322,7 +322,9 @@ class Context:
     def stats(self) -> dict:
         s = _Stats()
         self._ck(lib.ho_get_stats(self.h, C.byref(s)))
-        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+        d = {k: getattr(s, k) for k, _ in _Stats._fields_}
+        d["phase_cycles"] = dict(zip(("traversal", "iso_scan", "refine", "faces"), list(s.phase_cycles)))
+        return d
 
 
 def fp32_fma_peak_tflops(device: int = 0) -> float:

@@ -85,7 +85,15 @@ def test_train_save_load_and_learned_mode(ctx, tmp_path):
           "face", sp["face_iters"], "->", sl["face_iters"], "accepted", sl["mlp_accepted"], "rejected",
           sl["mlp_rejected"])
     assert same.mean() >= 0.995
-    m = same & (hp["kind"] > 0)
-    assert np.abs(hp["t"][m] - hl["t"][m]).max() < 2e-4
+    # equal error: face hits to the face Newton's tolerance; isosurface hits
+    # both meet the reference's stopping rule |u - iso| < 1e-5 (which bounds t
+    # only through du/dt, so t itself may differ more where u varies slowly)
+    face = same & (hp["kind"] == hr.HIT_FACE)
+    assert np.abs(hp["t"][face] - hl["t"][face]).max() < 2e-4
+    isoh = same & (hp["kind"] == hr.HIT_ISO)
+    iso_of = np.broadcast_to(np.array(isos, np.float32)[:, None, None], hp.shape)
+    for h in (hp, hl):
+        assert (np.abs(h["u"][isoh] - iso_of[isoh]) < 2e-5).mean() >= 0.99
+    assert np.abs(hp["t"][isoh] - hl["t"][isoh]).max() < 2e-3
     assert sl["newton_iters"] + sl["face_iters"] < 0.7 * (sp["newton_iters"] + sp["face_iters"])
     assert sl["mlp_accepted"] > 4 * sl["mlp_rejected"]
