@@ -48,12 +48,14 @@ __global__ void __launch_bounds__(32 * kSetupWarps) setup_kernel(const float* __
                                                                  BernMats bm, float* __restrict__ box,
                                                                  float* __restrict__ hull, float* __restrict__ fbox) {
   constexpr int S = N * N * N;
+  constexpr int RS = row_stride(N), BF = block_floats(N);
   __shared__ float sh[kSetupWarps][2 * S];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t e = static_cast<int64_t>(blockIdx.x) * kSetupWarps + wib;
   if (e >= n_elem) return;
+  const float* r = rec + e * record_floats(N);
   Elem<N> el;
-  el.c = rec + e * 4 * S;
+  el.c = CoefRef<false>{r};
   el.has_field = false;
   Work w;
   const bool tri = (flags[e] & 2u) != 0;
@@ -63,7 +65,7 @@ __global__ void __launch_bounds__(32 * kSetupWarps) setup_kernel(const float* __
     if (lane < 8) {
       const int i = lane & 1, j = (lane >> 1) & 1, k = lane >> 2;
       for (int c = 0; c < 3; ++c) {
-        const float v = el.c[c * S + (k * N + j) * N + i];
+        const float v = r[c * BF + (k * N + j) * RS + i];
         lo[c] = v;
         hi[c] = v;
       }
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(32 * kSetupWarps) setup_kernel(const float* __
   float* t1 = sh[wib] + S;
   float elo[3], ehi[3], flo[6][3], fhi[6][3];
   for (int c = 0; c < 3; ++c) {
-    const float* src = el.c + c * S;
+    const float* src = r + c * BF;
     // faces: slices at the fixed axis' vertex mode, then 2-D transform
     for (int f = 0; f < 6; ++f) {
       int fixed, ua, va;
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(32 * kSetupWarps) setup_kernel(const float* __
             idx[fixed] = m;
             idx[ua] = iu;
             idx[va] = iv;
-            const float cv = src[(idx[2] * N + idx[1]) * N + idx[0]];
+            const float cv = src[(idx[2] * N + idx[1]) * RS + idx[0]];
             acc = fmaf(cv, bm.face[iu * kMaxModes + bu] * bm.face[iv * kMaxModes + bv], acc);
           }
         mn = fminf(mn, acc);
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(32 * kSetupWarps) setup_kernel(const float* __
     for (int q = lane; q < S; q += 32) {
       const int b = q % N, j = (q / N) % N, k = q / (N * N);
       float acc = 0.f;
-      for (int i = 0; i < N; ++i) acc = fmaf(src[(k * N + j) * N + i], bm.cube[i * kMaxModes + b], acc);
+      for (int i = 0; i < N; ++i) acc = fmaf(src[(k * N + j) * RS + i], bm.cube[i * kMaxModes + b], acc);
       t0[q] = acc;
     }
     __syncwarp();

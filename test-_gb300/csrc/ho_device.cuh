@@ -116,10 +116,44 @@ struct Basis {
   float ar[N], dr[N], as[N], ds[N], at[N], dt[N];
 };
 
+// Where an element record lives: global memory (read-only path) or a warp's
+// shared-memory staging slot. Offsets are in floats.
+template <bool SM>
+struct CoefRef;
+template <>
+struct CoefRef<false> {
+  const float* __restrict__ p;
+  __device__ __forceinline__ float4 ld4(int off) const { return __ldg(reinterpret_cast<const float4*>(p + off)); }
+  __device__ __forceinline__ CoefRef at(int off) const { return CoefRef{p + off}; }
+};
+template <>
+struct CoefRef<true> {
+  uint32_t a;  // shared-space byte address
+  __device__ __forceinline__ float4 ld4(int off) const {
+    float4 v;
+    asm("ld.shared.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a + 4u * off));
+    return v;
+  }
+  __device__ __forceinline__ CoefRef at(int off) const { return CoefRef{a + 4u * static_cast<uint32_t>(off)}; }
+};
+
+// One coefficient row (N values) into registers, RS/4 vector loads.
+template <int N, bool SM>
+__device__ __forceinline__ void load_row(const CoefRef<SM>& c, int off, float (&r)[row_stride(N)]) {
+#pragma unroll
+  for (int q = 0; q < row_stride(N) / 4; ++q) {
+    const float4 v = c.ld4(off + 4 * q);
+    r[4 * q] = v.x;
+    r[4 * q + 1] = v.y;
+    r[4 * q + 2] = v.z;
+    r[4 * q + 3] = v.w;
+  }
+}
+
 // value and the three reference-space partials: out = {v, dv/dr, dv/ds, dv/dt}
-template <int N>
-__device__ __noinline__ void contract_vd(const float* __restrict__ c, const Basis<N>* __restrict__ B,
-                                         float* __restrict__ out) {
+template <int N, bool SM>
+__device__ __noinline__ void contract_vd(CoefRef<SM> c, const Basis<N>* __restrict__ B, float* __restrict__ out) {
+  constexpr int RS = row_stride(N);
   float ar[N], dr[N], as[N], ds[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
@@ -132,17 +166,16 @@ __device__ __noinline__ void contract_vd(const float* __restrict__ c, const Basi
 #pragma unroll 1
   for (int k = 0; k < N; ++k) {
     const float tk = B->at[k], dtk = B->dt[k];
-    const float* ck = c + k * N * N;
     float q0 = 0.f, q1 = 0.f, q2 = 0.f;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const float* row = ck + j * N;
+      float row[RS];
+      load_row<N, SM>(c, (k * N + j) * RS, row);
       float s0 = 0.f, s1 = 0.f;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        const float cv = __ldg(row + i);
-        s0 = fmaf(cv, ar[i], s0);
-        s1 = fmaf(cv, dr[i], s1);
+        s0 = fmaf(row[i], ar[i], s0);
+        s1 = fmaf(row[i], dr[i], s1);
       }
       q0 = fmaf(s0, as[j], q0);
       q1 = fmaf(s1, as[j], q1);
@@ -160,8 +193,9 @@ __device__ __noinline__ void contract_vd(const float* __restrict__ c, const Basi
 }
 
 // value only
-template <int N>
-__device__ __noinline__ float contract_v(const float* __restrict__ c, const Basis<N>* __restrict__ B) {
+template <int N, bool SM>
+__device__ __noinline__ float contract_v(CoefRef<SM> c, const Basis<N>* __restrict__ B) {
+  constexpr int RS = row_stride(N);
   float ar[N], as[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) {
@@ -172,14 +206,14 @@ __device__ __noinline__ float contract_v(const float* __restrict__ c, const Basi
 #pragma unroll 1
   for (int k = 0; k < N; ++k) {
     const float tk = B->at[k];
-    const float* ck = c + k * N * N;
     float q0 = 0.f;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const float* row = ck + j * N;
+      float row[RS];
+      load_row<N, SM>(c, (k * N + j) * RS, row);
       float s0 = 0.f;
 #pragma unroll
-      for (int i = 0; i < N; ++i) s0 = fmaf(__ldg(row + i), ar[i], s0);
+      for (int i = 0; i < N; ++i) s0 = fmaf(row[i], ar[i], s0);
       q0 = fmaf(s0, as[j], q0);
     }
     v = fmaf(q0, tk, v);
@@ -187,31 +221,30 @@ __device__ __noinline__ float contract_v(const float* __restrict__ c, const Basi
   return v;
 }
 
-// Element record: x, y, z geometry blocks then the field block, N^3 floats each.
-template <int N>
+// Element record (record_floats(N) floats): x, y, z geometry blocks then the
+// field block, in global memory (SM = false) or a shared-memory slot.
+template <int N, bool SM = false>
 struct Elem {
-  const float* __restrict__ c;  // 4*N^3 floats
+  CoefRef<SM> c;
   bool has_field;
-  __device__ __forceinline__ const float* gx() const { return c; }
-  __device__ __forceinline__ const float* fld() const { return c + 3 * N * N * N; }
+  __device__ __forceinline__ CoefRef<SM> fld() const { return c.at(3 * block_floats(N)); }
 };
 
 // x(xi) and J (row-major J[row=x,y,z][col=r,s,t]).
-template <int N>
-__device__ __noinline__ void geom_eval_raw(const float* __restrict__ c, float3 xi, float* __restrict__ xJ) {
+template <int N, bool SM>
+__device__ __noinline__ void geom_eval_raw(CoefRef<SM> c, float3 xi, float* __restrict__ xJ) {
   Basis<N> B;
   basis_val_der<N>(xi.x, B.ar, B.dr);
   basis_val_der<N>(xi.y, B.as, B.ds);
   basis_val_der<N>(xi.z, B.at, B.dt);
-  constexpr int S = N * N * N;
 #pragma unroll 1
-  for (int comp = 0; comp < 3; ++comp) contract_vd<N>(c + comp * S, &B, xJ + 4 * comp);
+  for (int comp = 0; comp < 3; ++comp) contract_vd<N, SM>(c.at(comp * block_floats(N)), &B, xJ + 4 * comp);
 }
 
-template <int N>
-__device__ __forceinline__ void geom_eval(const Elem<N>& e, float3 xi, float3& x, float (&J)[9], Work& w) {
+template <int N, bool SM>
+__device__ __forceinline__ void geom_eval(const Elem<N, SM>& e, float3 xi, float3& x, float (&J)[9], Work& w) {
   float r[12];
-  geom_eval_raw<N>(e.c, xi, r);
+  geom_eval_raw<N, SM>(e.c, xi, r);
   x = make_float3(r[0], r[4], r[8]);
   J[0] = r[1]; J[1] = r[2]; J[2] = r[3];
   J[3] = r[5]; J[4] = r[6]; J[5] = r[7];
@@ -219,56 +252,55 @@ __device__ __forceinline__ void geom_eval(const Elem<N>& e, float3 xi, float3& x
   ++w.geom;
 }
 
-template <int N>
-__device__ __noinline__ float3 geom_map_raw(const float* __restrict__ c, float3 xi) {
+template <int N, bool SM>
+__device__ __noinline__ float3 geom_map_raw(CoefRef<SM> c, float3 xi) {
   Basis<N> B;
   basis_val<N>(xi.x, B.ar);
   basis_val<N>(xi.y, B.as);
   basis_val<N>(xi.z, B.at);
-  constexpr int S = N * N * N;
-  const float x = contract_v<N>(c, &B);
-  const float y = contract_v<N>(c + S, &B);
-  const float z = contract_v<N>(c + 2 * S, &B);
+  const float x = contract_v<N, SM>(c, &B);
+  const float y = contract_v<N, SM>(c.at(block_floats(N)), &B);
+  const float z = contract_v<N, SM>(c.at(2 * block_floats(N)), &B);
   return make_float3(x, y, z);
 }
 
-template <int N>
-__device__ __forceinline__ float3 geom_map(const Elem<N>& e, float3 xi, Work& w) {
+template <int N, bool SM>
+__device__ __forceinline__ float3 geom_map(const Elem<N, SM>& e, float3 xi, Work& w) {
   ++w.map;
-  return geom_map_raw<N>(e.c, xi);
+  return geom_map_raw<N, SM>(e.c, xi);
 }
 
 // u(xi) and grad_xi u
-template <int N>
-__device__ __noinline__ void field_eval_raw(const float* __restrict__ c, float3 xi, float* __restrict__ ug) {
+template <int N, bool SM>
+__device__ __noinline__ void field_eval_raw(CoefRef<SM> c, float3 xi, float* __restrict__ ug) {
   Basis<N> B;
   basis_val_der<N>(xi.x, B.ar, B.dr);
   basis_val_der<N>(xi.y, B.as, B.ds);
   basis_val_der<N>(xi.z, B.at, B.dt);
-  contract_vd<N>(c, &B, ug);
+  contract_vd<N, SM>(c, &B, ug);
 }
 
-template <int N>
-__device__ __forceinline__ void field_eval(const Elem<N>& e, float3 xi, float& u, float3& g, Work& w) {
+template <int N, bool SM>
+__device__ __forceinline__ void field_eval(const Elem<N, SM>& e, float3 xi, float& u, float3& g, Work& w) {
   float r[4];
-  field_eval_raw<N>(e.fld(), xi, r);
+  field_eval_raw<N, SM>(e.fld(), xi, r);
   u = r[0];
   g = make_float3(r[1], r[2], r[3]);
   ++w.field;
 }
 
-template <int N>
-__device__ __noinline__ float field_value_raw(const float* __restrict__ c, float3 xi) {
+template <int N, bool SM>
+__device__ __noinline__ float field_value_raw(CoefRef<SM> c, float3 xi) {
   Basis<N> B;
   basis_val<N>(xi.x, B.ar);
   basis_val<N>(xi.y, B.as);
   basis_val<N>(xi.z, B.at);
-  return contract_v<N>(c, &B);
+  return contract_v<N, SM>(c, &B);
 }
 
-template <int N>
-__device__ __forceinline__ float field_value(const Elem<N>& e, float3 xi) {
-  return field_value_raw<N>(e.fld(), xi);
+template <int N, bool SM>
+__device__ __forceinline__ float field_value(const Elem<N, SM>& e, float3 xi) {
+  return field_value_raw<N, SM>(e.fld(), xi);
 }
 
 // Adjugate / determinant inverse, no singular guard (HexElement.cu:208-225).
@@ -292,8 +324,8 @@ __device__ __forceinline__ void invert3(const float (&J)[9], float (&K)[9]) {
 // Inverse map x(xi) = p by Newton from xi0 (the reference always starts at
 // 0), at most 50 iterations, converged when every |delta| < 1e-5.
 // A NaN iterate can never converge, so it stops early with the same answer.
-template <int N>
-__device__ __forceinline__ bool inverse_map(const Elem<N>& e, float3 p, float3& xi, Work& w,
+template <int N, bool SM>
+__device__ __forceinline__ bool inverse_map(const Elem<N, SM>& e, float3 p, float3& xi, Work& w,
                                             float3 xi0 = make_float3(0.f, 0.f, 0.f), int max_it = 50) {
   xi = xi0;
   for (int it = 0; it < max_it; ++it) {
@@ -323,8 +355,8 @@ struct Sample {
   float3 g;
 };
 
-template <int N>
-__device__ __forceinline__ bool sample_along(const Elem<N>& e, float3 o, float3 d, float t, float iso, Sample& s,
+template <int N, bool SM>
+__device__ __forceinline__ bool sample_along(const Elem<N, SM>& e, float3 o, float3 d, float t, float iso, Sample& s,
                                              Work& w, float3 xi0 = make_float3(0.f, 0.f, 0.f), int max_it = 50) {
   const float3 p = make_float3(o.x + t * d.x, o.y + t * d.y, o.z + t * d.z);
   if (!inverse_map<N>(e, p, s.xi, w, xi0, max_it)) return false;
@@ -346,8 +378,8 @@ __device__ __forceinline__ bool sample_along(const Elem<N>& e, float3 o, float3 
 // if that does not converge the plain cold-start solve answers (the fallback
 // the learned guess never replaces).
 constexpr int kWarmCap = 4;
-template <int N>
-__device__ __forceinline__ bool sample_warm(const Elem<N>& e, float3 o, float3 d, float t, float iso, Sample& s,
+template <int N, bool SM>
+__device__ __forceinline__ bool sample_warm(const Elem<N, SM>& e, float3 o, float3 d, float t, float iso, Sample& s,
                                             Work& w, bool warm, float3 xi0) {
   if (warm) {
     if (sample_along<N>(e, o, d, t, iso, s, w, xi0, kWarmCap)) {
@@ -366,8 +398,8 @@ __device__ __forceinline__ float3 lerp3(float3 a, float3 b, float u) {
 // At most 20 safeguarded Newton/bisection steps on a bracket [lt, rt] whose
 // left sample is ls; done when |f| < 1e-5, else the midpoint with the left
 // sample's xi and gradient (RayIsosurface.cu:121-177).
-template <int N>
-__device__ __forceinline__ bool refine_bracket(const Elem<N>& e, float3 o, float3 d, float iso, float lt, float rt,
+template <int N, bool SM>
+__device__ __forceinline__ bool refine_bracket(const Elem<N, SM>& e, float3 o, float3 d, float iso, float lt, float rt,
                                                Sample ls, float& th, float3& xh, float3& gh, Work& w,
                                                bool warm = false, float3 rxi = make_float3(0.f, 0.f, 0.f)) {
   for (int it = 0; it < 20; ++it) {
@@ -407,8 +439,8 @@ __device__ __forceinline__ bool refine_bracket(const Elem<N>& e, float3 o, float
 
 // First sign change over 17 uniform samples of [t0,t1], then the bracket
 // refinement (RayIsosurface.cu:67-188). One thread.
-template <int N>
-__device__ bool find_iso(const Elem<N>& e, float3 o, float3 d, float t0, float t1, float iso, float& th, float3& xh,
+template <int N, bool SM>
+__device__ bool find_iso(const Elem<N, SM>& e, float3 o, float3 d, float t0, float t1, float iso, float& th, float3& xh,
                          float3& gh, Work& w) {
   bool have = false;
   float tp = t0;
@@ -457,8 +489,8 @@ struct Pred {
   }
 };
 
-template <int N>
-__device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, float t1, float iso, float& th,
+template <int N, bool L, bool SM>
+__device__ bool find_iso_warp(const Elem<N, SM>& e, float3 o, float3 d, float t0, float t1, float iso, float& th,
                               float3& xh, float3& gh, Work& w, Work& wu, const Pred& pr) {
   const int lane = threadIdx.x & 31;
   Sample s;
@@ -469,7 +501,7 @@ __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, fl
   const long long c0 = clock64();
   const float t = t0 + (t1 - t0) * (float(lane) / 16.0f);
   bool ok = false;
-  if (!pr.on) {
+  if (!L || !pr.on) {
     if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w);
   } else {
     // learned: Newton from the predicted xi, short cap
@@ -518,7 +550,7 @@ __device__ bool find_iso_warp(const Elem<N>& e, float3 o, float3 d, float t0, fl
   ls.g = shfl3(s.g, li);
   const float3 rxi = shfl3(s.xi, ri);
   const long long c1 = clock64();
-  const bool found = refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, pr.on, rxi);
+  const bool found = refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, L && pr.on, rxi);
   wu.cyc[2] += clock64() - c1;
   return found;
 }
@@ -571,12 +603,12 @@ __device__ __forceinline__ void setc(float3& v, int a, float s) {
 // iterations, accept when max|X-Y| < 1e-4 with u,v in [-1.001,1.001] and tau
 // in [tmin,tmax]; step clamp 0.25, divergence break after 5 iterations
 // (high_order.h:213-300).
-template <int N>
-__device__ bool face_newton(const Elem<N>& e, float3 o, float3 d, int f, float3 p, float tau, float tmin, float tmax,
+template <int N, bool SM>
+__device__ bool face_newton(const Elem<N, SM>& e, float3 o, float3 d, int f, float3 p, float tau, float tmin, float tmax,
                             float& th, float3& xh, Work& w, int max_it);
 
-template <int N>
-__device__ bool face_seed(const Elem<N>& e, float3 o, float3 d, int f, int si, int sj, float tmin, float tmax,
+template <int N, bool SM>
+__device__ bool face_seed(const Elem<N, SM>& e, float3 o, float3 d, int f, int si, int sj, float tmin, float tmax,
                           float& th, float3& xh, Work& w) {
   int fixed, ua, va;
   float val;
@@ -594,8 +626,8 @@ __device__ bool face_seed(const Elem<N>& e, float3 o, float3 d, int f, int si, i
 }
 
 // The (u,v,tau) Newton of one seed from a given start point.
-template <int N>
-__device__ bool face_newton(const Elem<N>& e, float3 o, float3 d, int f, float3 p, float tau, float tmin, float tmax,
+template <int N, bool SM>
+__device__ bool face_newton(const Elem<N, SM>& e, float3 o, float3 d, int f, float3 p, float tau, float tmin, float tmax,
                             float& th, float3& xh, Work& w, int max_it) {
   int fixed, ua, va;
   float val;
@@ -640,8 +672,8 @@ __device__ bool face_newton(const Elem<N>& e, float3 o, float3 d, int f, float3 
 
 // Ray against one curved face: the 9 seeds {-0.8,0,0.8}^2 in order (v outer,
 // u inner); the first seed accepted answers (high_order.h:189-304).
-template <int N>
-__device__ bool hit_face(const Elem<N>& e, float3 o, float3 d, int f, float tmin, float tmax, float& th, float3& xh,
+template <int N, bool SM>
+__device__ bool hit_face(const Elem<N, SM>& e, float3 o, float3 d, int f, float tmin, float tmax, float& th, float3& xh,
                          Work& w) {
   for (int sj = 0; sj < 3; ++sj)
     for (int si = 0; si < 3; ++si)
@@ -656,8 +688,8 @@ __device__ bool hit_face(const Elem<N>& e, float3 o, float3 d, int f, float tmin
 // reference's answer for the face is "no hit" (exact culling).
 // The reference's padded-box pre-test (high_order.h:420-431) is the same box
 // the candidate was admitted with, so it always passes here.
-template <int N>
-__device__ bool hit_hex(const Elem<N>& e, const float* __restrict__ fbox, float3 o, float3 d, float tmin, float tmax,
+template <int N, bool SM>
+__device__ bool hit_hex(const Elem<N, SM>& e, const float* __restrict__ fbox, float3 o, float3 d, float tmin, float tmax,
                         float& th, float3& xh, int& face, Work& w) {
   bool any = false;
   float best = tmax;
@@ -704,8 +736,8 @@ struct HitState {
 
 // Per-candidate policy of the reference's hex branch: iso search on the
 // padded-box segment when enabled; if it finds nothing, nearest curved face.
-template <int N>
-__device__ void visit_candidate(const Elem<N>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d,
+template <int N, bool SM>
+__device__ void visit_candidate(const Elem<N, SM>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d,
                                 float te, float tx, float iso, bool iso_on, HitState& best, Work& w) {
   ++w.cand;
   float th;
@@ -796,8 +828,8 @@ __device__ __forceinline__ bool predicted_entry(const Pred& pr, float tmin, floa
   return true;
 }
 
-template <int N>
-__device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, float3 o, float3 d, float tmin,
+template <int N, bool L, bool SM>
+__device__ bool hit_hex_warp(const Elem<N, SM>& e, const float* __restrict__ fbox, float3 o, float3 d, float tmin,
                              float tmax, float& th, float3& xh, int& face, Work& w, Work& wu, const Pred& pr) {
   const int lane = threadIdx.x & 31;
   unsigned packed = 0;
@@ -807,7 +839,7 @@ __device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, f
   int lf = -1;
   float lt = 0.f;
   float3 lx = make_float3(0.f, 0.f, 0.f);
-  if (pr.on) {
+  if (L && pr.on) {
     float3 p0;
     float tau0;
     int f0;
@@ -883,13 +915,13 @@ __device__ bool hit_hex_warp(const Elem<N>& e, const float* __restrict__ fbox, f
 }
 
 // Warp version of visit_candidate: every lane holds the same `best`.
-template <int N>
-__device__ void visit_warp(const Elem<N>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d, float te,
+template <int N, bool L, bool SM>
+__device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d, float te,
                            float tx, float iso, bool iso_on, HitState& best, Work& w, Work& wu, const Pred& pr) {
   ++wu.cand;
   float th;
   float3 xi, g;
-  if (iso_on && e.has_field && find_iso_warp<N>(e, o, d, te, tx, iso, th, xi, g, w, wu, pr)) {
+  if (iso_on && e.has_field && find_iso_warp<N, L>(e, o, d, te, tx, iso, th, xi, g, w, wu, pr)) {
     if (th > 0.001f && th < best.t) {
       float3 n = normalize3(g);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
@@ -905,7 +937,7 @@ __device__ void visit_warp(const Elem<N>& e, const float* __restrict__ fbox, int
   }
   int face = -1;
   const long long c0 = clock64();
-  const bool fh = hit_hex_warp<N>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu, pr);
+  const bool fh = hit_hex_warp<N, L>(e, fbox, o, d, 0.001f, best.t, th, xi, face, w, wu, pr);
   wu.cyc[3] += clock64() - c0;
   if (fh) {
     if (th > 0.001f && th < best.t) {

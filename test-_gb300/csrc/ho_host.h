@@ -43,8 +43,9 @@ int generate_synthetic(const ho_synth_params& p, HostScene& hs, std::string& err
 
 // Largest modes count over geometry and field (trilinear counts as 2).
 int scene_max_modes(const HostScene& hs);
-// Pack the scene into per-element records of 4*N^3 floats (x, y, z geometry
-// blocks then the field block), zero-padded to N modes per direction.
+// Pack the scene into per-element records of record_floats(N) floats (x, y,
+// z geometry blocks then the field block, rows padded to row_stride(N)),
+// zero-padded to N modes per direction.
 // Trilinear elements become their exact N = 2 modal form. flags[e] bit 0:
 // has field; bit 1: trilinear (box rule of FEM-AABB/high_order.h:59-76);
 // own[e]: the element's own geometry modes (box sample count).
@@ -78,7 +79,7 @@ struct ho_context {
   // device scene
   int N = 0;
   int64_t n_elem = 0;
-  float* d_rec = nullptr;         // n_elem * 4 * N^3
+  float* d_rec = nullptr;         // n_elem * record_floats(N)
   float* d_box = nullptr;         // n_elem * 6 padded sampled boxes
   float* d_hull = nullptr;        // n_elem * 6 Bernstein hull boxes
   float* d_fbox = nullptr;        // n_elem * 36 face hull boxes

@@ -70,4 +70,12 @@ constexpr int kFaceBoxFloats = 36;
 constexpr int kMaxModes = 9;
 constexpr int kMinModes = 2;
 
+// Element record layout: x, y, z geometry blocks then the field block; in a
+// block, coefficient (i,j,k) sits at (k*N + j)*RS + i with the row stride RS
+// = N rounded up to a multiple of 4 (rows start on 16-byte boundaries, so a
+// row is fetched with float4 loads; the padding is zero).
+__host__ __device__ constexpr int row_stride(int n) { return (n + 3) & ~3; }
+__host__ __device__ constexpr int block_floats(int n) { return n * n * row_stride(n); }
+__host__ __device__ constexpr int record_floats(int n) { return 4 * block_floats(n); }
+
 }  // namespace ho

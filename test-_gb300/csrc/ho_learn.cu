@@ -24,15 +24,15 @@ template <int N>
 __global__ void desc_kernel(const float* __restrict__ rec, int64_t n, float* __restrict__ desc) {
   const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  constexpr int S = N * N * N;
+  const float* r = rec + e * record_floats(N);
   Elem<N> el;
-  el.c = rec + e * 4 * S;
+  el.c = CoefRef<false>{r};
   el.has_field = false;
   Work w;
   float cx[8][3];
   for (int v = 0; v < 8; ++v) {  // Z-order corner (i,j,k): vertex-mode coefficient
     const int i = v & 1, j = (v >> 1) & 1, k = v >> 2;
-    for (int c = 0; c < 3; ++c) cx[v][c] = el.c[c * S + (k * N + j) * N + i];
+    for (int c = 0; c < 3; ++c) cx[v][c] = r[c * block_floats(N) + (k * N + j) * row_stride(N) + i];
   }
   float cen[3] = {0.f, 0.f, 0.f}, lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
   for (int v = 0; v < 8; ++v)
@@ -90,7 +90,6 @@ __global__ void datagen_kernel(const float* __restrict__ rec, const float* __res
                                __nv_bfloat16* __restrict__ X, float* __restrict__ T, uint8_t* __restrict__ V) {
   const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  constexpr int S = N * N * N;
   const int64_t e = static_cast<int64_t>(unit_rand(seed, q, 0) * n_elem) % n_elem;
   const float* b = box + 6 * e;
   const float3 p = make_float3(b[0] + unit_rand(seed, q, 1) * (b[3] - b[0]), b[1] + unit_rand(seed, q, 2) * (b[4] - b[1]),
@@ -110,7 +109,7 @@ __global__ void datagen_kernel(const float* __restrict__ rec, const float* __res
   for (int j = 0; j < kMlpOut; ++j) t[j] = 0.f;
   if (ok) {
     Elem<N> el;
-    el.c = rec + e * 4 * S;
+    el.c = CoefRef<false>{rec + e * record_floats(N)};
     el.has_field = false;
     Work w;
     float3 xi;

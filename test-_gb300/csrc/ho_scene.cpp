@@ -360,13 +360,13 @@ static const int kXml2Z[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vector<uint32_t>& flags,
                   std::vector<int32_t>& own) {
   const int64_t ne = hs.size();
-  const int64_t S = static_cast<int64_t>(N) * N * N;
-  rec.assign(static_cast<size_t>(ne) * 4 * S, 0.0f);
+  const int64_t S = block_floats(N), RS = row_stride(N);
+  rec.assign(static_cast<size_t>(ne) * record_floats(N), 0.0f);
   flags.assign(ne, 0);
   own.assign(ne, 0);
   parallel_chunks(ne, [&](int64_t b, int64_t e_end) {
     for (int64_t e = b; e < e_end; ++e) {
-      float* r = rec.data() + e * 4 * S;
+      float* r = rec.data() + e * record_floats(N);
       uint32_t fl = 0;
       if (hs.goff[e] >= 0) {
         const uint32_t mx = hs.gmodes[3 * e], my = hs.gmodes[3 * e + 1], mz = hs.gmodes[3 * e + 2];
@@ -376,7 +376,7 @@ void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vect
           for (uint32_t k = 0; k < mz; ++k)
             for (uint32_t j = 0; j < my; ++j)
               for (uint32_t i = 0; i < mx; ++i)
-                r[c * S + (k * N + j) * N + i] = src[(k * my + j) * mx + i];
+                r[c * S + (k * N + j) * RS + i] = src[(k * my + j) * mx + i];
         }
         own[e] = static_cast<int32_t>(std::max(mx, std::max(my, mz)));
       } else {
@@ -385,7 +385,7 @@ void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vect
         for (int v = 0; v < 8; ++v) {
           const int z = kXml2Z[v];
           const int i = z & 1, j = (z >> 1) & 1, k = (z >> 2) & 1;
-          for (int c = 0; c < 3; ++c) r[c * S + (k * N + j) * N + i] = cv[3 * v + c];
+          for (int c = 0; c < 3; ++c) r[c * S + (k * N + j) * RS + i] = cv[3 * v + c];
         }
         fl |= 2u;
         own[e] = 0;
@@ -396,7 +396,7 @@ void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vect
           const float* src = hs.field.data() + hs.foff[e];
           for (uint32_t k = 0; k < mz; ++k)
             for (uint32_t j = 0; j < my; ++j)
-              for (uint32_t i = 0; i < mx; ++i) r[3 * S + (k * N + j) * N + i] = src[(k * my + j) * mx + i];
+              for (uint32_t i = 0; i < mx; ++i) r[3 * S + (k * N + j) * RS + i] = src[(k * my + j) * mx + i];
           fl |= 1u;
         }
       }

@@ -239,7 +239,10 @@ __device__ __forceinline__ HitState miss_state() {
 template <int N, bool LEARNED>
 __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
   const int lane = threadIdx.x & 31;
-  constexpr int64_t S = static_cast<int64_t>(N) * N * N;
+  // one staging slot per warp for the element record being visited
+  extern __shared__ __align__(16) float stage[];
+  float4* slot4 = reinterpret_cast<float4*>(stage + (threadIdx.x >> 5) * record_floats(N));
+  const uint32_t slot_addr = static_cast<uint32_t>(__cvta_generic_to_shared(slot4));
   Work w, wu;
   const unsigned n_work = *P.qcount;
   for (;;) {
@@ -289,8 +292,13 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
         const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
         float te, tx;
         if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
-          Elem<N> el;
-          el.c = P.rec + static_cast<int64_t>(ce) * 4 * S;
+          // stage the candidate's record in this warp's shared-memory slot
+          const float4* src = reinterpret_cast<const float4*>(P.rec + static_cast<int64_t>(ce) * record_floats(N));
+          __syncwarp();
+          for (int q4 = lane; q4 < record_floats(N) / 4; q4 += 32) slot4[q4] = __ldg(src + q4);
+          __syncwarp();
+          Elem<N, true> el;
+          el.c = CoefRef<true>{slot_addr};
           el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
           Pred pr;
           pr.on = false;
@@ -302,8 +310,8 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
             pr.k = __ldg(P.desc + static_cast<int64_t>(ce) * kDescFloats + 45);
             pr.te = te;
           }
-          visit_warp<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on, best,
-                        w, wu, pr);
+          visit_warp<N, LEARNED>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso,
+                                 iso_on, best, w, wu, pr);
         }
         kt = ct;
         ke = ce;
@@ -359,7 +367,6 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
   if (active) {
     const float iso = P.iso[iso_idx];
     const bool iso_on = (P.iso_on_mask >> iso_idx) & 1u;
-    constexpr int64_t S = static_cast<int64_t>(N) * N * N;
     float kt = -FLT_MAX;
     int ke = -1;
     for (;;) {
@@ -391,7 +398,7 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
         float te, tx;
         if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
           Elem<N> el;
-          el.c = P.rec + static_cast<int64_t>(ce) * 4 * S;
+          el.c = CoefRef<false>{P.rec + static_cast<int64_t>(ce) * record_floats(N)};
           el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
           visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
                              best, w);
@@ -419,15 +426,22 @@ cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads,
   static int grid[2] = {0, 0};  // persistent grid: resident blocks per SM x SMs
   int& g = grid[learned ? 1 : 0];
   if (g == 0) {
+    const int smem_i = static_cast<int>((kTraceBlock / 32) * record_floats(N) * sizeof(float));
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (learned) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, true>, kTraceBlock, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, false>, kTraceBlock, 0);
+    if (learned) {
+      cudaFuncSetAttribute(isect_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_i);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, true>, kTraceBlock, smem_i);
+    } else {
+      cudaFuncSetAttribute(isect_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_i);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, false>, kTraceBlock, smem_i);
+    }
     g = sms * (per > 0 ? per : 1);
   }
-  if (learned) isect_kernel<N, true><<<g, kTraceBlock, 0, s>>>(P);
-  else isect_kernel<N, false><<<g, kTraceBlock, 0, s>>>(P);
+  const size_t smem = static_cast<size_t>(kTraceBlock / 32) * record_floats(N) * sizeof(float);
+  if (learned) isect_kernel<N, true><<<g, kTraceBlock, smem, s>>>(P);
+  else isect_kernel<N, false><<<g, kTraceBlock, smem, s>>>(P);
   return cudaGetLastError();
 }
 
