@@ -163,6 +163,8 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_rgb);
     cudaFree(c->d_rays);
     cudaFree(c->d_work);
+    cudaFree(c->d_kbuf);
+    cudaFree(c->d_kovf);
     cudaFree(c->d_qctr);
     cudaFree(c->d_feat);
     cudaFree(c->d_pred);

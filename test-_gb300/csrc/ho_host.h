@@ -109,6 +109,8 @@ struct ho_context {
   int32_t* d_cand = nullptr;      // elements the predictions belong to
   size_t pred_cap = 0;
   int32_t* d_work = nullptr;      // query queue of the intersect pass
+  float2* d_kbuf = nullptr;       // first ordered candidates per queued query
+  uint8_t* d_kovf = nullptr;
   size_t work_cap = 0;
   unsigned* d_qctr = nullptr;     // [0] queue length, [1] next item
   void* h_pinned = nullptr;

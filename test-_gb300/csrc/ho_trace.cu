@@ -5,43 +5,27 @@
 
 namespace ho {
 
-// Does the ray meet any padded element box in [0.001, inf)? (early exit)
-static __device__ bool any_candidate(const BNode* __restrict__ nodes, float3 o, float3 d, Work& w) {
-  int stack[kStack];
-  int sp = 0;
-  stack[sp++] = 0;
-  while (sp > 0) {
-    const int node = stack[--sp];
-    ++w.nodes;
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      float lo[3], hi[3];
-      int id;
-      uint32_t aux;
-      load_child(nodes, node, c, lo, hi, id, aux);
-      if (id == kEmptyChild) continue;
-      float a0, a1;
-      if (!ray_box(o, d, lo, hi, 0.001f, FLT_MAX, a0, a1)) continue;
-      if (id < 0) return true;
-      if (sp >= kStack) return true;  // let the intersect kernel see (and report) it
-      stack[sp++] = id;
-    }
-  }
-  return false;
-}
-
 // Pass 1, one thread per query: rays that meet no padded box are finished
-// here (miss); the rest are appended to the work queue.
+// here (miss); the rest are appended to the work queue together with their
+// first kCandK ordered candidates.
 __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_queries) {
   const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   Work w;
-  bool need = false;
+  bool need = false, overflow = false;
+  float bt[kCandK];
+  int be[kCandK];
   float3 o = make_float3(0.f, 0.f, 0.f), d = make_float3(0.f, 0.f, 1.f);
   if (q < n_queries) {
     int iso_idx;
     query_ray(P, q, o, d, iso_idx);
-    need = any_candidate(P.nodes, o, d, w);
+    // the ray's first kCandK ordered candidates (nothing is hit yet, so the
+    // bound is infinite): the intersect pass starts from this list
+    if (!collect(P, o, d, FLT_MAX, -FLT_MAX, -1, bt, be, overflow, w)) {
+      atomicOr(&P.stats->status, kStatusStackOverflow);
+      be[0] = INT_MAX;
+    }
+    need = be[0] != INT_MAX;
     if (!need) write_result(P, q, d, miss_state(), 0);
   }
   const unsigned m = __ballot_sync(kFull, need);
@@ -50,7 +34,14 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
     unsigned base = 0;
     if (lane == leader) base = atomicAdd(P.qcount, static_cast<unsigned>(__popc(m)));
     base = __shfl_sync(kFull, base, leader);
-    if (need) P.work[base + __popc(m & ((1u << lane) - 1u))] = static_cast<int32_t>(q);
+    if (need) {
+      const unsigned slot = base + __popc(m & ((1u << lane) - 1u));
+      P.work[slot] = static_cast<int32_t>(q);
+      float2* kb = P.kbuf + static_cast<int64_t>(slot) * kCandK;
+#pragma unroll
+      for (int j = 0; j < kCandK; ++j) kb[j] = make_float2(bt[j], __int_as_float(be[j]));
+      P.kovf[slot] = overflow ? 1 : 0;
+    }
   }
   flush_work(P.stats, w, q < n_queries);
 }
@@ -68,17 +59,16 @@ __global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16*
     float3 o, d;
     int iso_idx;
     query_ray(P, q, o, d, iso_idx);
-    float bt[kCandK];
-    int be[kCandK];
-    bool overflow;
-    const bool ok = collect(P, o, d, FLT_MAX, -FLT_MAX, -1, bt, be, overflow, w);
+    const float2* kb = P.kbuf + item * kCandK;
 #pragma unroll
     for (int j = 0; j < kPredK; ++j) {
-      const int e = (ok && be[j] != INT_MAX) ? be[j] : -1;
+      const float2 c = kb[j];
+      const int ce = __float_as_int(c.y);
+      const int e = ce != INT_MAX ? ce : -1;
       cand_e[item * kPredK + j] = e;
       __nv_bfloat16* row = X + (item * kPredK + j) * kMlpInPad;
       if (e >= 0) {
-        write_features(P.desc + static_cast<int64_t>(e) * kDescFloats, o, d, bt[j], row);
+        write_features(P.desc + static_cast<int64_t>(e) * kDescFloats, o, d, c.x, row);
       } else {
         for (int c = 0; c < kMlpInPad; ++c) row[c] = __float2bfloat16(0.f);
       }
@@ -119,9 +109,15 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   if (n_threads == 0) return 0;
   if (static_cast<size_t>(n_queries) > c->work_cap || !c->d_work) {
     cudaFree(c->d_work);
+    cudaFree(c->d_kbuf);
+    cudaFree(c->d_kovf);
     c->d_work = nullptr;
+    c->d_kbuf = nullptr;
+    c->d_kovf = nullptr;
     c->work_cap = 0;
     cudaError_t e = cudaMalloc(&c->d_work, static_cast<size_t>(n_queries) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_kbuf, static_cast<size_t>(n_queries) * kCandK * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_kovf, static_cast<size_t>(n_queries));
     if (e != cudaSuccess) return int(e);
     c->work_cap = static_cast<size_t>(n_queries);
   }
@@ -154,6 +150,8 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   P.work = c->d_work;
   P.qcount = c->d_qctr;
   P.qnext = c->d_qctr + 1;
+  P.kbuf = c->d_kbuf;
+  P.kovf = c->d_kovf;
   classify_kernel<<<static_cast<unsigned>((n_queries + 255) / 256), 256, 0, s>>>(P, n_queries);
   {
     cudaError_t e = cudaGetLastError();

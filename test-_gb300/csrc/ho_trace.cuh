@@ -47,6 +47,8 @@ struct TraceParams {
   uint8_t* __restrict__ rgb;
   DevStats* stats;
   int32_t* work;      // queue of query indices that meet at least one box
+  float2* kbuf;       // [queue slot][kCandK] first ordered candidates (t entry, element bits)
+  uint8_t* kovf;      // [queue slot] more candidates than kCandK were in range
   unsigned* qcount;   // queue length (written by the classify pass)
   unsigned* qnext;    // next queue item to take (intersect pass)
   // learned mode
@@ -266,7 +268,20 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
       int be[kCandK];
       bool overflow;
       const long long c0 = clock64();
-      const bool walked = collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu);
+      bool walked = true;
+      if (pass == 0) {
+        // the classify pass already walked the tree for this ray
+        const float2* kb = P.kbuf + static_cast<int64_t>(item) * kCandK;
+#pragma unroll
+        for (int j = 0; j < kCandK; ++j) {
+          const float2 c = kb[j];
+          bt[j] = c.x;
+          be[j] = __float_as_int(c.y);
+        }
+        overflow = P.kovf[item] != 0;
+      } else {
+        walked = collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu);
+      }
       wu.cyc[0] += clock64() - c0;
       if (!walked) {
         if (lane == 0) atomicOr(&P.stats->status, kStatusStackOverflow);
