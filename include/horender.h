@@ -189,6 +189,21 @@ int ho_intersect(ho_context* ctx, int64_t n, const float* rays, float iso, int i
 int ho_intersect_device(ho_context* ctx, int64_t n, const float* rays_dev, float iso, int iso_enabled,
                         ho_hit* out_dev, void* stream);
 
+/* Allocation-free variant of ho_intersect_device (batched mode). No
+ * reference counterpart. For callers that may not call the CUDA allocator
+ * while querying — an application whose own pool owns all device memory, or a
+ * real-time loop that cannot absorb the device-wide synchronisation of
+ * cudaFree. Its scratch is one fixed device array (about 2.3 MB, held by every
+ * GPU that loads the library's device code until exit; with lazy module
+ * loading it becomes resident at the first call on a device) sized for
+ * HO_NOALLOC_MAX_RAYS rays per call; larger n fails with HO_ERR_RANGE. Needs ho_build_bvh first; the
+ * caller owns rays_dev (n*6 floats) and out_dev (n hits). The first call on a
+ * device looks the array's address up; make it before any stream capture.
+ * All calls share the array: calls whose GPU work overlaps race. */
+#define HO_NOALLOC_MAX_RAYS 32768
+int ho_intersect_device_noalloc(ho_context* ctx, int64_t n, const float* rays_dev, float iso, int iso_enabled,
+                                ho_hit* out_dev, void* stream);
+
 /* Solver mode (HO_MODE_*). No reference counterpart: the reference has one.
  * HO_MODE_LEARNED needs a trained (ho_train_mlp) or loaded (ho_mlp_load)
  * network. */

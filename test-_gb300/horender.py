@@ -24,6 +24,7 @@ ERRORS = {-1: "HO_ERR_ARG", -2: "HO_ERR_CUDA", -3: "HO_ERR_STATE", -4: "HO_ERR_I
           -6: "HO_ERR_NOMEM", -7: "HO_ERR_RANGE", -8: "HO_ERR_DEVICE"}
 MODE_PLAIN, MODE_LEARNED, MODE_BATCHED = 0, 1, 2
 MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
+NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
 FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW = 1, 2, 4
 
@@ -87,6 +88,7 @@ def _load():
     L.ho_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.ho_save_ppm.argtypes = [vp, i32, i32, C.c_char_p]
     L.ho_measure_fp32_peak.argtypes = [i32, C.POINTER(C.c_double)]
+    L.ho_intersect_device_noalloc.argtypes = [vp, i64, vp, f32, i32, vp, vp]
     L.ho_mlp_init.argtypes = [vp, C.c_uint64]
     L.ho_mlp_set_params.argtypes = [vp, vp]
     L.ho_mlp_get_params.argtypes = [vp, vp]
@@ -318,6 +320,13 @@ class Context:
 
     def mlp_load(self, path: str):
         self._ck(lib.ho_mlp_load(self.h, str(path).encode()))
+
+    def intersect_device_noalloc(self, n: int, rays_ptr: int, iso: float, iso_enabled: bool, out_ptr: int,
+                                 stream_ptr):
+        """Batched-mode ray queries that never call the CUDA allocator (scratch
+        in a fixed device array; at most NOALLOC_MAX_RAYS rays per call)."""
+        self._ck(lib.ho_intersect_device_noalloc(self.h, int(n), rays_ptr, float(iso), int(iso_enabled), out_ptr,
+                                                 stream_ptr))
 
     def stats(self) -> dict:
         s = _Stats()

@@ -1,0 +1,60 @@
+"""ho_intersect_device_noalloc — the entry point for callers that may not
+call the CUDA allocator while querying (an application whose own pool owns
+all device memory, or a real-time loop that cannot absorb cudaFree's
+device-wide synchronisation). Its scratch is a fixed device array for at most
+HO_NOALLOC_MAX_RAYS rays per call.
+
+Checked through the C ABI against the regular entry point, on two calls in a
+row, with the tolerance the other GPU tests use (hit identity on >= 99.9% of
+rays, t within 2e-4); the second call takes no device memory; a call over the
+limit is refused with HO_ERR_RANGE. This file sorts last so a run that stops
+at the first failure has already run every other test.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import horender as hr
+import oracle_bind as ob
+
+pytestmark = pytest.mark.gpu
+
+
+def _hits(buf):
+    return buf.cpu().numpy().view(hr.HIT_DTYPE).reshape(-1)
+
+
+def test_noalloc_matches_regular_entry_point_on_two_calls():
+    import torch
+
+    ctx, w = hr.workload_context("hex4_p4")
+    W = H = 128  # 16,384 rays, under the per-call limit
+    rays = ob.camera_rays(w.camera.lookfrom, w.camera.lookat, w.camera.vup, w.camera.vfov_deg, W, H)
+    n = rays.shape[0]
+    iso = w.isovalues[0]
+    ctx.set_mode(hr.MODE_BATCHED)
+    ref = ctx.intersect(rays, iso, True)  # the existing entry point
+    d_rays = torch.from_numpy(rays).cuda()
+    d_out = torch.zeros(n * hr.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    torch.cuda.synchronize()
+    free = []
+    for call in range(2):
+        d_out.fill_(0xFF)  # stale contents must not leak into the result
+        ctx.intersect_device_noalloc(n, d_rays.data_ptr(), iso, True, d_out.data_ptr(), stream)
+        torch.cuda.synchronize()
+        got = _hits(d_out)
+        same = (got["kind"] == ref["kind"]) & (got["elem"] == ref["elem"]) & (got["face"] == ref["face"])
+        assert same.mean() >= 0.999, (call, same.mean())
+        hit = same & (ref["kind"] > 0)
+        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 2e-4, call
+        assert (ref["kind"] > 0).sum() > 1000
+        free.append(torch.cuda.mem_get_info()[0])
+    # the first call places the fixed scratch array on the device (CUDA loads
+    # module data lazily); after that a call takes no device memory
+    assert abs(free[1] - free[0]) < (1 << 20)
+    with pytest.raises(hr.HoError) as ei:
+        ctx.intersect_device_noalloc(hr.NOALLOC_MAX_RAYS + 1, d_rays.data_ptr(), iso, True, d_out.data_ptr(), stream)
+    assert ei.value.code == -7 and "limit" in str(ei.value)
+    ctx.close()
