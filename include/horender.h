@@ -131,8 +131,12 @@ void ho_destroy(ho_context* ctx);
 const char* ho_last_error(const ho_context* ctx);
 
 /* Replaces: bool load_xml_fld(xml, fld, Scene&) (FEM-AABB/xml_fld_loader.h:14-16,
- * xml_fld_loader.cpp:16-402). Hexahedra with curved edges/faces; FLD payload
- * ASCII or base64+zlib FP64. Appends to the scene. */
+ * xml_fld_loader.cpp:16-402). Nektar++ hexahedra with curved edges/faces,
+ * composites/expansions; FLD payload ASCII or base64 of zlib / raw deflate /
+ * plain FP64 (FP32). Appends to the scene; on error the scene is unchanged.
+ * HO_ERR_IO: mesh file unreadable; HO_ERR_PARSE: no vertices or no hexahedra;
+ * HO_ERR_RANGE: geometry modes outside [2, 9] or field modes outside [1, 9].
+ * A missing or empty FLD file loads the geometry without field. */
 int ho_load_xml_fld(ho_context* ctx, const char* xml_path, const char* fld_path);
 
 /* Replaces: Scene::add_hex (FEM-AABB/raytracer.h:118-166), batched.
