@@ -110,6 +110,16 @@ def flops_field(n):  # u and grad: (2n^3 + 3n^2 + 4n) FMA + basis (3 x 8n)
     return 2 * (2 * n**3 + 3 * n**2 + 4 * n) + 3 * 8 * n
 
 
+# DRAM bytes (read + write) of one intersect launch, from an ncu capture of the
+# same workload (dram__bytes_read.sum + dram__bytes_write.sum; the capture
+# command is in profiles/isect_learned_hex32_p6.md). Keyed by workload, image
+# size and mode; absent -> null.
+ISECT_TRAFFIC = {
+    ("hex32_p6", 1920, 1080, "learned"): 159.22e6 + 4.99e6,
+    ("hex32_p6", 480, 272, "learned"): 28.74e6 + 1.60e6,
+}
+
+
 def algorithmic_flops(st, n):
     # + 3x3 inverse and update per Newton iteration (about 60 flops each)
     return (st["geom_evals"] * flops_geom(n) + st["map_evals"] * flops_map(n) + st["field_evals"] * flops_field(n)
@@ -347,7 +357,8 @@ def run_gpu(args, rank, world):
                    "l2": "flushed (256 MiB write) before every timed step",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": (achieved_tflops / fp32_peak) if fp32_peak else None, "traffic": None,
+                     "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,
+                     "traffic": ISECT_TRAFFIC.get((w.name, W, H, head)),
                      "peak_source": "FP32 FMA loop measured in this run (peaks file has HBM and bf16 only)",
                      "flops_per_launch": flops},
         "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4 * n_iso,

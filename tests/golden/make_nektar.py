@@ -13,7 +13,8 @@ placed there), with curved edges and faces sampled from F.
 
   nek_faces   12 hexes given by face ids; curved edges (GLL and evenly spaced
               points, random edge directions), curved faces (evenly spaced,
-              grids written in random orientations); NUMMODES=5; one field u,
+              grids written in random orientations); NUMMODES=5; one smooth
+              field u (random modal coefficients decaying as 0.4^(i+j+k)),
               base64 + zlib FP64.
   nek_verts   8 hexes given by vertex ids; two composites with
               NUMMODESPERDIR="4,5,6" and NUMMODES="3"; fields u,v (the hex's
@@ -200,7 +201,10 @@ def main():
                           "    <DOMAIN> C[0] </DOMAIN>"],
             "expansions": ["  <EXPANSIONS>", '    <E COMPOSITE="C[0]" NUMMODES="5" TYPE="MODIFIED" FIELDS="u" />',
                            "  </EXPANSIONS>"]}
-    coef = rng.standard_normal(len(m.hexes) * 125)
+    # smooth field: modal coefficients (i fastest) decaying as 0.4^(i+j+k)
+    i, j, k = np.meshgrid(np.arange(5), np.arange(5), np.arange(5), indexing="ij")
+    decay = (0.4 ** (i + j + k)).transpose(2, 1, 0).reshape(-1)
+    coef = (rng.standard_normal((len(m.hexes), 125)) * decay).reshape(-1)
     payload = base64.b64encode(zlib.compress(coef.astype("<f8").tobytes())).decode()
     cases["nek_faces"] = (m.xml("faces", ce, cf, tail), fld_text("u", payload, "B64Z-LittleEndian"))
 
