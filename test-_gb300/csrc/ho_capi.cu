@@ -127,7 +127,8 @@ int read_stats(ho_context* c) {
   s.status = ds.status;
   if (ds.status != 0)
     return fail(c, HO_ERR_DEVICE, "kernel reported status " + std::to_string(ds.status) +
-                                      (ds.status & ho::kStatusStackOverflow ? " (traversal stack overflow)" : ""));
+                                      (ds.status & ho::kStatusStackOverflow ? " (traversal stack overflow)" : "") +
+                                      (ds.status & ho::kStatusRoundGuard ? " (intersection round did not finish)" : ""));
   return HO_OK;
 }
 
@@ -166,6 +167,14 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_kbuf);
     cudaFree(c->d_kovf);
     cudaFree(c->d_qctr);
+    cudaFree(c->rounds.state);
+    cudaFree(c->rounds.pairs);
+    cudaFree(c->rounds.pelem);
+    cudaFree(c->rounds.prank);
+    cudaFree(c->rounds.batches);
+    cudaFree(c->rounds.ecount);
+    cudaFree(c->rounds.eoff);
+    cudaFree(c->rounds.ctr);
     cudaFree(c->d_feat);
     cudaFree(c->d_pred);
     cudaFree(c->d_cand);

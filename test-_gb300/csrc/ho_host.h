@@ -68,6 +68,28 @@ int load_xml_fld(const std::string& xml, const std::string& fld, HostScene& hs, 
 
 }  // namespace ho
 
+namespace ho {
+// Scratch of the element-major intersection rounds, grown on demand.
+struct RoundBufs {
+  void* state = nullptr;     // per queue item
+  size_t state_cap = 0;
+  void* pairs = nullptr;     // gathered + element-sorted pairs
+  size_t pairs_cap = 0;
+  int32_t* pelem = nullptr;
+  size_t pelem_cap = 0;
+  uint32_t* prank = nullptr;
+  size_t prank_cap = 0;
+  void* batches = nullptr;
+  size_t batches_cap = 0;
+  uint32_t* ecount = nullptr;  // per element
+  size_t ecount_cap = 0;
+  uint32_t* eoff = nullptr;
+  size_t eoff_cap = 0;
+  unsigned* ctr = nullptr;   // pairs, batches, next batch
+  size_t ctr_cap = 0;
+};
+}  // namespace ho
+
 struct ho_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -113,6 +135,7 @@ struct ho_context {
   uint8_t* d_kovf = nullptr;
   size_t work_cap = 0;
   unsigned* d_qctr = nullptr;     // [0] queue length, [1] next item
+  ho::RoundBufs rounds;
   void* h_pinned = nullptr;
   size_t pinned_cap = 0;
 };

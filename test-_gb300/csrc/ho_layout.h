@@ -62,6 +62,7 @@ struct DevStats {
 
 constexpr int kStatusStackOverflow = 1;
 constexpr int kStatusBadModes = 2;
+constexpr int kStatusRoundGuard = 4;
 
 // Per-face hull boxes: 6 faces x (lo xyz, hi xyz).
 constexpr int kFaceBoxFloats = 36;

@@ -1,0 +1,243 @@
+// Host side of the element-major intersection rounds (batched and learned
+// modes) and the small kernels between rounds: gather each ray's next
+// candidate, bucket the pairs by element (counting sort), cut the buckets
+// into batches, and write the final results.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "ho_host.h"
+#include "ho_rounds.cuh"
+
+namespace ho {
+
+__global__ void __launch_bounds__(1024) scan_kernel(uint32_t* __restrict__ data, int64_t len);
+
+__global__ void round_init_kernel(RayState* __restrict__ st, const uint8_t* __restrict__ kovf, unsigned n_items) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_items) return;
+  RayState r;
+  r.best = miss_state();
+  r.cursor = 0;
+  r.pass = 0;
+  r.kt = -FLT_MAX;
+  r.ke = -1;
+  r.done = 0;
+  r.ovf = kovf[i];
+  r.its = 0;
+  r.pad = 0;
+  st[i] = r;
+}
+
+// One thread per ray in flight: its next ordered candidate whose padded box
+// the ray meets before the closest hit so far (the candidate loop of the
+// reference's traversal, FEM-AABB/raytracer.cu:117-356, in ascending
+// (entry t, element) order). A ray whose list was cut at kCandK walks the
+// tree again for the candidates after the last visited one.
+__global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, unsigned n_items,
+                                    RoundPair* __restrict__ pairs, int32_t* __restrict__ pelem,
+                                    uint32_t* __restrict__ prank, uint32_t* __restrict__ ecount,
+                                    unsigned* __restrict__ ctr) {
+  const unsigned item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= n_items) return;
+  RayState& r = st[item];
+  if (r.done) return;
+  float3 o, d;
+  int iso_idx;
+  query_ray(P, P.work[item], o, d, iso_idx);
+  Work w;
+  float2* kb = P.kbuf + static_cast<int64_t>(item) * kCandK;
+  for (int guard = 0; guard < (1 << 20); ++guard) {
+    if (r.cursor >= kCandK) {
+      if (!r.ovf) {
+        r.done = 1;
+        break;
+      }
+      float bt[kCandK];
+      int be[kCandK];
+      bool overflow;
+      if (!collect(P, o, d, r.best.t, r.kt, r.ke, bt, be, overflow, w)) {
+        atomicOr(&P.stats->status, kStatusStackOverflow);
+        r.done = 1;
+        break;
+      }
+      for (int j = 0; j < kCandK; ++j) kb[j] = make_float2(bt[j], __int_as_float(be[j]));
+      r.ovf = overflow ? 1 : 0;
+      r.cursor = 0;
+      ++r.pass;
+      ++w.restarts;
+      r.best.flags |= HO_FLAG_OVERFLOW;
+    }
+    const float2 c = kb[r.cursor];
+    const float ct = c.x;
+    const int ce = __float_as_int(c.y);
+    if (ce == INT_MAX || ct > r.best.t) {
+      r.done = 1;
+      break;
+    }
+    const int j = r.cursor;
+    ++r.cursor;
+    r.kt = ct;
+    r.ke = ce;
+    const float* b = P.box + 6 * static_cast<int64_t>(ce);
+    const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
+    const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
+    float te, tx;
+    if (!ray_box(o, d, lo, hi, 0.001f, r.best.t, te, tx)) continue;
+    const unsigned k = atomicAdd(ctr, 1u);
+    RoundPair p;
+    p.item = static_cast<int32_t>(item);
+    p.j = r.pass == 0 ? j : -1;
+    p.te = te;
+    p.tx = tx;
+    pairs[k] = p;
+    pelem[k] = ce;
+    prank[k] = atomicAdd(&ecount[ce], 1u);
+    break;
+  }
+  if (w.nodes || w.restarts) {
+    atomicAdd(&P.stats->c[ST_NODES], static_cast<unsigned long long>(w.nodes));
+    atomicAdd(&P.stats->c[ST_RESTART], static_cast<unsigned long long>(w.restarts));
+  }
+}
+
+__global__ void round_scatter_kernel(const RoundPair* __restrict__ pairs, const int32_t* __restrict__ pelem,
+                                     const uint32_t* __restrict__ prank, const uint32_t* __restrict__ eoff,
+                                     unsigned n_pairs, RoundPair* __restrict__ sorted) {
+  const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_pairs) return;
+  sorted[eoff[pelem[k]] + prank[k]] = pairs[k];
+}
+
+// Each element's pairs in batches of at most B.
+__global__ void round_batch_kernel(const uint32_t* __restrict__ ecount, const uint32_t* __restrict__ eoff,
+                                   int64_t n_elem, int B, RoundBatch* __restrict__ batches,
+                                   unsigned* __restrict__ n_batches) {
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n_elem) return;
+  const int c = static_cast<int>(ecount[e]);
+  if (c == 0) return;
+  const int nb = (c + B - 1) / B;
+  const unsigned base = atomicAdd(n_batches, static_cast<unsigned>(nb));
+  for (int k = 0; k < nb; ++k) {
+    RoundBatch bt;
+    bt.elem = static_cast<int32_t>(e);
+    bt.first = static_cast<int32_t>(eoff[e]) + k * B;
+    bt.count = min(B, c - k * B);
+    bt.pad = 0;
+    batches[base + k] = bt;
+  }
+}
+
+__global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ st, unsigned n_items) {
+  const unsigned item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= n_items) return;
+  const int64_t q = P.work[item];
+  float3 o, d;
+  int iso_idx;
+  query_ray(P, q, o, d, iso_idx);
+  write_result(P, q, d, st[item].best, static_cast<uint32_t>(st[item].its));
+}
+
+// Grow-only device buffer of `want` elements of `size` bytes.
+template <typename T>
+static cudaError_t grow(T*& p, size_t& cap, size_t want, size_t size) {
+  if (p && cap >= want) return cudaSuccess;
+  cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  void* q = nullptr;
+  const cudaError_t e = cudaMalloc(&q, std::max<size_t>(want, 1) * size);
+  if (e == cudaSuccess) {
+    p = static_cast<T*>(q);
+    cap = want;
+  }
+  return e;
+}
+
+#define RT_TRY(x)                        \
+  do {                                   \
+    const cudaError_t e_ = (x);          \
+    if (e_ != cudaSuccess) return int(e_); \
+  } while (0)
+
+int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned) {
+  unsigned n_items = 0;
+  RT_TRY(cudaMemcpyAsync(&n_items, P.qcount, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  RT_TRY(cudaStreamSynchronize(s));
+  if (n_items == 0) return 0;
+  const int64_t n_elem = c->n_elem;
+  RoundBufs& rb = c->rounds;
+  RT_TRY(grow(rb.state, rb.state_cap, n_items, sizeof(RayState)));
+  RT_TRY(grow(rb.pairs, rb.pairs_cap, 2 * static_cast<size_t>(n_items), sizeof(RoundPair)));
+  RT_TRY(grow(rb.pelem, rb.pelem_cap, n_items, sizeof(int32_t)));
+  RT_TRY(grow(rb.prank, rb.prank_cap, n_items, sizeof(uint32_t)));
+  RT_TRY(grow(rb.batches, rb.batches_cap, n_items, sizeof(RoundBatch)));
+  RT_TRY(grow(rb.ecount, rb.ecount_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
+  RT_TRY(grow(rb.eoff, rb.eoff_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
+  RT_TRY(grow(rb.ctr, rb.ctr_cap, 4, sizeof(unsigned)));
+  RayState* st = static_cast<RayState*>(rb.state);
+  RoundPair* gathered = static_cast<RoundPair*>(rb.pairs);
+  RoundPair* sorted = gathered + n_items;
+  RoundBatch* batches = static_cast<RoundBatch*>(rb.batches);
+  const unsigned gi = (n_items + 255) / 256;
+  round_init_kernel<<<gi, 256, 0, s>>>(st, P.kovf, n_items);
+  RT_TRY(cudaGetLastError());
+
+  RoundParams R;
+  R.rec = P.rec;
+  R.fbox = P.fbox;
+  R.flags = P.flags;
+  R.rays = P.rays;
+  R.n_rays = P.n_rays;
+  R.cam = P.cam;
+  for (int i = 0; i < 8; ++i) R.iso[i] = P.iso[i];
+  R.iso_on_mask = P.iso_on_mask;
+  R.work = P.work;
+  R.state = st;
+  R.pairs = sorted;
+  R.batches = batches;
+  R.n_batches = rb.ctr + 1;
+  R.next_batch = rb.ctr + 2;
+  R.stats = P.stats;
+  R.desc = P.desc;
+  R.cand_e = P.cand_e;
+  R.pred = P.pred;
+  const int B = round_batch(c->N);
+  for (int round = 0; round < 100000; ++round) {
+    RT_TRY(cudaMemsetAsync(rb.ecount, 0, static_cast<size_t>(n_elem) * sizeof(uint32_t), s));
+    RT_TRY(cudaMemsetAsync(rb.ctr, 0, 4 * sizeof(unsigned), s));
+    round_gather_kernel<<<gi, 256, 0, s>>>(P, st, n_items, gathered, rb.pelem, rb.prank, rb.ecount, rb.ctr);
+    RT_TRY(cudaGetLastError());
+    unsigned n_pairs = 0;
+    RT_TRY(cudaMemcpyAsync(&n_pairs, rb.ctr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    RT_TRY(cudaStreamSynchronize(s));
+    if (n_pairs == 0) break;
+    RT_TRY(cudaMemcpyAsync(rb.eoff, rb.ecount, static_cast<size_t>(n_elem) * sizeof(uint32_t),
+                           cudaMemcpyDeviceToDevice, s));
+    scan_kernel<<<1, 1024, 0, s>>>(rb.eoff, n_elem);
+    round_scatter_kernel<<<(n_pairs + 255) / 256, 256, 0, s>>>(gathered, rb.pelem, rb.prank, rb.eoff, n_pairs,
+                                                                 sorted);
+    round_batch_kernel<<<static_cast<unsigned>((n_elem + 255) / 256), 256, 0, s>>>(rb.ecount, rb.eoff, n_elem, B,
+                                                                                   batches, rb.ctr + 1);
+    RT_TRY(cudaGetLastError());
+    cudaError_t e;
+    switch (c->N) {
+      case 2: e = launch_round_n<2>(R, s, learned); break;
+      case 3: e = launch_round_n<3>(R, s, learned); break;
+      case 4: e = launch_round_n<4>(R, s, learned); break;
+      case 5: e = launch_round_n<5>(R, s, learned); break;
+      case 6: e = launch_round_n<6>(R, s, learned); break;
+      case 7: e = launch_round_n<7>(R, s, learned); break;
+      case 8: e = launch_round_n<8>(R, s, learned); break;
+      case 9: e = launch_round_n<9>(R, s, learned); break;
+      default: e = cudaErrorInvalidValue; break;
+    }
+    RT_TRY(e);
+  }
+  round_finish_kernel<<<gi, 256, 0, s>>>(P, st, n_items);
+  RT_TRY(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace ho

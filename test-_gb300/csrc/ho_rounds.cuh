@@ -1,0 +1,760 @@
+// Element-major intersection rounds (batched and learned modes).
+//
+// The per-candidate algorithm is the reference's hex branch
+// (FEM-AABB/raytracer.cu:184-254): isosurface scan of 17 samples on the
+// candidate's padded-box segment with bracket refinement
+// (FEM-AABB/fem/RayIsosurface.cu:67-188); when that finds no root, the
+// nearest curved-face hit over the 6 faces from 9 seeds each
+// (FEM-AABB/high_order.h:189-304, 409-465). Every step is a Newton solve
+// whose iterations each evaluate the element's geometry (x and J).
+//
+// How the work is laid out here. A round takes, for every ray still in
+// flight, its next ordered candidate (ascending box entry, element index),
+// so a round's (ray, element) pairs are independent. The pairs are bucketed
+// by element, and one warp takes a batch of up to B pairs of one element:
+// the element's record is staged in the warp's shared memory once, and the
+// Newton solves of all its pairs (17 samples each, the refinement, the
+// learned face start, the face seeds) are tasks in a warp-local queue. Each
+// lane runs one solve at a time; every loop iteration all busy lanes
+// evaluate the geometry at their own point (the same code, so the warp stays
+// converged), then advance their own solve; a lane whose solve ends takes
+// the next task. Tasks that depend on others (a pair's refinement or face
+// search after its 17 samples) are queued by the lane that finishes the
+// last task they depend on.
+//
+// Results equal the warp-per-ray kernel's: the same solves with the same
+// start points, iteration caps and acceptance rules, the same bracket (first
+// sign change in sample order) and the same face choice (per face the lowest
+// accepted seed index, faces compared in index order).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ho_device.cuh"
+#include "ho_host.h"
+#include "ho_learn.h"
+#include "ho_trace.cuh"
+
+namespace ho {
+
+constexpr int kRoundBlock = 128;  // 4 warps, one batch each
+constexpr int kSamples = 17;
+
+// Pairs per batch: the per-warp shared memory (record + pair states + task
+// queue) must leave room for two 4-warp blocks per SM.
+constexpr int round_batch(int n) { return n <= 7 ? 16 : 8; }
+
+template <int N>
+struct RoundCfg {
+  static constexpr int B = round_batch(N);  // pairs per batch
+  static constexpr int Ring = B * 64;         // task queue entries (>= B*54 face seeds + B)
+};
+
+// A (ray, candidate) pair of one round, as the gather pass writes it.
+struct RoundPair {
+  int32_t item;  // queue item (ray)
+  int32_t j;     // index of the candidate in the ray's list (learned prediction lookup)
+  float te, tx;  // segment: the candidate's padded box clipped to [0.001, closest hit]
+};
+
+struct RoundBatch {
+  int32_t elem;
+  int32_t first;  // into the element-sorted pairs
+  int32_t count;
+  int32_t pad;
+};
+
+// Per queue item state kept across rounds.
+struct RayState {
+  HitState best;
+  int cursor;   // next candidate in the item's list
+  int pass;     // 0: the classify pass's list (with predictions); >0 re-collected
+  float kt;     // last visited key (entry t, element)
+  int ke;
+  int done;
+  int ovf;      // the current list was cut at kCandK candidates
+  int its;      // Newton and face iterations spent on the ray
+  int pad;
+};
+
+struct RoundParams {
+  const float* __restrict__ rec;
+  const float* __restrict__ fbox;
+  const uint32_t* __restrict__ flags;
+  const float* __restrict__ rays;
+  int64_t n_rays;
+  CamArgs cam;
+  float iso[8];
+  uint32_t iso_on_mask;
+  const int32_t* __restrict__ work;  // queue item -> query index
+  RayState* __restrict__ state;
+  const RoundPair* __restrict__ pairs;  // element-sorted
+  const RoundBatch* __restrict__ batches;
+  const unsigned* n_batches;
+  unsigned* next_batch;
+  DevStats* stats;
+  // learned mode
+  const float* desc;
+  const int32_t* cand_e;
+  const float* pred;
+};
+
+// Task word: kind (3 bits) | pair (5 bits) | argument (8 bits).
+enum TaskKind { TK_SAMPLE = 0, TK_REFINE = 1, TK_FSEED = 2, TK_FLEARN = 3, TK_FPOST = 4, TK_IPOST = 5 };
+__device__ __forceinline__ uint32_t task_word(int kind, int pp, int arg) {
+  return (static_cast<uint32_t>(kind) << 13) | (static_cast<uint32_t>(pp) << 8) | static_cast<uint32_t>(arg);
+}
+
+// Per pair, in the warp's shared memory.
+struct PairSm {
+  float o[3], d[3];
+  float te, tx, iso, best_t;
+  float pxi[3], pv[3], pk, pte;  // learned prediction (xi at te, d xi/dt per element size)
+  int item, elem;
+  int fl;        // bit 0 has field, 1 iso on, 2 prediction available, 3 a warm start was rejected
+  int pend;      // tasks of the current phase still running
+  uint32_t okm;  // samples that converged
+  // isosurface samples
+  float sf[kSamples];
+  float sx[kSamples][3], sg[kSamples][3];
+  // refinement
+  float rlt, rrt, mt, ct;
+  float lsf, lsx[3], lsg[3];
+  float rxi[3];
+  float msf, msdf, msx[3], msg[3];
+  int rit, rstage;
+  // face search
+  int lf;
+  float lt, lx[3];
+  int fseed[6];
+  float ft[6], fx[6][3];
+  // result under construction
+  float ht, hx[3], hg[3];
+  int hface;
+  int its;  // Newton and face iterations of this pair
+};
+
+template <int N>
+struct WarpSm {
+  float rec[record_floats(N)];
+  PairSm pr[RoundCfg<N>::B];
+  uint32_t ring[RoundCfg<N>::Ring];
+  unsigned head, tail;
+  int pad[2];
+};
+
+template <int N>
+constexpr size_t round_smem_bytes() {
+  return (kRoundBlock / 32) * ((sizeof(WarpSm<N>) + 15) / 16 * 16);
+}
+
+__device__ __forceinline__ float3 ld3(const float* p) { return make_float3(p[0], p[1], p[2]); }
+__device__ __forceinline__ void st3(float* p, float3 v) {
+  p[0] = v.x;
+  p[1] = v.y;
+  p[2] = v.z;
+}
+
+// One lane's current solve.
+struct LaneSolve {
+  int task;  // -1: idle
+  int kind, pp, arg;
+  float3 xi;  // inverse map: xi; face Newton: the face point
+  float t;    // inverse map: the sample's t; face Newton: tau
+  int it, cap;
+  bool warm, post, inited;
+  float prev;
+};
+
+__device__ __forceinline__ void push_task(unsigned* tail, uint32_t* ring, int cap, uint32_t w) {
+  const unsigned s = atomicAdd(tail, 1u);
+  ring[s % cap] = w;
+}
+
+// Start an inverse-map solve of f(t) at t from xi0 (warm: capped, with a cold
+// restart on failure).
+__device__ __forceinline__ void start_sample_solve(LaneSolve& s, float t, bool warm, float3 xi0) {
+  s.t = t;
+  s.warm = warm;
+  s.xi = warm ? xi0 : make_float3(0.f, 0.f, 0.f);
+  s.it = 0;
+  s.cap = warm ? kWarmCap : 50;
+  s.post = false;
+}
+
+
+template <int N>
+__device__ __forceinline__ Pred pair_pred(const PairSm& p) {
+  Pred pr;
+  pr.on = (p.fl & 4) != 0;
+  pr.xi_in = ld3(p.pxi);
+  pr.v = ld3(p.pv);
+  pr.k = p.pk;
+  pr.te = p.pte;
+  return pr;
+}
+
+// Face search of a pair after its isosurface search found nothing (or iso
+// is off): the learned start face first when there is one, else the seeds
+// of the faces whose hull box meets [0.001, closest].
+template <int N, bool L>
+__device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox, float cull_hi, Work& w);
+
+template <int N, bool L>
+__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s);
+
+template <int N, bool L>
+__device__ void start_faces(WarpSm<N>& W, int pp, const float* __restrict__ fbox, Work& w, LaneSolve& s) {
+  PairSm& p = W.pr[pp];
+  p.lf = -1;
+  if (L && (p.fl & 4)) {
+    int f0;
+    float3 p0;
+    float tau0;
+    if (predicted_entry(pair_pred<N>(p), 0.001f, p.best_t, f0, p0, tau0)) {
+      p.pend = 1;
+      push_task(&W.tail, W.ring, RoundCfg<N>::Ring, task_word(TK_FLEARN, pp, f0));
+      return;
+    }
+    ++w.rejected;
+  }
+  start_seeds<N, L>(W, pp, fbox, p.best_t, w);
+  if (p.pend == 0) finalize_faces<N, L>(W, pp, s);
+}
+
+template <int N, bool L>
+__device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox, float cull_hi, Work& w) {
+  PairSm& p = W.pr[pp];
+  const float3 o = ld3(p.o), d = ld3(p.d);
+  int n = 0;
+  uint32_t faces = 0;
+  for (int f = 0; f < 6; ++f) {
+    if (f == p.lf) continue;
+    if (face_may_hit(fbox, f, o, d, 0.001f, cull_hi)) {
+      faces |= 1u << f;
+      n += 9;
+    } else {
+      ++w.culled;
+    }
+  }
+  p.pend = n;
+  if (n == 0) return;
+  const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(n));
+  unsigned k = base;
+  for (int f = 0; f < 6; ++f)
+    if (faces >> f & 1u)
+      for (int sd = 0; sd < 9; ++sd) W.ring[(k++) % RoundCfg<N>::Ring] = task_word(TK_FSEED, pp, 9 * f + sd);
+}
+
+// Nearest face over the learned face and every face's first accepted seed,
+// in face order; a hit starts the lane's post evaluation (normal, field).
+// Returns true when the lane got a new solve.
+template <int N, bool L>
+__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s) {
+  PairSm& p = W.pr[pp];
+  float best = p.best_t;
+  int face = -1;
+  float3 xh = make_float3(0.f, 0.f, 0.f);
+  for (int f = 0; f < 6; ++f) {
+    float tf;
+    float3 xf;
+    if (f == p.lf) {
+      tf = p.lt;
+      xf = ld3(p.lx);
+    } else if (p.fseed[f] < 9) {
+      tf = p.ft[f];
+      xf = ld3(p.fx[f]);
+    } else {
+      continue;
+    }
+    if (tf > 0.001f && tf < best) {
+      best = tf;
+      face = f;
+      xh = xf;
+    }
+  }
+  if (face < 0) return false;
+  p.ht = best;
+  st3(p.hx, xh);
+  p.hface = face;
+  s.task = 0;
+  s.kind = TK_FPOST;
+  s.pp = pp;
+  s.xi = xh;
+  s.post = true;
+  s.it = 0;
+  s.warm = false;
+  return true;
+}
+
+// Begin a popped task.
+template <int N, bool L>
+__device__ __forceinline__ void begin_task(WarpSm<N>& W, uint32_t tw, LaneSolve& s) {
+  s.task = static_cast<int>(tw);
+  s.kind = static_cast<int>(tw >> 13);
+  s.pp = static_cast<int>((tw >> 8) & 31u);
+  s.arg = static_cast<int>(tw & 255u);
+  s.inited = false;
+  s.prev = FLT_MAX;
+  const PairSm& p = W.pr[s.pp];
+  if (s.kind == TK_SAMPLE) {
+    const float t = p.te + (p.tx - p.te) * (float(s.arg) / 16.0f);
+    const bool warm = L && (p.fl & 4);
+    start_sample_solve(s, t, warm, warm ? pair_pred<N>(p).at(t) : make_float3(0.f, 0.f, 0.f));
+  } else if (s.kind == TK_FSEED) {
+    const int f = s.arg / 9, sd = s.arg - 9 * f;
+    int fixed, ua, va;
+    float val;
+    face_param(f, fixed, val, ua, va);
+    const int si = sd % 3, sj = sd / 3;
+    float3 q = make_float3(0.f, 0.f, 0.f);
+    setc(q, fixed, val);
+    setc(q, ua, si == 0 ? -0.8f : (si == 1 ? 0.0f : 0.8f));
+    setc(q, va, sj == 0 ? -0.8f : (sj == 1 ? 0.0f : 0.8f));
+    s.xi = q;
+    s.t = 0.f;
+    s.it = 0;
+    s.cap = 50;
+    s.warm = false;
+    s.post = false;
+  } else {  // TK_FLEARN: the predicted entry face and point
+    int f0;
+    float3 p0;
+    float tau0;
+    predicted_entry(pair_pred<N>(p), 0.001f, p.best_t, f0, p0, tau0);
+    s.arg = f0;
+    s.xi = p0;
+    s.t = tau0;
+    s.it = 0;
+    s.cap = kWarmCap;
+    s.warm = true;
+    s.post = false;
+    s.inited = true;
+  }
+}
+
+// The ray's state after a pair produced a hit.
+__device__ __forceinline__ void commit_hit(const RoundParams& P, const PairSm& p, int kind, int face, float t, float3 xi,
+                                           float3 n, float u) {
+  HitState& b = P.state[p.item].best;
+  b.t = t;
+  b.elem = p.elem;
+  b.face = face;
+  b.kind = kind;
+  b.xi = xi;
+  b.n = n;
+  b.u = u;
+  if (p.fl & 8) b.flags |= HO_FLAG_FALLBACK;
+}
+
+template <int N, bool L>
+__global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
+  constexpr int B = RoundCfg<N>::B, R = RoundCfg<N>::Ring;
+  constexpr size_t kWarpBytes = (sizeof(WarpSm<N>) + 15) / 16 * 16;
+  const int lane = threadIdx.x & 31;
+  extern __shared__ __align__(16) unsigned char round_smem[];
+  WarpSm<N>& W = *reinterpret_cast<WarpSm<N>*>(round_smem + (threadIdx.x >> 5) * kWarpBytes);
+  Elem<N, true> el;
+  el.c = CoefRef<true>{static_cast<uint32_t>(__cvta_generic_to_shared(W.rec))};
+  Work w;
+  const unsigned nb = *P.n_batches;
+  for (;;) {
+    unsigned b = 0;
+    if (lane == 0) b = atomicAdd(P.next_batch, 1u);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= nb) break;
+    RoundBatch bt = P.batches[b];
+    bt.count = min(bt.count, B);
+    const float* fbox = P.fbox + static_cast<int64_t>(bt.elem) * kFaceBoxFloats;
+    {
+      const float4* src = reinterpret_cast<const float4*>(P.rec + static_cast<int64_t>(bt.elem) * record_floats(N));
+      float4* dst = reinterpret_cast<float4*>(W.rec);
+      for (int q4 = lane; q4 < record_floats(N) / 4; q4 += 32) dst[q4] = __ldg(src + q4);
+    }
+    const bool has_field = (__ldg(P.flags + bt.elem) & 1u) != 0;
+    el.has_field = has_field;
+    if (lane == 0) {
+      W.head = 0;
+      W.tail = 0;
+    }
+    __syncwarp();
+    if (lane < bt.count) {
+      const RoundPair rp = P.pairs[bt.first + lane];
+      PairSm& p = W.pr[lane];
+      const int64_t q = P.work[rp.item];
+      float3 o, d;
+      int iso_idx;
+      query_ray_from(P.rays, P.n_rays, P.cam, q, o, d, iso_idx);
+      st3(p.o, o);
+      st3(p.d, d);
+      p.te = rp.te;
+      p.tx = rp.tx;
+      p.iso = P.iso[iso_idx];
+      p.best_t = P.state[rp.item].best.t;
+      p.item = rp.item;
+      p.elem = bt.elem;
+      int fl = (has_field ? 1 : 0) | ((P.iso_on_mask >> iso_idx) & 1u ? 2 : 0);
+      if (L && rp.j >= 0 && rp.j < kPredK && P.cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == bt.elem) {
+        const float* y = P.pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
+        p.pxi[0] = y[0]; p.pxi[1] = y[1]; p.pxi[2] = y[2];
+        p.pv[0] = y[3]; p.pv[1] = y[4]; p.pv[2] = y[5];
+        p.pk = __ldg(P.desc + static_cast<int64_t>(bt.elem) * kDescFloats + 45);
+        p.pte = rp.te;
+        fl |= 4;
+      }
+      p.fl = fl;
+      p.okm = 0u;
+      p.lf = -1;
+      p.its = 0;
+      for (int f = 0; f < 6; ++f) p.fseed[f] = 9;
+      ++w.cand;
+    }
+    __syncwarp();
+    LaneSolve s;
+    s.task = -1;
+    s.kind = 0;
+    s.pp = 0;
+    s.arg = 0;
+    s.xi = make_float3(0.f, 0.f, 0.f);
+    s.t = 0.f;
+    s.it = 0;
+    s.cap = 0;
+    s.warm = s.post = s.inited = false;
+    s.prev = FLT_MAX;
+    if (lane < bt.count) {
+      PairSm& p = W.pr[lane];
+      if ((p.fl & 3) == 3) {
+        p.pend = kSamples;
+        const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kSamples));
+        for (int i = 0; i < kSamples; ++i) W.ring[(base + i) % R] = task_word(TK_SAMPLE, lane, i);
+      } else {
+        start_faces<N, L>(W, lane, fbox, w, s);
+      }
+    }
+    __syncwarp();
+    // every task ends within a bounded number of steps; the guard is far above
+    // the longest legal batch and only reports a broken invariant
+    int guard = 0;
+    for (;; ++guard) {
+      if (guard == (1 << 16)) {
+        if (lane == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
+        break;
+      }
+      // -- take tasks
+      const unsigned idle = __ballot_sync(kFull, s.task < 0);
+      const unsigned head = W.head, tail = W.tail;
+      const unsigned avail = tail - head;
+      if (avail == 0u && idle == kFull) break;
+      const unsigned rank = __popc(idle & ((1u << lane) - 1u));
+      if (s.task < 0 && rank < avail) begin_task<N, L>(W, W.ring[(head + rank) % R], s);
+      __syncwarp();
+      if (lane == 0) W.head = head + min(avail, static_cast<unsigned>(__popc(idle)));
+      // -- evaluate: every busy lane evaluates the geometry at its point
+      const bool act = s.task >= 0;
+      float3 X = make_float3(0.f, 0.f, 0.f);
+      float J[9];
+      float u = 0.f;
+      float3 gr = make_float3(0.f, 0.f, 0.f);
+      if (act && s.kind != TK_IPOST) geom_eval<N>(el, s.xi, X, J, w);
+      if (act && s.post && (s.kind != TK_FPOST || has_field)) field_eval<N>(el, s.xi, u, gr, w);
+      // -- advance the solve
+      // end: 0 running, 1 converged / accepted, 2 failed
+      int end = 0;
+      float sf = 0.f, sdf = 0.f;
+      float3 sg = make_float3(0.f, 0.f, 0.f);
+      if (act) {
+        PairSm& p = W.pr[s.pp];
+        if (s.kind == TK_SAMPLE || s.kind == TK_REFINE) {
+          float K[9];
+          invert3(J, K);
+          if (!s.post) {
+            ++w.newton;
+            const float rx = X.x - (p.o[0] + s.t * p.d[0]), ry = X.y - (p.o[1] + s.t * p.d[1]),
+                        rz = X.z - (p.o[2] + s.t * p.d[2]);
+            const float d0 = K[0] * rx + K[1] * ry + K[2] * rz;
+            const float d1 = K[3] * rx + K[4] * ry + K[5] * rz;
+            const float d2 = K[6] * rx + K[7] * ry + K[8] * rz;
+            s.xi.x -= d0;
+            s.xi.y -= d1;
+            s.xi.z -= d2;
+            ++s.it;
+            if (fabsf(d0) < 1e-5f && fabsf(d1) < 1e-5f && fabsf(d2) < 1e-5f) s.post = true;
+            else if (!(fabsf(d0) + fabsf(d1) + fabsf(d2) < FLT_MAX)) end = 2;
+            else if (s.it >= s.cap) end = 2;
+          } else {
+            sg = make_float3(K[0] * gr.x + K[3] * gr.y + K[6] * gr.z, K[1] * gr.x + K[4] * gr.y + K[7] * gr.z,
+                             K[2] * gr.x + K[5] * gr.y + K[8] * gr.z);
+            sf = u - p.iso;
+            sdf = sg.x * p.d[0] + sg.y * p.d[1] + sg.z * p.d[2];
+            end = 1;
+          }
+          if (s.warm && end != 0) {
+            if (end == 1) {
+              ++w.accepted;
+            } else {  // the warm start failed: the plain cold start answers
+              ++w.rejected;
+              atomicOr(&p.fl, 8);
+              atomicAdd(&p.its, s.it);
+              s.warm = false;
+              s.xi = make_float3(0.f, 0.f, 0.f);
+              s.it = 0;
+              s.cap = 50;
+              s.post = false;
+              end = 0;
+            }
+          }
+        } else if (s.kind == TK_FSEED || s.kind == TK_FLEARN) {
+          const int f = s.kind == TK_FSEED ? s.arg / 9 : s.arg;
+          int fixed, ua, va;
+          float val;
+          face_param(f, fixed, val, ua, va);
+          const float tmin = 0.001f, tmax = p.best_t;
+          if (!s.inited) {  // seed: tau from the seed point's position (same evaluation)
+            const float dd = p.d[0] * p.d[0] + p.d[1] * p.d[1] + p.d[2] * p.d[2];
+            float tau = dd > 0.f ? ((X.x - p.o[0]) * p.d[0] + (X.y - p.o[1]) * p.d[1] + (X.z - p.o[2]) * p.d[2]) / dd
+                                 : 0.f;
+            s.t = fminf(fmaxf(tau, tmin), tmax);
+            s.inited = true;
+          }
+          ++w.face;
+          const float rx = X.x - (p.o[0] + s.t * p.d[0]), ry = X.y - (p.o[1] + s.t * p.d[1]),
+                      rz = X.z - (p.o[2] + s.t * p.d[2]);
+          const float m = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));
+          if (m < 1e-4f) {
+            const float pu = getc(s.xi, ua), pv = getc(s.xi, va);
+            end = (pu >= -1.001f && pu <= 1.001f && pv >= -1.001f && pv <= 1.001f && s.t >= tmin && s.t <= tmax) ? 1
+                                                                                                                : 2;
+          } else if (s.it > 5 && m > s.prev * 1.5f) {
+            end = 2;
+          } else {
+            s.prev = m;
+            const float A[9] = {J[ua], J[va], -p.d[0], J[3 + ua], J[3 + va], -p.d[1], J[6 + ua], J[6 + va], -p.d[2]};
+            float K[9];
+            invert3(A, K);
+            const float du = -(K[0] * rx + K[1] * ry + K[2] * rz);
+            const float dv = -(K[3] * rx + K[4] * ry + K[5] * rz);
+            const float dtau = -(K[6] * rx + K[7] * ry + K[8] * rz);
+            const float mx = fmaxf(fabsf(du), fmaxf(fabsf(dv), fabsf(dtau)));
+            const float sc = mx > 0.25f ? 0.25f / mx : 1.0f;
+            float nu = getc(s.xi, ua) + du * sc, nv = getc(s.xi, va) + dv * sc;
+            s.t = fminf(fmaxf(s.t + dtau * sc, tmin), tmax);
+            nu = fminf(fmaxf(nu, -1.5f), 1.5f);
+            nv = fminf(fmaxf(nv, -1.5f), 1.5f);
+            setc(s.xi, ua, nu);
+            setc(s.xi, va, nv);
+            setc(s.xi, fixed, val);
+            if (++s.it >= s.cap) end = 2;
+          }
+          if (end != 0 && s.kind == TK_FLEARN) {
+            if (end == 1) ++w.accepted;
+            else ++w.rejected;
+          }
+        } else {
+          end = 1;  // post evaluations finish in one step
+        }
+        if (end != 0) atomicAdd(&p.its, s.it);
+      }
+      // face seeds: the lowest accepted seed index of each face wins
+      const bool seed_ok = act && end == 1 && s.kind == TK_FSEED;
+      if (seed_ok) atomicMin(&W.pr[s.pp].fseed[s.arg / 9], s.arg % 9);
+      if (act && end != 0 && s.kind == TK_SAMPLE) {  // store the sample
+        PairSm& p = W.pr[s.pp];
+        const int i = s.arg;
+        if (end == 1) {
+          atomicOr(&p.okm, 1u << i);
+          p.sf[i] = sf;
+          st3(p.sx[i], s.xi);
+          st3(p.sg[i], sg);
+        }
+      }
+      __syncwarp();
+      if (seed_ok) {
+        PairSm& p = W.pr[s.pp];
+        const int f = s.arg / 9;
+        if (p.fseed[f] == s.arg % 9) {
+          p.ft[f] = s.t;
+          st3(p.fx[f], s.xi);
+        }
+      }
+      __syncwarp();
+      // -- finished solves: phase transitions
+      if (act && end != 0) {
+        PairSm& p = W.pr[s.pp];
+        const int pp = s.pp;
+        const bool warm_pair = L && (p.fl & 4);
+        s.task = -1;
+        if (s.kind == TK_SAMPLE) {
+          if (atomicSub(&p.pend, 1) == 1) {
+            // all 17 samples done: first sign change between consecutive good samples
+            int prev = -1, found = -1;
+            for (int i = 0; i < kSamples; ++i) {
+              if (!((p.okm >> i) & 1u)) continue;
+              if (prev >= 0 && p.sf[prev] * p.sf[i] <= 0.0f) {
+                found = i;
+                break;
+              }
+              prev = i;
+            }
+            if (found >= 0) {
+              p.rlt = p.te + (p.tx - p.te) * (float(prev) / 16.0f);
+              p.rrt = p.te + (p.tx - p.te) * (float(found) / 16.0f);
+              p.lsf = p.sf[prev];
+              for (int c = 0; c < 3; ++c) {
+                p.lsx[c] = p.sx[prev][c];
+                p.lsg[c] = p.sg[prev][c];
+                p.rxi[c] = p.sx[found][c];
+              }
+              p.rit = 0;
+              p.rstage = 0;
+              p.mt = 0.5f * (p.rlt + p.rrt);
+              s.task = 0;
+              s.kind = TK_REFINE;
+              s.pp = pp;
+              start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f));
+            } else {
+              start_faces<N, L>(W, pp, fbox, w, s);
+            }
+          }
+        } else if (s.kind == TK_REFINE) {
+          if (p.rstage == 0) {  // midpoint solve ended
+            if (end == 2) {
+              start_faces<N, L>(W, pp, fbox, w, s);  // the isosurface search failed
+            } else {
+              p.msf = sf;
+              p.msdf = sdf;
+              st3(p.msx, s.xi);
+              st3(p.msg, sg);
+              float ct = p.mt;
+              if (fabsf(sdf) > 1e-8f) {
+                const float nt = p.mt - sf / sdf;
+                if (nt > p.rlt && nt < p.rrt) ct = nt;
+              }
+              p.ct = ct;
+              p.rstage = 1;
+              s.task = 0;
+              start_sample_solve(s, ct, warm_pair, s.xi);
+            }
+          } else {  // Newton candidate solve ended
+            float ct = p.ct, csf;
+            float3 csx = s.xi, csg;
+            if (end == 1) {
+              csf = sf;
+              csg = sg;
+            } else {  // keep the failed solve's xi
+              ct = p.mt;
+              csf = p.msf;
+              csg = ld3(p.msg);
+            }
+            bool found = false;
+            if (fabsf(csf) < 1e-5f) {
+              p.ht = ct;
+              st3(p.hx, csx);
+              st3(p.hg, csg);
+              found = true;
+            } else {
+              if (p.lsf * csf <= 0.0f) {
+                p.rrt = ct;
+                st3(p.rxi, csx);
+              } else {
+                p.rlt = ct;
+                p.lsf = csf;
+                st3(p.lsx, csx);
+                st3(p.lsg, csg);
+              }
+              if (++p.rit >= 20) {
+                p.ht = 0.5f * (p.rlt + p.rrt);
+                for (int c = 0; c < 3; ++c) {
+                  p.hx[c] = p.lsx[c];
+                  p.hg[c] = p.lsg[c];
+                }
+                found = true;
+              } else {
+                p.mt = 0.5f * (p.rlt + p.rrt);
+                p.rstage = 0;
+                s.task = 0;
+                start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f));
+              }
+            }
+            if (found) {  // the field value at the root's xi, then the hit
+              s.task = 0;
+              s.kind = TK_IPOST;
+              s.xi = ld3(p.hx);
+              s.post = true;
+              s.it = 0;
+              s.warm = false;
+            }
+          }
+        } else if (s.kind == TK_FSEED) {
+          if (atomicSub(&p.pend, 1) == 1) finalize_faces<N, L>(W, pp, s);
+        } else if (s.kind == TK_FLEARN) {
+          if (end == 1) {
+            p.lf = s.arg;
+            p.lt = s.t;
+            st3(p.lx, s.xi);
+          }
+          start_seeds<N, L>(W, pp, fbox, end == 1 ? s.t : p.best_t, w);
+          if (p.pend == 0) finalize_faces<N, L>(W, pp, s);
+        } else if (s.kind == TK_FPOST) {
+          // normal from the Jacobian columns (the face's two tangents)
+          const float3 dr = make_float3(J[0], J[3], J[6]), ds = make_float3(J[1], J[4], J[7]),
+                       dt = make_float3(J[2], J[5], J[8]);
+          const float3 xi = s.xi;
+          float3 n;
+          if (fabsf(xi.x) > 0.9f) n = cross3(ds, dt);
+          else if (fabsf(xi.y) > 0.9f) n = cross3(dr, dt);
+          else n = cross3(dr, ds);
+          n = normalize3(n);
+          if (n.x * p.d[0] + n.y * p.d[1] + n.z * p.d[2] > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+          commit_hit(P, p, HO_HIT_FACE, p.hface, p.ht, xi, n, has_field ? u : 0.f);
+        } else if (s.kind == TK_IPOST) {
+          if (p.ht > 0.001f && p.ht < p.best_t) {
+            float3 n = normalize3(ld3(p.hg));
+            if (n.x * p.d[0] + n.y * p.d[1] + n.z * p.d[2] > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+            commit_hit(P, p, HO_HIT_ISO, -1, p.ht, s.xi, n, u);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    // iterations of the batch's pairs into their rays
+    if (lane < bt.count) P.state[W.pr[lane].item].its += W.pr[lane].its;
+    __syncwarp();
+  }
+  flush_work(P.stats, w, false);
+}
+
+template <int N>
+cudaError_t launch_round_n(const RoundParams& R, cudaStream_t s, bool learned) {
+  static int grid[2] = {0, 0};  // persistent grid: resident blocks per SM x SMs
+  const size_t smem = round_smem_bytes<N>();
+  int& g = grid[learned ? 1 : 0];
+  if (g == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (learned) {
+      cudaFuncSetAttribute(round_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, round_kernel<N, true>, kRoundBlock, smem);
+    } else {
+      cudaFuncSetAttribute(round_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(smem));
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, round_kernel<N, false>, kRoundBlock, smem);
+    }
+    g = sms * (per > 0 ? per : 1);
+  }
+  if (learned) round_kernel<N, true><<<g, kRoundBlock, smem, s>>>(R);
+  else round_kernel<N, false><<<g, kRoundBlock, smem, s>>>(R);
+  return cudaGetLastError();
+}
+
+// explicit instantiations live in ho_trace_n*.cu
+extern template cudaError_t launch_round_n<2>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<3>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<4>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<5>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<6>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<7>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<8>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<9>(const RoundParams& R, cudaStream_t s, bool learned);
+
+}  // namespace ho

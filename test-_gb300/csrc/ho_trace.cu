@@ -76,6 +76,8 @@ __global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16*
   }
 }
 
+int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned);
+
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   TraceParams P;
   P.nodes = c->d_nodes;
@@ -188,19 +190,8 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
     P.cand_e = c->d_cand;
     P.pred = c->d_pred;
   }
-  cudaError_t e;
-  switch (c->N) {
-    case 2: e = launch_n<2>(P, n_queries, n_threads, s, mode); break;
-    case 3: e = launch_n<3>(P, n_queries, n_threads, s, mode); break;
-    case 4: e = launch_n<4>(P, n_queries, n_threads, s, mode); break;
-    case 5: e = launch_n<5>(P, n_queries, n_threads, s, mode); break;
-    case 6: e = launch_n<6>(P, n_queries, n_threads, s, mode); break;
-    case 7: e = launch_n<7>(P, n_queries, n_threads, s, mode); break;
-    case 8: e = launch_n<8>(P, n_queries, n_threads, s, mode); break;
-    case 9: e = launch_n<9>(P, n_queries, n_threads, s, mode); break;
-    default: return int(cudaErrorInvalidValue);
-  }
-  return int(e);
+  // element-major rounds over the queued rays
+  return run_rounds(c, P, s, learned);
 }
 
 }  // namespace ho

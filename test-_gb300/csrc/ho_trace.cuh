@@ -184,25 +184,30 @@ __device__ __forceinline__ void shade(const HitState& h, float3 d, uint8_t* out)
 }
 
 // Rays as the kernels see them: query q -> (origin, direction, isovalue index).
-__device__ __forceinline__ void query_ray(const TraceParams& P, int64_t q, float3& o, float3& d, int& iso_idx) {
-  if (P.rays == nullptr) {
-    const int64_t npix = static_cast<int64_t>(P.cam.width) * P.cam.height;
+__device__ __forceinline__ void query_ray_from(const float* __restrict__ rays, int64_t n_rays, const CamArgs& cam,
+                                               int64_t q, float3& o, float3& d, int& iso_idx) {
+  if (rays == nullptr) {
+    const int64_t npix = static_cast<int64_t>(cam.width) * cam.height;
     iso_idx = static_cast<int>(q / npix);
     const int64_t pix = q - static_cast<int64_t>(iso_idx) * npix;
-    const int x = static_cast<int>(pix % P.cam.width), y = static_cast<int>(pix / P.cam.width);
-    const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(P.cam.width);
-    const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(P.cam.height);
-    o = P.cam.origin;
-    d = make_float3(P.cam.llc.x + s * P.cam.horiz.x + t * P.cam.vert.x - o.x,
-                    P.cam.llc.y + s * P.cam.horiz.y + t * P.cam.vert.y - o.y,
-                    P.cam.llc.z + s * P.cam.horiz.z + t * P.cam.vert.z - o.z);
+    const int x = static_cast<int>(pix % cam.width), y = static_cast<int>(pix / cam.width);
+    const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(cam.width);
+    const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(cam.height);
+    o = cam.origin;
+    d = make_float3(cam.llc.x + s * cam.horiz.x + t * cam.vert.x - o.x,
+                    cam.llc.y + s * cam.horiz.y + t * cam.vert.y - o.y,
+                    cam.llc.z + s * cam.horiz.z + t * cam.vert.z - o.z);
     d = normalize3(d);
   } else {
-    iso_idx = static_cast<int>(q / P.n_rays);
-    const float* rp = P.rays + 6 * (q - static_cast<int64_t>(iso_idx) * P.n_rays);
+    iso_idx = static_cast<int>(q / n_rays);
+    const float* rp = rays + 6 * (q - static_cast<int64_t>(iso_idx) * n_rays);
     o = make_float3(rp[0], rp[1], rp[2]);
     d = make_float3(rp[3], rp[4], rp[5]);
   }
+}
+
+__device__ __forceinline__ void query_ray(const TraceParams& P, int64_t q, float3& o, float3& d, int& iso_idx) {
+  query_ray_from(P.rays, P.n_rays, P.cam, q, o, d, iso_idx);
 }
 
 __device__ __forceinline__ void write_result(const TraceParams& P, int64_t q, float3 d, const HitState& best,
