@@ -118,9 +118,14 @@ typedef struct {
   uint64_t restarts;         /* candidate-list overflows                       */
   int32_t max_modes;
   int32_t status;            /* device error status (0 = fine)                 */
-  uint64_t phase_cycles[4];  /* batched/learned: SM cycles spent per warp in
-                                traversal, isosurface scan, bracket refinement,
-                                face search (summed over warps)                */
+  uint64_t phase_cycles[4];  /* warp-per-ray intersect kernel (no-alloc entry):
+                                SM cycles per warp in traversal, isosurface
+                                scan, bracket refinement, face search         */
+  uint64_t rounds;           /* batched/learned: intersection rounds           */
+  uint64_t round_pairs;      /* (ray, element) pairs over all rounds           */
+  uint64_t solve_steps;      /* loop steps of the round kernel's warps         */
+  uint64_t lane_steps;       /* busy lanes summed over those steps: lane use
+                                = lane_steps / (32 * solve_steps)             */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

@@ -125,6 +125,10 @@ int read_stats(ho_context* c) {
   for (int k = 0; k < 4; ++k) s.phase_cycles[k] = ds.c[ho::ST_CYC_TRAV + k];
   s.max_modes = c->N;
   s.status = ds.status;
+  s.rounds = c->last_rounds;
+  s.round_pairs = c->last_pairs;
+  s.solve_steps = ds.c[ho::ST_STEPS];
+  s.lane_steps = ds.c[ho::ST_LANES];
   if (ds.status != 0)
     return fail(c, HO_ERR_DEVICE, "kernel reported status " + std::to_string(ds.status) +
                                       (ds.status & ho::kStatusStackOverflow ? " (traversal stack overflow)" : "") +

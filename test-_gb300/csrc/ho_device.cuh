@@ -32,6 +32,8 @@ struct Work {
   // SM cycles by phase (warp kernels, counted on lane 0): traversal, isosurface
   // scan, bracket refinement, face search
   unsigned long long cyc[4] = {0, 0, 0, 0};
+  // round kernel: loop steps and busy lanes over them (counted on lane 0)
+  unsigned long long steps = 0, lanes = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -301,6 +303,55 @@ __device__ __noinline__ float field_value_raw(CoefRef<SM> c, float3 xi) {
 template <int N, bool SM>
 __device__ __forceinline__ float field_value(const Elem<N, SM>& e, float3 xi) {
   return field_value_raw<N, SM>(e.fld(), xi);
+}
+
+// Components [c0, c1) of one point evaluation, out of line: 0-2 are x, y, z
+// (value and the three partials), 3 is the field. The basis values stay in
+// registers: the rolled k loop picks at[k] / dt[k] with a predicated select
+// instead of reading them back from the stack, and one loop body serves all
+// components, so the code stays small. Same FMA order as contract_vd.
+template <int N, bool SM>
+__device__ __noinline__ void eval_comps(CoefRef<SM> c, float3 xi, int c0, int c1, float4* __restrict__ out) {
+  constexpr int RS = row_stride(N);
+  float ar[N], dr[N], as[N], ds[N], at[N], dt[N];
+  basis_val_der<N>(xi.x, ar, dr);
+  basis_val_der<N>(xi.y, as, ds);
+  basis_val_der<N>(xi.z, at, dt);
+#pragma unroll 1
+  for (int comp = c0; comp < c1; ++comp) {
+    const CoefRef<SM> cc = c.at(comp * block_floats(N));
+    float v = 0.f, vr = 0.f, vs = 0.f, vt = 0.f;
+#pragma unroll 1
+    for (int k = 0; k < N; ++k) {
+      float tk = at[0], dtk = dt[0];
+#pragma unroll
+      for (int m = 1; m < N; ++m)
+        if (k == m) {
+          tk = at[m];
+          dtk = dt[m];
+        }
+      float q0 = 0.f, q1 = 0.f, q2 = 0.f;
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        float row[RS];
+        load_row<N, SM>(cc, (k * N + j) * RS, row);
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          s0 = fmaf(row[i], ar[i], s0);
+          s1 = fmaf(row[i], dr[i], s1);
+        }
+        q0 = fmaf(s0, as[j], q0);
+        q1 = fmaf(s1, as[j], q1);
+        q2 = fmaf(s0, ds[j], q2);
+      }
+      v = fmaf(q0, tk, v);
+      vr = fmaf(q1, tk, vr);
+      vs = fmaf(q2, tk, vs);
+      vt = fmaf(q0, dtk, vt);
+    }
+    out[comp] = make_float4(v, vr, vs, vt);
+  }
 }
 
 // Adjugate / determinant inverse, no singular guard (HexElement.cu:208-225).

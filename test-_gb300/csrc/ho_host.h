@@ -136,6 +136,7 @@ struct ho_context {
   size_t work_cap = 0;
   unsigned* d_qctr = nullptr;     // [0] queue length, [1] next item
   ho::RoundBufs rounds;
+  uint64_t last_rounds = 0, last_pairs = 0;
   void* h_pinned = nullptr;
   size_t pinned_cap = 0;
 };

@@ -51,6 +51,8 @@ enum StatSlot {
   ST_CYC_SCAN,
   ST_CYC_REFINE,
   ST_CYC_FACE,
+  ST_STEPS,
+  ST_LANES,
   ST_COUNT
 };
 

@@ -165,6 +165,8 @@ int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned
   unsigned n_items = 0;
   RT_TRY(cudaMemcpyAsync(&n_items, P.qcount, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   RT_TRY(cudaStreamSynchronize(s));
+  c->last_rounds = 0;
+  c->last_pairs = 0;
   if (n_items == 0) return 0;
   const int64_t n_elem = c->n_elem;
   RoundBufs& rb = c->rounds;
@@ -203,7 +205,7 @@ int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned
   R.desc = P.desc;
   R.cand_e = P.cand_e;
   R.pred = P.pred;
-  const int B = round_batch(c->N);
+  const int B = kRoundChunk;
   for (int round = 0; round < 100000; ++round) {
     RT_TRY(cudaMemsetAsync(rb.ecount, 0, static_cast<size_t>(n_elem) * sizeof(uint32_t), s));
     RT_TRY(cudaMemsetAsync(rb.ctr, 0, 4 * sizeof(unsigned), s));
@@ -213,6 +215,8 @@ int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned
     RT_TRY(cudaMemcpyAsync(&n_pairs, rb.ctr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     RT_TRY(cudaStreamSynchronize(s));
     if (n_pairs == 0) break;
+    ++c->last_rounds;
+    c->last_pairs += n_pairs;
     RT_TRY(cudaMemcpyAsync(rb.eoff, rb.ecount, static_cast<size_t>(n_elem) * sizeof(uint32_t),
                            cudaMemcpyDeviceToDevice, s));
     scan_kernel<<<1, 1024, 0, s>>>(rb.eoff, n_elem);

@@ -40,14 +40,18 @@ namespace ho {
 constexpr int kRoundBlock = 128;  // 4 warps, one batch each
 constexpr int kSamples = 17;
 
-// Pairs per batch: the per-warp shared memory (record + pair states + task
-// queue) must leave room for two 4-warp blocks per SM.
-constexpr int round_batch(int n) { return n <= 7 ? 16 : 8; }
+// Pair slots per warp: the per-warp shared memory (element record, pair
+// slots, task queue) is sized so that three 4-warp blocks fit on an SM up to
+// N = 8 (two at N = 9, whose record alone is 15.5 KB).
+constexpr int round_slots(int n) { return n <= 7 ? 16 : (n == 8 ? 12 : 8); }
+// Pairs per batch: a warp admits a batch's pairs into its slots as earlier
+// pairs finish, so a batch may be several times the slot count.
+constexpr int kRoundChunk = 64;
 
 template <int N>
 struct RoundCfg {
-  static constexpr int B = round_batch(N);  // pairs per batch
-  static constexpr int Ring = B * 64;         // task queue entries (>= B*54 face seeds + B)
+  static constexpr int B = round_slots(N);  // pair slots
+  static constexpr int Ring = B * 64;         // task queue entries (>= B*54 face seeds)
 };
 
 // A (ray, candidate) pair of one round, as the gather pass writes it.
@@ -105,7 +109,8 @@ __device__ __forceinline__ uint32_t task_word(int kind, int pp, int arg) {
   return (static_cast<uint32_t>(kind) << 13) | (static_cast<uint32_t>(pp) << 8) | static_cast<uint32_t>(arg);
 }
 
-// Per pair, in the warp's shared memory.
+// Per pair, in the warp's shared memory. The sample store is dead once the
+// bracket is taken, so the refinement and face-search state overlay it.
 struct PairSm {
   float o[3], d[3];
   float te, tx, iso, best_t;
@@ -114,33 +119,39 @@ struct PairSm {
   int fl;        // bit 0 has field, 1 iso on, 2 prediction available, 3 a warm start was rejected
   int pend;      // tasks of the current phase still running
   uint32_t okm;  // samples that converged
-  // isosurface samples
-  float sf[kSamples];
-  float sx[kSamples][3], sg[kSamples][3];
-  // refinement
-  float rlt, rrt, mt, ct;
-  float lsf, lsx[3], lsg[3];
-  float rxi[3];
-  float msf, msdf, msx[3], msg[3];
-  int rit, rstage;
-  // face search
-  int lf;
-  float lt, lx[3];
-  int fseed[6];
-  float ft[6], fx[6][3];
   // result under construction
   float ht, hx[3], hg[3];
   int hface;
   int its;  // Newton and face iterations of this pair
+  union {
+    struct {  // isosurface samples
+      float sf[kSamples];
+      float sx[kSamples][3], sg[kSamples][3];
+    };
+    struct {
+      // refinement
+      float rlt, rrt, mt, ct;
+      float lsf, lsx[3], lsg[3];
+      float rxi[3];
+      float msf, msdf, msx[3], msg[3];
+      int rit, rstage;
+      // face search
+      int lf;
+      float lt, lx[3];
+      int fseed[6];
+      float ft[6], fx[6][3];
+    };
+  };
 };
 
 template <int N>
 struct WarpSm {
   float rec[record_floats(N)];
   PairSm pr[RoundCfg<N>::B];
-  uint32_t ring[RoundCfg<N>::Ring];
+  uint16_t ring[RoundCfg<N>::Ring];
   unsigned head, tail;
-  int pad[2];
+  unsigned freem;     // free pair slots
+  unsigned admitted;  // pairs of the batch admitted so far
 };
 
 template <int N>
@@ -149,6 +160,9 @@ constexpr size_t round_smem_bytes() {
 }
 
 __device__ __forceinline__ float3 ld3(const float* p) { return make_float3(p[0], p[1], p[2]); }
+// Warp control words are written by other lanes (plain stores and shared
+// atomics) between the warp barriers: always read them from memory.
+__device__ __forceinline__ unsigned ld_ctl(const unsigned* p) { return *reinterpret_cast<const volatile unsigned*>(p); }
 __device__ __forceinline__ void st3(float* p, float3 v) {
   p[0] = v.x;
   p[1] = v.y;
@@ -166,9 +180,9 @@ struct LaneSolve {
   float prev;
 };
 
-__device__ __forceinline__ void push_task(unsigned* tail, uint32_t* ring, int cap, uint32_t w) {
+__device__ __forceinline__ void push_task(unsigned* tail, uint16_t* ring, int cap, uint32_t w) {
   const unsigned s = atomicAdd(tail, 1u);
-  ring[s % cap] = w;
+  ring[s % cap] = static_cast<uint16_t>(w);
 }
 
 // Start an inverse-map solve of f(t) at t from xi0 (warm: capped, with a cold
@@ -201,12 +215,22 @@ template <int N, bool L>
 __device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox, float cull_hi, Work& w);
 
 template <int N, bool L>
-__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s);
+__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s, const RoundParams& P);
+
+// A pair is finished: its iterations go to its ray and its slot is free.
+template <int N>
+__device__ __forceinline__ void pair_done(WarpSm<N>& W, int pp, const RoundParams& P) {
+  const PairSm& p = W.pr[pp];
+  atomicAdd(&P.state[p.item].its, p.its);
+  atomicOr(&W.freem, 1u << pp);
+}
 
 template <int N, bool L>
-__device__ void start_faces(WarpSm<N>& W, int pp, const float* __restrict__ fbox, Work& w, LaneSolve& s) {
+__device__ void start_faces(WarpSm<N>& W, int pp, const float* __restrict__ fbox, Work& w, LaneSolve& s,
+                            const RoundParams& P) {
   PairSm& p = W.pr[pp];
   p.lf = -1;
+  for (int f = 0; f < 6; ++f) p.fseed[f] = 9;
   if (L && (p.fl & 4)) {
     int f0;
     float3 p0;
@@ -219,7 +243,7 @@ __device__ void start_faces(WarpSm<N>& W, int pp, const float* __restrict__ fbox
     ++w.rejected;
   }
   start_seeds<N, L>(W, pp, fbox, p.best_t, w);
-  if (p.pend == 0) finalize_faces<N, L>(W, pp, s);
+  if (p.pend == 0) finalize_faces<N, L>(W, pp, s, P);
 }
 
 template <int N, bool L>
@@ -243,14 +267,14 @@ __device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox
   unsigned k = base;
   for (int f = 0; f < 6; ++f)
     if (faces >> f & 1u)
-      for (int sd = 0; sd < 9; ++sd) W.ring[(k++) % RoundCfg<N>::Ring] = task_word(TK_FSEED, pp, 9 * f + sd);
+      for (int sd = 0; sd < 9; ++sd) W.ring[(k++) % RoundCfg<N>::Ring] = static_cast<uint16_t>(task_word(TK_FSEED, pp, 9 * f + sd));
 }
 
 // Nearest face over the learned face and every face's first accepted seed,
 // in face order; a hit starts the lane's post evaluation (normal, field).
 // Returns true when the lane got a new solve.
 template <int N, bool L>
-__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s) {
+__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s, const RoundParams& P) {
   PairSm& p = W.pr[pp];
   float best = p.best_t;
   int face = -1;
@@ -273,7 +297,10 @@ __device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s) {
       xh = xf;
     }
   }
-  if (face < 0) return false;
+  if (face < 0) {
+    pair_done<N>(W, pp, P);
+    return false;
+  }
   p.ht = best;
   st3(p.hx, xh);
   p.hface = face;
@@ -294,6 +321,10 @@ __device__ __forceinline__ void begin_task(WarpSm<N>& W, uint32_t tw, LaneSolve&
   s.kind = static_cast<int>(tw >> 13);
   s.pp = static_cast<int>((tw >> 8) & 31u);
   s.arg = static_cast<int>(tw & 255u);
+  if (s.pp >= RoundCfg<N>::B || s.kind > TK_IPOST) {  // never queued: drop it
+    s.task = -1;
+    return;
+  }
   s.inited = false;
   s.prev = FLT_MAX;
   const PairSm& p = W.pr[s.pp];
@@ -348,8 +379,48 @@ __device__ __forceinline__ void commit_hit(const RoundParams& P, const PairSm& p
 }
 
 template <int N, bool L>
+__device__ __forceinline__ void admit_pair(WarpSm<N>& W, const RoundParams& P, int slot, const RoundPair& rp, int elem,
+                                           bool has_field, const float* __restrict__ fbox, Work& w, LaneSolve& s) {
+  constexpr int R = RoundCfg<N>::Ring;
+  PairSm& p = W.pr[slot];
+  const int64_t q = P.work[rp.item];
+  float3 o, d;
+  int iso_idx;
+  query_ray_from(P.rays, P.n_rays, P.cam, q, o, d, iso_idx);
+  st3(p.o, o);
+  st3(p.d, d);
+  p.te = rp.te;
+  p.tx = rp.tx;
+  p.iso = P.iso[iso_idx];
+  p.best_t = P.state[rp.item].best.t;
+  p.item = rp.item;
+  p.elem = elem;
+  int fl = (has_field ? 1 : 0) | ((P.iso_on_mask >> iso_idx) & 1u ? 2 : 0);
+  if (L && rp.j >= 0 && rp.j < kPredK && P.cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == elem) {
+    const float* y = P.pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
+    p.pxi[0] = y[0]; p.pxi[1] = y[1]; p.pxi[2] = y[2];
+    p.pv[0] = y[3]; p.pv[1] = y[4]; p.pv[2] = y[5];
+    p.pk = __ldg(P.desc + static_cast<int64_t>(elem) * kDescFloats + 45);
+    p.pte = rp.te;
+    fl |= 4;
+  }
+  p.fl = fl;
+  p.okm = 0u;
+  p.its = 0;
+  ++w.cand;
+  if ((fl & 3) == 3) {
+    p.pend = kSamples;
+    const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kSamples));
+    for (int i = 0; i < kSamples; ++i) W.ring[(base + i) % R] = static_cast<uint16_t>(task_word(TK_SAMPLE, slot, i));
+  } else {
+    start_faces<N, L>(W, slot, fbox, w, s, P);
+  }
+}
+
+template <int N, bool L>
 __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
   constexpr int B = RoundCfg<N>::B, R = RoundCfg<N>::Ring;
+  constexpr unsigned kAllSlots = B >= 32 ? 0xffffffffu : ((1u << B) - 1u);
   constexpr size_t kWarpBytes = (sizeof(WarpSm<N>) + 15) / 16 * 16;
   const int lane = threadIdx.x & 31;
   extern __shared__ __align__(16) unsigned char round_smem[];
@@ -363,8 +434,8 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
     if (lane == 0) b = atomicAdd(P.next_batch, 1u);
     b = __shfl_sync(kFull, b, 0);
     if (b >= nb) break;
-    RoundBatch bt = P.batches[b];
-    bt.count = min(bt.count, B);
+    const RoundBatch bt = P.batches[b];
+    const unsigned count = static_cast<unsigned>(bt.count);
     const float* fbox = P.fbox + static_cast<int64_t>(bt.elem) * kFaceBoxFloats;
     {
       const float4* src = reinterpret_cast<const float4*>(P.rec + static_cast<int64_t>(bt.elem) * record_floats(N));
@@ -376,38 +447,8 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
     if (lane == 0) {
       W.head = 0;
       W.tail = 0;
-    }
-    __syncwarp();
-    if (lane < bt.count) {
-      const RoundPair rp = P.pairs[bt.first + lane];
-      PairSm& p = W.pr[lane];
-      const int64_t q = P.work[rp.item];
-      float3 o, d;
-      int iso_idx;
-      query_ray_from(P.rays, P.n_rays, P.cam, q, o, d, iso_idx);
-      st3(p.o, o);
-      st3(p.d, d);
-      p.te = rp.te;
-      p.tx = rp.tx;
-      p.iso = P.iso[iso_idx];
-      p.best_t = P.state[rp.item].best.t;
-      p.item = rp.item;
-      p.elem = bt.elem;
-      int fl = (has_field ? 1 : 0) | ((P.iso_on_mask >> iso_idx) & 1u ? 2 : 0);
-      if (L && rp.j >= 0 && rp.j < kPredK && P.cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == bt.elem) {
-        const float* y = P.pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
-        p.pxi[0] = y[0]; p.pxi[1] = y[1]; p.pxi[2] = y[2];
-        p.pv[0] = y[3]; p.pv[1] = y[4]; p.pv[2] = y[5];
-        p.pk = __ldg(P.desc + static_cast<int64_t>(bt.elem) * kDescFloats + 45);
-        p.pte = rp.te;
-        fl |= 4;
-      }
-      p.fl = fl;
-      p.okm = 0u;
-      p.lf = -1;
-      p.its = 0;
-      for (int f = 0; f < 6; ++f) p.fseed[f] = 9;
-      ++w.cand;
+      W.freem = kAllSlots;
+      W.admitted = 0;
     }
     __syncwarp();
     LaneSolve s;
@@ -421,42 +462,97 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
     s.cap = 0;
     s.warm = s.post = s.inited = false;
     s.prev = FLT_MAX;
-    if (lane < bt.count) {
-      PairSm& p = W.pr[lane];
-      if ((p.fl & 3) == 3) {
-        p.pend = kSamples;
-        const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kSamples));
-        for (int i = 0; i < kSamples; ++i) W.ring[(base + i) % R] = task_word(TK_SAMPLE, lane, i);
-      } else {
-        start_faces<N, L>(W, lane, fbox, w, s);
-      }
-    }
-    __syncwarp();
     // every task ends within a bounded number of steps; the guard is far above
     // the longest legal batch and only reports a broken invariant
-    int guard = 0;
-    for (;; ++guard) {
-      if (guard == (1 << 16)) {
+    for (int guard = 0;; ++guard) {
+      if (guard == (1 << 18)) {
         if (lane == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
         break;
       }
+      // -- admit the batch's next pairs into free slots
+      {
+        unsigned fm = 0u, adm = 0u;  // lane 0 reads, every lane uses the same values
+        if (lane == 0) {
+          fm = ld_ctl(&W.freem);
+          adm = ld_ctl(&W.admitted);
+        }
+        fm = __shfl_sync(kFull, fm, 0);
+        adm = __shfl_sync(kFull, adm, 0);
+        const unsigned nadm = min(static_cast<unsigned>(__popc(fm)), count - adm);
+        __syncwarp();  // every lane has read freem / admitted before any lane changes them
+        if (nadm > 0u) {
+          if (lane < static_cast<int>(nadm)) {
+            unsigned m = fm;  // the lane-th free slot: drop the lowest `lane` set bits
+            for (int k = 0; k < lane; ++k) m &= m - 1u;
+            const int slot = __ffs(m) - 1;
+            if (slot >= 0 && slot < B) {
+              atomicAnd(&W.freem, ~(1u << slot));
+              LaneSolve scratch;
+              scratch.task = -1;
+              admit_pair<N, L>(W, P, slot, P.pairs[bt.first + adm + lane], bt.elem, has_field, fbox, w, scratch);
+            } else {
+              atomicOr(&P.stats->status, kStatusRoundGuard);
+            }
+          }
+          if (lane == 0) W.admitted = adm + nadm;
+        }
+        __syncwarp();
+      }
       // -- take tasks
       const unsigned idle = __ballot_sync(kFull, s.task < 0);
-      const unsigned head = W.head, tail = W.tail;
+      unsigned head = 0u, tail = 0u, admitted = 0u;
+      if (lane == 0) {
+        head = ld_ctl(&W.head);
+        tail = ld_ctl(&W.tail);
+        admitted = ld_ctl(&W.admitted);
+      }
+      head = __shfl_sync(kFull, head, 0);
+      tail = __shfl_sync(kFull, tail, 0);
+      admitted = __shfl_sync(kFull, admitted, 0);
       const unsigned avail = tail - head;
-      if (avail == 0u && idle == kFull) break;
+      if (avail > static_cast<unsigned>(R)) {  // the queue can never hold more: a broken invariant
+        if (lane == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
+        break;
+      }
+      if (avail == 0u && idle == kFull) {
+        if (admitted >= count) break;
+        __syncwarp();
+        continue;
+      }
       const unsigned rank = __popc(idle & ((1u << lane) - 1u));
       if (s.task < 0 && rank < avail) begin_task<N, L>(W, W.ring[(head + rank) % R], s);
       __syncwarp();
-      if (lane == 0) W.head = head + min(avail, static_cast<unsigned>(__popc(idle)));
+      if (lane == 0) {
+        W.head = head + min(avail, static_cast<unsigned>(__popc(idle)));
+        ++w.steps;
+        w.lanes += 32u - __popc(idle) + min(avail, static_cast<unsigned>(__popc(idle)));
+      }
       // -- evaluate: every busy lane evaluates the geometry at its point
       const bool act = s.task >= 0;
       float3 X = make_float3(0.f, 0.f, 0.f);
       float J[9];
       float u = 0.f;
       float3 gr = make_float3(0.f, 0.f, 0.f);
-      if (act && s.kind != TK_IPOST) geom_eval<N>(el, s.xi, X, J, w);
-      if (act && s.post && (s.kind != TK_FPOST || has_field)) field_eval<N>(el, s.xi, u, gr, w);
+      if (act) {
+        const bool want_geom = s.kind != TK_IPOST;
+        const bool want_field = s.post && (s.kind != TK_FPOST || has_field);
+        float4 r[4];
+        eval_comps<N, true>(el.c, s.xi, want_geom ? 0 : 3, want_field ? 4 : 3, r);
+        if (want_geom) {
+          X = make_float3(r[0].x, r[1].x, r[2].x);
+          J[0] = r[0].y; J[1] = r[0].z; J[2] = r[0].w;
+          J[3] = r[1].y; J[4] = r[1].z; J[5] = r[1].w;
+          J[6] = r[2].y; J[7] = r[2].z; J[8] = r[2].w;
+          ++w.geom;
+        } else {
+          for (int q = 0; q < 9; ++q) J[q] = 0.f;
+        }
+        if (want_field) {
+          u = r[3].x;
+          gr = make_float3(r[3].y, r[3].z, r[3].w);
+          ++w.field;
+        }
+      }
       // -- advance the solve
       // end: 0 running, 1 converged / accepted, 2 failed
       int end = 0;
@@ -596,14 +692,15 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
               prev = i;
             }
             if (found >= 0) {
+              // the refinement state overlays the sample store: read first
+              const float lf0 = p.sf[prev];
+              const float3 lx0 = ld3(p.sx[prev]), lg0 = ld3(p.sg[prev]), rx0 = ld3(p.sx[found]);
               p.rlt = p.te + (p.tx - p.te) * (float(prev) / 16.0f);
               p.rrt = p.te + (p.tx - p.te) * (float(found) / 16.0f);
-              p.lsf = p.sf[prev];
-              for (int c = 0; c < 3; ++c) {
-                p.lsx[c] = p.sx[prev][c];
-                p.lsg[c] = p.sg[prev][c];
-                p.rxi[c] = p.sx[found][c];
-              }
+              p.lsf = lf0;
+              st3(p.lsx, lx0);
+              st3(p.lsg, lg0);
+              st3(p.rxi, rx0);
               p.rit = 0;
               p.rstage = 0;
               p.mt = 0.5f * (p.rlt + p.rrt);
@@ -612,13 +709,13 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
               s.pp = pp;
               start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f));
             } else {
-              start_faces<N, L>(W, pp, fbox, w, s);
+              start_faces<N, L>(W, pp, fbox, w, s, P);
             }
           }
         } else if (s.kind == TK_REFINE) {
           if (p.rstage == 0) {  // midpoint solve ended
             if (end == 2) {
-              start_faces<N, L>(W, pp, fbox, w, s);  // the isosurface search failed
+              start_faces<N, L>(W, pp, fbox, w, s, P);  // the isosurface search failed
             } else {
               p.msf = sf;
               p.msdf = sdf;
@@ -685,7 +782,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             }
           }
         } else if (s.kind == TK_FSEED) {
-          if (atomicSub(&p.pend, 1) == 1) finalize_faces<N, L>(W, pp, s);
+          if (atomicSub(&p.pend, 1) == 1) finalize_faces<N, L>(W, pp, s, P);
         } else if (s.kind == TK_FLEARN) {
           if (end == 1) {
             p.lf = s.arg;
@@ -693,7 +790,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             st3(p.lx, s.xi);
           }
           start_seeds<N, L>(W, pp, fbox, end == 1 ? s.t : p.best_t, w);
-          if (p.pend == 0) finalize_faces<N, L>(W, pp, s);
+          if (p.pend == 0) finalize_faces<N, L>(W, pp, s, P);
         } else if (s.kind == TK_FPOST) {
           // normal from the Jacobian columns (the face's two tangents)
           const float3 dr = make_float3(J[0], J[3], J[6]), ds = make_float3(J[1], J[4], J[7]),
@@ -706,19 +803,18 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
           n = normalize3(n);
           if (n.x * p.d[0] + n.y * p.d[1] + n.z * p.d[2] > 0.f) n = make_float3(-n.x, -n.y, -n.z);
           commit_hit(P, p, HO_HIT_FACE, p.hface, p.ht, xi, n, has_field ? u : 0.f);
+          pair_done<N>(W, pp, P);
         } else if (s.kind == TK_IPOST) {
           if (p.ht > 0.001f && p.ht < p.best_t) {
             float3 n = normalize3(ld3(p.hg));
             if (n.x * p.d[0] + n.y * p.d[1] + n.z * p.d[2] > 0.f) n = make_float3(-n.x, -n.y, -n.z);
             commit_hit(P, p, HO_HIT_ISO, -1, p.ht, s.xi, n, u);
           }
+          pair_done<N>(W, pp, P);
         }
       }
       __syncwarp();
     }
-    // iterations of the batch's pairs into their rays
-    if (lane < bt.count) P.state[W.pr[lane].item].its += W.pr[lane].its;
-    __syncwarp();
   }
   flush_work(P.stats, w, false);
 }

@@ -79,6 +79,8 @@ __global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16*
 int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned);
 
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
+  c->last_rounds = 0;
+  c->last_pairs = 0;
   TraceParams P;
   P.nodes = c->d_nodes;
   P.rec = c->d_rec;

@@ -59,7 +59,9 @@ class _Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("rays", "candidates", "geom_evals", "map_evals", "field_evals",
                                           "newton_iters", "face_iters", "faces_culled", "node_visits",
                                           "mlp_accepted", "mlp_rejected", "restarts")] + [
-        ("max_modes", C.c_int32), ("status", C.c_int32), ("phase_cycles", C.c_uint64 * 4)]
+        ("max_modes", C.c_int32), ("status", C.c_int32), ("phase_cycles", C.c_uint64 * 4),
+        ("rounds", C.c_uint64), ("round_pairs", C.c_uint64), ("solve_steps", C.c_uint64),
+        ("lane_steps", C.c_uint64)]
 
 
 def _load():
