@@ -208,49 +208,26 @@ __device__ __forceinline__ Pred pair_pred(const PairSm& p) {
   return pr;
 }
 
-// Face search of a pair after its isosurface search found nothing (or iso
-// is off): the learned start face first when there is one, else the seeds
-// of the faces whose hull box meets [0.001, closest].
-template <int N, bool L>
-__device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox, float cull_hi, Work& w);
-
-template <int N, bool L>
-__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s, const RoundParams& P);
-
 // A pair is finished: its iterations go to its ray and its slot is free.
 template <int N>
-__device__ __forceinline__ void pair_done(WarpSm<N>& W, int pp, const RoundParams& P) {
+__device__ __forceinline__ void pair_done(WarpSm<N>& W, int pp, const RoundParams* P) {
   const PairSm& p = W.pr[pp];
-  atomicAdd(&P.state[p.item].its, p.its);
+  atomicAdd(&P->state[p.item].its, p.its);
   atomicOr(&W.freem, 1u << pp);
 }
 
-template <int N, bool L>
-__device__ void start_faces(WarpSm<N>& W, int pp, const float* __restrict__ fbox, Work& w, LaneSolve& s,
-                            const RoundParams& P) {
-  PairSm& p = W.pr[pp];
-  p.lf = -1;
-  for (int f = 0; f < 6; ++f) p.fseed[f] = 9;
-  if (L && (p.fl & 4)) {
-    int f0;
-    float3 p0;
-    float tau0;
-    if (predicted_entry(pair_pred<N>(p), 0.001f, p.best_t, f0, p0, tau0)) {
-      p.pend = 1;
-      push_task(&W.tail, W.ring, RoundCfg<N>::Ring, task_word(TK_FLEARN, pp, f0));
-      return;
-    }
-    ++w.rejected;
-  }
-  start_seeds<N, L>(W, pp, fbox, p.best_t, w);
-  if (p.pend == 0) finalize_faces<N, L>(W, pp, s, P);
-}
+// The pair-level steps below run once per pair phase, not once per Newton
+// step, so they are kept out of line: the per-step loop stays small in the
+// instruction cache. Counters come back in the return value.
 
-template <int N, bool L>
-__device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox, float cull_hi, Work& w) {
+// Queue the 9 seeds of every face (other than the learned face) whose hull
+// box meets [0.001, cull_hi]; returns the number of faces culled.
+template <int N>
+__device__ __noinline__ int start_seeds(WarpSm<N>* Wp, int pp, const float* __restrict__ fbox, float cull_hi) {
+  WarpSm<N>& W = *Wp;
   PairSm& p = W.pr[pp];
   const float3 o = ld3(p.o), d = ld3(p.d);
-  int n = 0;
+  int n = 0, culled = 0;
   uint32_t faces = 0;
   for (int f = 0; f < 6; ++f) {
     if (f == p.lf) continue;
@@ -258,23 +235,26 @@ __device__ void start_seeds(WarpSm<N>& W, int pp, const float* __restrict__ fbox
       faces |= 1u << f;
       n += 9;
     } else {
-      ++w.culled;
+      ++culled;
     }
   }
   p.pend = n;
-  if (n == 0) return;
+  if (n == 0) return culled;
   const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(n));
   unsigned k = base;
   for (int f = 0; f < 6; ++f)
     if (faces >> f & 1u)
-      for (int sd = 0; sd < 9; ++sd) W.ring[(k++) % RoundCfg<N>::Ring] = static_cast<uint16_t>(task_word(TK_FSEED, pp, 9 * f + sd));
+      for (int sd = 0; sd < 9; ++sd)
+        W.ring[(k++) % RoundCfg<N>::Ring] = static_cast<uint16_t>(task_word(TK_FSEED, pp, 9 * f + sd));
+  return culled;
 }
 
 // Nearest face over the learned face and every face's first accepted seed,
-// in face order; a hit starts the lane's post evaluation (normal, field).
-// Returns true when the lane got a new solve.
-template <int N, bool L>
-__device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s, const RoundParams& P) {
+// in face order. A hit is left in the pair's result fields (the caller
+// starts its post evaluation); no hit finishes the pair.
+template <int N>
+__device__ __noinline__ bool finalize_faces(WarpSm<N>* Wp, int pp, const RoundParams* P) {
+  WarpSm<N>& W = *Wp;
   PairSm& p = W.pr[pp];
   float best = p.best_t;
   int face = -1;
@@ -304,14 +284,54 @@ __device__ bool finalize_faces(WarpSm<N>& W, int pp, LaneSolve& s, const RoundPa
   p.ht = best;
   st3(p.hx, xh);
   p.hface = face;
+  return true;
+}
+
+__device__ __forceinline__ void start_post(LaneSolve& s, int kind, int pp, float3 xi) {
   s.task = 0;
-  s.kind = TK_FPOST;
+  s.kind = kind;
   s.pp = pp;
-  s.xi = xh;
+  s.xi = xi;
   s.post = true;
   s.it = 0;
   s.warm = false;
-  return true;
+}
+
+// Face search of a pair after its isosurface search found nothing (or iso is
+// off): the learned start face first when there is one, else the seeds of
+// the faces whose hull box meets [0.001, closest]. Returns culled faces |
+// 256 when a learned start was rejected | 65536 when the pair needs its face
+// post evaluation now.
+template <int N, bool L>
+__device__ __noinline__ int start_faces(WarpSm<N>* Wp, int pp, const float* __restrict__ fbox, const RoundParams* P) {
+  WarpSm<N>& W = *Wp;
+  PairSm& p = W.pr[pp];
+  p.lf = -1;
+  for (int f = 0; f < 6; ++f) p.fseed[f] = 9;
+  int code = 0;
+  if (L && (p.fl & 4)) {
+    int f0;
+    float3 p0;
+    float tau0;
+    if (predicted_entry(pair_pred<N>(p), 0.001f, p.best_t, f0, p0, tau0)) {
+      p.pend = 1;
+      push_task(&W.tail, W.ring, RoundCfg<N>::Ring, task_word(TK_FLEARN, pp, f0));
+      return 0;
+    }
+    code |= 256;
+  }
+  code |= start_seeds<N>(Wp, pp, fbox, p.best_t);
+  if (p.pend == 0 && finalize_faces<N>(Wp, pp, P)) code |= 65536;
+  return code;
+}
+
+template <int N, bool L>
+__device__ __forceinline__ void face_phase(WarpSm<N>& W, int pp, const float* __restrict__ fbox, const RoundParams* P,
+                                           Work& w, LaneSolve& s) {
+  const int code = start_faces<N, L>(&W, pp, fbox, P);
+  w.culled += code & 255;
+  if (code & 256) ++w.rejected;
+  if (code & 65536) start_post(s, TK_FPOST, pp, ld3(W.pr[pp].hx));
 }
 
 // Begin a popped task.
@@ -378,43 +398,45 @@ __device__ __forceinline__ void commit_hit(const RoundParams& P, const PairSm& p
   if (p.fl & 8) b.flags |= HO_FLAG_FALLBACK;
 }
 
+// Fill a free slot with a pair of the batch and queue its first tasks.
+// Returns start_faces' code for pairs that go straight to the face search.
 template <int N, bool L>
-__device__ __forceinline__ void admit_pair(WarpSm<N>& W, const RoundParams& P, int slot, const RoundPair& rp, int elem,
-                                           bool has_field, const float* __restrict__ fbox, Work& w, LaneSolve& s) {
+__device__ __noinline__ int admit_pair(WarpSm<N>* Wp, const RoundParams* P, int slot, RoundPair rp, int elem,
+                                       bool has_field, const float* __restrict__ fbox) {
   constexpr int R = RoundCfg<N>::Ring;
+  WarpSm<N>& W = *Wp;
   PairSm& p = W.pr[slot];
-  const int64_t q = P.work[rp.item];
+  const int64_t q = P->work[rp.item];
   float3 o, d;
   int iso_idx;
-  query_ray_from(P.rays, P.n_rays, P.cam, q, o, d, iso_idx);
+  query_ray_from(P->rays, P->n_rays, P->cam, q, o, d, iso_idx);
   st3(p.o, o);
   st3(p.d, d);
   p.te = rp.te;
   p.tx = rp.tx;
-  p.iso = P.iso[iso_idx];
-  p.best_t = P.state[rp.item].best.t;
+  p.iso = P->iso[iso_idx];
+  p.best_t = P->state[rp.item].best.t;
   p.item = rp.item;
   p.elem = elem;
-  int fl = (has_field ? 1 : 0) | ((P.iso_on_mask >> iso_idx) & 1u ? 2 : 0);
-  if (L && rp.j >= 0 && rp.j < kPredK && P.cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == elem) {
-    const float* y = P.pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
+  int fl = (has_field ? 1 : 0) | ((P->iso_on_mask >> iso_idx) & 1u ? 2 : 0);
+  if (L && rp.j >= 0 && rp.j < kPredK && P->cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == elem) {
+    const float* y = P->pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
     p.pxi[0] = y[0]; p.pxi[1] = y[1]; p.pxi[2] = y[2];
     p.pv[0] = y[3]; p.pv[1] = y[4]; p.pv[2] = y[5];
-    p.pk = __ldg(P.desc + static_cast<int64_t>(elem) * kDescFloats + 45);
+    p.pk = __ldg(P->desc + static_cast<int64_t>(elem) * kDescFloats + 45);
     p.pte = rp.te;
     fl |= 4;
   }
   p.fl = fl;
   p.okm = 0u;
   p.its = 0;
-  ++w.cand;
   if ((fl & 3) == 3) {
     p.pend = kSamples;
     const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kSamples));
     for (int i = 0; i < kSamples; ++i) W.ring[(base + i) % R] = static_cast<uint16_t>(task_word(TK_SAMPLE, slot, i));
-  } else {
-    start_faces<N, L>(W, slot, fbox, w, s, P);
+    return 0;
   }
+  return start_faces<N, L>(Wp, slot, fbox, P);
 }
 
 template <int N, bool L>
@@ -487,9 +509,10 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             const int slot = __ffs(m) - 1;
             if (slot >= 0 && slot < B) {
               atomicAnd(&W.freem, ~(1u << slot));
-              LaneSolve scratch;
-              scratch.task = -1;
-              admit_pair<N, L>(W, P, slot, P.pairs[bt.first + adm + lane], bt.elem, has_field, fbox, w, scratch);
+              const int code = admit_pair<N, L>(&W, &P, slot, P.pairs[bt.first + adm + lane], bt.elem, has_field, fbox);
+              ++w.cand;
+              w.culled += code & 255;
+              if (code & 256) ++w.rejected;  // a face post at admission cannot happen: no face was searched
             } else {
               atomicOr(&P.stats->status, kStatusRoundGuard);
             }
@@ -709,13 +732,13 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
               s.pp = pp;
               start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f));
             } else {
-              start_faces<N, L>(W, pp, fbox, w, s, P);
+              face_phase<N, L>(W, pp, fbox, &P, w, s);
             }
           }
         } else if (s.kind == TK_REFINE) {
           if (p.rstage == 0) {  // midpoint solve ended
             if (end == 2) {
-              start_faces<N, L>(W, pp, fbox, w, s, P);  // the isosurface search failed
+              face_phase<N, L>(W, pp, fbox, &P, w, s);  // the isosurface search failed
             } else {
               p.msf = sf;
               p.msdf = sdf;
@@ -782,15 +805,15 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             }
           }
         } else if (s.kind == TK_FSEED) {
-          if (atomicSub(&p.pend, 1) == 1) finalize_faces<N, L>(W, pp, s, P);
+          if (atomicSub(&p.pend, 1) == 1 && finalize_faces<N>(&W, pp, &P)) start_post(s, TK_FPOST, pp, ld3(p.hx));
         } else if (s.kind == TK_FLEARN) {
           if (end == 1) {
             p.lf = s.arg;
             p.lt = s.t;
             st3(p.lx, s.xi);
           }
-          start_seeds<N, L>(W, pp, fbox, end == 1 ? s.t : p.best_t, w);
-          if (p.pend == 0) finalize_faces<N, L>(W, pp, s, P);
+          w.culled += start_seeds<N>(&W, pp, fbox, end == 1 ? s.t : p.best_t);
+          if (p.pend == 0 && finalize_faces<N>(&W, pp, &P)) start_post(s, TK_FPOST, pp, ld3(p.hx));
         } else if (s.kind == TK_FPOST) {
           // normal from the Jacobian columns (the face's two tangents)
           const float3 dr = make_float3(J[0], J[3], J[6]), ds = make_float3(J[1], J[4], J[7]),
@@ -803,14 +826,14 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
           n = normalize3(n);
           if (n.x * p.d[0] + n.y * p.d[1] + n.z * p.d[2] > 0.f) n = make_float3(-n.x, -n.y, -n.z);
           commit_hit(P, p, HO_HIT_FACE, p.hface, p.ht, xi, n, has_field ? u : 0.f);
-          pair_done<N>(W, pp, P);
+          pair_done<N>(W, pp, &P);
         } else if (s.kind == TK_IPOST) {
           if (p.ht > 0.001f && p.ht < p.best_t) {
             float3 n = normalize3(ld3(p.hg));
             if (n.x * p.d[0] + n.y * p.d[1] + n.z * p.d[2] > 0.f) n = make_float3(-n.x, -n.y, -n.z);
             commit_hit(P, p, HO_HIT_ISO, -1, p.ht, s.xi, n, u);
           }
-          pair_done<N>(W, pp, P);
+          pair_done<N>(W, pp, &P);
         }
       }
       __syncwarp();
