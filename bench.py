@@ -265,8 +265,13 @@ def run_gpu(args, rank, world):
     def step():
         ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
 
+    tuned = {}
+
     def timed(mode):
         ctx.set_mode(mode)
+        if mode != hr.MODE_PLAIN:  # the round kernel's element batch size, picked on this workload
+            tuned[{hr.MODE_BATCHED: "batched", hr.MODE_LEARNED: "learned"}[mode]] = ctx.autotune(
+                w.camera, w.isovalues, W, H)
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
                 flush.zero_()
@@ -351,6 +356,7 @@ def run_gpu(args, rank, world):
         "speedup_vs_batched": (value / mode_summary("batched")["value"]) if "batched" in results and head != "batched"
         else None,
         "training": train,
+        "autotune": tuned,
         "config": {"workload": w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes", "order": w.order_max,
                    "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
                    "rays": f"{W}x{H}", "isovalues": w.isovalues, "queries_per_step": nq,

@@ -126,6 +126,7 @@ typedef struct {
   uint64_t solve_steps;      /* loop steps of the round kernel's warps         */
   uint64_t lane_steps;       /* busy lanes summed over those steps: lane use
                                 = lane_steps / (32 * solve_steps)             */
+  uint64_t graph;            /* 1: the call's launches ran as one CUDA graph   */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */
@@ -217,6 +218,35 @@ int ho_intersect_device_noalloc(ho_context* ctx, int64_t n, const float* rays_de
  * HO_MODE_LEARNED needs a trained (ho_train_mlp) or loaded (ho_mlp_load)
  * network. */
 int ho_set_mode(ho_context* ctx, int mode);
+
+/* Options of the batched and learned engine (no reference counterpart).
+ * HO_OPT_GRAPH        1 (default): from the second call on, a call's launches
+ *                     run as one CUDA graph (patched in place between calls);
+ *                     0: direct launches.
+ * HO_OPT_ROUNDS       at most this many intersection rounds are enqueued
+ *                     before the completion check (default 16, 1..256): a call
+ *                     enqueues one more than the previous call needed; rays
+ *                     still in flight afterwards get further rounds, one
+ *                     read-back each.
+ * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
+ *                     default: the kernel's pair slots, 16 up to 7 modes per
+ *                     direction, 12 at 8, 8 at 9); ho_autotune picks it.
+ * HO_ERR_ARG for an unknown option, HO_ERR_RANGE for a value out of range. */
+#define HO_OPT_GRAPH 1
+#define HO_OPT_ROUNDS 2
+#define HO_OPT_ROUND_CHUNK 3
+int ho_set_option(ho_context* ctx, int option, int64_t value);
+int ho_get_option(ho_context* ctx, int option, int64_t* value);
+
+/* Autotuner of the batched / learned engine (no reference counterpart): times
+ * the given render (device buffers only, CUDA events on the context's stream,
+ * one warm-up and one timed call per candidate) for HO_AUTOTUNE_N element
+ * batch sizes (0.5, 1, 2, 4 and 8 times the kernel's pair slots), keeps the
+ * fastest as HO_OPT_ROUND_CHUNK and returns it in *chunk_out; ms_out (may be
+ * NULL) receives the candidates' times. Uses the current mode. */
+#define HO_AUTOTUNE_N 5
+int ho_autotune(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int width, int height,
+                int iso_zero_disables, int64_t* chunk_out, int64_t* candidates_out, float* ms_out);
 
 /* ---- learned mode (no reference counterpart) ------------------------------
  * Network 48 -> 128 -> 128 -> 128 -> 8 (GELU), BF16 weights, FP32

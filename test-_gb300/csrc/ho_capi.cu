@@ -125,8 +125,9 @@ int read_stats(ho_context* c) {
   for (int k = 0; k < 4; ++k) s.phase_cycles[k] = ds.c[ho::ST_CYC_TRAV + k];
   s.max_modes = c->N;
   s.status = ds.status;
-  s.rounds = c->last_rounds;
-  s.round_pairs = c->last_pairs;
+  s.rounds = ds.c[ho::ST_ROUNDS];
+  s.round_pairs = ds.c[ho::ST_PAIRS];
+  s.graph = c->last_graph ? 1u : 0u;
   s.solve_steps = ds.c[ho::ST_STEPS];
   s.lane_steps = ds.c[ho::ST_LANES];
   if (ds.status != 0)
@@ -179,6 +180,7 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->rounds.ecount);
     cudaFree(c->rounds.eoff);
     cudaFree(c->rounds.ctr);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     cudaFree(c->d_feat);
     cudaFree(c->d_pred);
     cudaFree(c->d_cand);
@@ -434,6 +436,82 @@ int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso
   rc = ho_intersect_device(c, n, c->d_rays, iso, iso_enabled, c->d_hits, c->stream);
   if (rc) return rc;
   if (n > 0) CK(cudaMemcpyAsync(out, c->d_hits, n * sizeof(ho_hit), cudaMemcpyDeviceToHost, c->stream), "read hits");
+  return read_stats(c);
+}
+
+int ho_set_option(ho_context* c, int option, int64_t value) {
+  if (!c) return HO_ERR_ARG;
+  switch (option) {
+    case HO_OPT_GRAPH:
+      if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_GRAPH takes 0 or 1");
+      c->use_graph = value == 1;
+      return HO_OK;
+    case HO_OPT_ROUNDS:
+      if (value < 1 || value > 256) return fail(c, HO_ERR_RANGE, "HO_OPT_ROUNDS must be in [1, 256]");
+      c->round_count = static_cast<int>(value);
+      return HO_OK;
+    case HO_OPT_ROUND_CHUNK:
+      if (value < 1 || value > 4096) return fail(c, HO_ERR_RANGE, "HO_OPT_ROUND_CHUNK must be in [1, 4096]");
+      c->round_chunk = static_cast<int>(value);
+      return HO_OK;
+    default:
+      return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
+  }
+}
+
+int ho_get_option(ho_context* c, int option, int64_t* value) {
+  if (!c || !value) return HO_ERR_ARG;
+  switch (option) {
+    case HO_OPT_GRAPH: *value = c->use_graph ? 1 : 0; return HO_OK;
+    case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
+    case HO_OPT_ROUND_CHUNK: *value = c->round_chunk > 0 ? c->round_chunk : ho::round_slots(c->N > 0 ? c->N : 2); return HO_OK;
+    default: return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
+  }
+}
+
+int ho_autotune(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int iso_zero_disables,
+                int64_t* chunk_out, int64_t* candidates_out, float* ms_out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (!cam || !chunk_out) return fail(c, HO_ERR_ARG, "null argument");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (W <= 0 || H <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
+  const size_t nq = static_cast<size_t>(W) * H * n_iso;
+  if ((rc = ensure_buf(c, c->d_rgb, c->rgb_cap, nq * 3, "cudaMalloc(rgb)"))) return rc;
+  const int slots = ho::round_slots(c->N);
+  const int64_t cand[HO_AUTOTUNE_N] = {slots / 2, slots, 2 * slots, 4 * slots, 8 * slots};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  CK(cudaEventCreate(&ev0), "cudaEventCreate");
+  CK(cudaEventCreate(&ev1), "cudaEventCreate");
+  const int keep = c->round_chunk;
+  float best_ms = 0.f;
+  int64_t best = keep;
+  for (int k = 0; k < HO_AUTOTUNE_N && rc == HO_OK; ++k) {
+    c->round_chunk = static_cast<int>(cand[k]);
+    float ms = 0.f;
+    for (int rep = 0; rep < 2 && rc == HO_OK; ++rep) {
+      if (rep == 1 && cudaEventRecord(ev0, c->stream) != cudaSuccess) rc = fail(c, HO_ERR_CUDA, "event record");
+      if (rc == HO_OK) rc = ho_render_device(c, cam, iso, n_iso, W, H, iso_zero_disables, c->d_rgb, nullptr, c->stream);
+      if (rc == HO_OK && rep == 1) {
+        if (cudaEventRecord(ev1, c->stream) != cudaSuccess || cudaEventSynchronize(ev1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess)
+          rc = fail(c, HO_ERR_CUDA, "event timing");
+      }
+    }
+    if (rc != HO_OK) break;
+    if (ms_out) ms_out[k] = ms;
+    if (candidates_out) candidates_out[k] = cand[k];
+    if (k == 0 || ms < best_ms) {
+      best_ms = ms;
+      best = cand[k];
+    }
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  c->round_chunk = rc == HO_OK ? static_cast<int>(best) : keep;
+  if (rc != HO_OK) return rc;
+  *chunk_out = best;
   return read_stats(c);
 }
 

@@ -136,7 +136,14 @@ struct ho_context {
   size_t work_cap = 0;
   unsigned* d_qctr = nullptr;     // [0] queue length, [1] next item
   ho::RoundBufs rounds;
-  uint64_t last_rounds = 0, last_pairs = 0;
+  // batched / learned engine options (ho_set_option)
+  int round_chunk = 0;       // pairs per element batch (0: the kernel's pair slots)
+  int round_count = 16;      // rounds enqueued before the completion check (at most)
+  int rounds_needed = 0;     // non-empty rounds of the previous batched / learned call
+  bool use_graph = true;     // run a call's launches as one CUDA graph
+  bool graph_warm = false;   // the first call of a context runs direct
+  cudaGraphExec_t graph_exec = nullptr;
+  bool last_graph = false;
   void* h_pinned = nullptr;
   size_t pinned_cap = 0;
 };

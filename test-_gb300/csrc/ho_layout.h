@@ -53,6 +53,8 @@ enum StatSlot {
   ST_CYC_FACE,
   ST_STEPS,
   ST_LANES,
+  ST_ROUNDS,
+  ST_PAIRS,
   ST_COUNT
 };
 
@@ -71,6 +73,10 @@ constexpr int kFaceBoxFloats = 36;
 
 // Largest supported modes per direction (P = 8).
 constexpr int kMaxModes = 9;
+// Pair slots per warp of the round kernel: the per-warp shared memory (element
+// record, pair slots, task queue) is sized so that three 4-warp blocks fit on
+// an SM up to N = 8 (two at N = 9, whose record alone is 15.5 KB).
+constexpr int round_slots(int n) { return n <= 7 ? 16 : (n == 8 ? 12 : 8); }
 constexpr int kMinModes = 2;
 
 // Element record layout: x, y, z geometry blocks then the field block; in a

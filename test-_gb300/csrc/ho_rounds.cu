@@ -13,9 +13,10 @@ namespace ho {
 
 __global__ void __launch_bounds__(1024) scan_kernel(uint32_t* __restrict__ data, int64_t len);
 
-__global__ void round_init_kernel(RayState* __restrict__ st, const uint8_t* __restrict__ kovf, unsigned n_items) {
+__global__ void round_init_kernel(RayState* __restrict__ st, const uint8_t* __restrict__ kovf,
+                                  const unsigned* __restrict__ qcount) {
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_items) return;
+  if (i >= *qcount) return;
   RayState r;
   r.best = miss_state();
   r.cursor = 0;
@@ -34,12 +35,11 @@ __global__ void round_init_kernel(RayState* __restrict__ st, const uint8_t* __re
 // reference's traversal, FEM-AABB/raytracer.cu:117-356, in ascending
 // (entry t, element) order). A ray whose list was cut at kCandK walks the
 // tree again for the candidates after the last visited one.
-__global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, unsigned n_items,
-                                    RoundPair* __restrict__ pairs, int32_t* __restrict__ pelem,
-                                    uint32_t* __restrict__ prank, uint32_t* __restrict__ ecount,
-                                    unsigned* __restrict__ ctr) {
+__global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, RoundPair* __restrict__ pairs,
+                                    int32_t* __restrict__ pelem, uint32_t* __restrict__ prank,
+                                    uint32_t* __restrict__ ecount, unsigned* __restrict__ ctr) {
   const unsigned item = blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= n_items) return;
+  if (item >= *P.qcount) return;
   RayState& r = st[item];
   if (r.done) return;
   float3 o, d;
@@ -101,10 +101,17 @@ __global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, un
   }
 }
 
+// Also tallies the round (non-empty rounds and pairs) into the work counters.
 __global__ void round_scatter_kernel(const RoundPair* __restrict__ pairs, const int32_t* __restrict__ pelem,
                                      const uint32_t* __restrict__ prank, const uint32_t* __restrict__ eoff,
-                                     unsigned n_pairs, RoundPair* __restrict__ sorted) {
+                                     const unsigned* __restrict__ ctr, RoundPair* __restrict__ sorted,
+                                     DevStats* stats) {
   const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned n_pairs = *ctr;
+  if (k == 0 && n_pairs > 0) {
+    atomicAdd(&stats->c[ST_ROUNDS], 1ull);
+    atomicAdd(&stats->c[ST_PAIRS], static_cast<unsigned long long>(n_pairs));
+  }
   if (k >= n_pairs) return;
   sorted[eoff[pelem[k]] + prank[k]] = pairs[k];
 }
@@ -129,9 +136,9 @@ __global__ void round_batch_kernel(const uint32_t* __restrict__ ecount, const ui
   }
 }
 
-__global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ st, unsigned n_items) {
+__global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ st) {
   const unsigned item = blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= n_items) return;
+  if (item >= *P.qcount) return;
   const int64_t q = P.work[item];
   float3 o, d;
   int iso_idx;
@@ -161,31 +168,25 @@ static cudaError_t grow(T*& p, size_t& cap, size_t want, size_t size) {
     if (e_ != cudaSuccess) return int(e_); \
   } while (0)
 
-int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned) {
-  unsigned n_items = 0;
-  RT_TRY(cudaMemcpyAsync(&n_items, P.qcount, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-  RT_TRY(cudaStreamSynchronize(s));
-  c->last_rounds = 0;
-  c->last_pairs = 0;
-  if (n_items == 0) return 0;
+// Scratch for up to n_cap queued rays (all queries of the call), allocated
+// before any stream capture.
+int prepare_rounds(ho_context* c, int64_t n_cap) {
+  const size_t n = static_cast<size_t>(std::max<int64_t>(n_cap, 1));
   const int64_t n_elem = c->n_elem;
   RoundBufs& rb = c->rounds;
-  RT_TRY(grow(rb.state, rb.state_cap, n_items, sizeof(RayState)));
-  RT_TRY(grow(rb.pairs, rb.pairs_cap, 2 * static_cast<size_t>(n_items), sizeof(RoundPair)));
-  RT_TRY(grow(rb.pelem, rb.pelem_cap, n_items, sizeof(int32_t)));
-  RT_TRY(grow(rb.prank, rb.prank_cap, n_items, sizeof(uint32_t)));
-  RT_TRY(grow(rb.batches, rb.batches_cap, n_items, sizeof(RoundBatch)));
+  RT_TRY(grow(rb.state, rb.state_cap, n, sizeof(RayState)));
+  RT_TRY(grow(rb.pairs, rb.pairs_cap, 2 * n, sizeof(RoundPair)));
+  RT_TRY(grow(rb.pelem, rb.pelem_cap, n, sizeof(int32_t)));
+  RT_TRY(grow(rb.prank, rb.prank_cap, n, sizeof(uint32_t)));
+  RT_TRY(grow(rb.batches, rb.batches_cap, n, sizeof(RoundBatch)));
   RT_TRY(grow(rb.ecount, rb.ecount_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
   RT_TRY(grow(rb.eoff, rb.eoff_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
   RT_TRY(grow(rb.ctr, rb.ctr_cap, 4, sizeof(unsigned)));
-  RayState* st = static_cast<RayState*>(rb.state);
-  RoundPair* gathered = static_cast<RoundPair*>(rb.pairs);
-  RoundPair* sorted = gathered + n_items;
-  RoundBatch* batches = static_cast<RoundBatch*>(rb.batches);
-  const unsigned gi = (n_items + 255) / 256;
-  round_init_kernel<<<gi, 256, 0, s>>>(st, P.kovf, n_items);
-  RT_TRY(cudaGetLastError());
+  return 0;
+}
 
+static RoundParams round_params(ho_context* c, const TraceParams& P) {
+  RoundBufs& rb = c->rounds;
   RoundParams R;
   R.rec = P.rec;
   R.fbox = P.fbox;
@@ -196,51 +197,91 @@ int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned
   for (int i = 0; i < 8; ++i) R.iso[i] = P.iso[i];
   R.iso_on_mask = P.iso_on_mask;
   R.work = P.work;
-  R.state = st;
-  R.pairs = sorted;
-  R.batches = batches;
+  R.state = static_cast<RayState*>(rb.state);
+  R.pairs = static_cast<RoundPair*>(rb.pairs) + rb.pairs_cap / 2;
+  R.batches = static_cast<RoundBatch*>(rb.batches);
   R.n_batches = rb.ctr + 1;
   R.next_batch = rb.ctr + 2;
   R.stats = P.stats;
   R.desc = P.desc;
   R.cand_e = P.cand_e;
   R.pred = P.pred;
-  const int B = kRoundChunk;
-  for (int round = 0; round < 100000; ++round) {
-    RT_TRY(cudaMemsetAsync(rb.ecount, 0, static_cast<size_t>(n_elem) * sizeof(uint32_t), s));
-    RT_TRY(cudaMemsetAsync(rb.ctr, 0, 4 * sizeof(unsigned), s));
-    round_gather_kernel<<<gi, 256, 0, s>>>(P, st, n_items, gathered, rb.pelem, rb.prank, rb.ecount, rb.ctr);
-    RT_TRY(cudaGetLastError());
-    unsigned n_pairs = 0;
-    RT_TRY(cudaMemcpyAsync(&n_pairs, rb.ctr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-    RT_TRY(cudaStreamSynchronize(s));
-    if (n_pairs == 0) break;
-    ++c->last_rounds;
-    c->last_pairs += n_pairs;
-    RT_TRY(cudaMemcpyAsync(rb.eoff, rb.ecount, static_cast<size_t>(n_elem) * sizeof(uint32_t),
-                           cudaMemcpyDeviceToDevice, s));
-    scan_kernel<<<1, 1024, 0, s>>>(rb.eoff, n_elem);
-    round_scatter_kernel<<<(n_pairs + 255) / 256, 256, 0, s>>>(gathered, rb.pelem, rb.prank, rb.eoff, n_pairs,
-                                                                 sorted);
-    round_batch_kernel<<<static_cast<unsigned>((n_elem + 255) / 256), 256, 0, s>>>(rb.ecount, rb.eoff, n_elem, B,
-                                                                                   batches, rb.ctr + 1);
-    RT_TRY(cudaGetLastError());
-    cudaError_t e;
-    switch (c->N) {
-      case 2: e = launch_round_n<2>(R, s, learned); break;
-      case 3: e = launch_round_n<3>(R, s, learned); break;
-      case 4: e = launch_round_n<4>(R, s, learned); break;
-      case 5: e = launch_round_n<5>(R, s, learned); break;
-      case 6: e = launch_round_n<6>(R, s, learned); break;
-      case 7: e = launch_round_n<7>(R, s, learned); break;
-      case 8: e = launch_round_n<8>(R, s, learned); break;
-      case 9: e = launch_round_n<9>(R, s, learned); break;
-      default: e = cudaErrorInvalidValue; break;
-    }
-    RT_TRY(e);
-  }
-  round_finish_kernel<<<gi, 256, 0, s>>>(P, st, n_items);
+  return R;
+}
+
+// One round: gather each ray's next pair, bucket by element, intersect. Every
+// launch has a fixed size and reads its counts on the device, so rounds can
+// be enqueued (and captured) without reading anything back.
+static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams& R, cudaStream_t s, bool learned,
+                         int64_t n_cap) {
+  RoundBufs& rb = c->rounds;
+  const int64_t n_elem = c->n_elem;
+  RoundPair* gathered = static_cast<RoundPair*>(rb.pairs);
+  const unsigned gi = static_cast<unsigned>((n_cap + 255) / 256);
+  RT_TRY(cudaMemsetAsync(rb.ecount, 0, static_cast<size_t>(n_elem) * sizeof(uint32_t), s));
+  RT_TRY(cudaMemsetAsync(rb.ctr, 0, 4 * sizeof(unsigned), s));
+  round_gather_kernel<<<gi, 256, 0, s>>>(P, R.state, gathered, rb.pelem, rb.prank, rb.ecount, rb.ctr);
+  RT_TRY(cudaMemcpyAsync(rb.eoff, rb.ecount, static_cast<size_t>(n_elem) * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                         s));
+  scan_kernel<<<1, 1024, 0, s>>>(rb.eoff, n_elem);
+  round_scatter_kernel<<<gi, 256, 0, s>>>(gathered, rb.pelem, rb.prank, rb.eoff, rb.ctr,
+                                          const_cast<RoundPair*>(R.pairs), P.stats);
+  round_batch_kernel<<<static_cast<unsigned>((n_elem + 255) / 256), 256, 0, s>>>(
+      rb.ecount, rb.eoff, n_elem, c->round_chunk > 0 ? c->round_chunk : round_slots(c->N),
+      const_cast<RoundBatch*>(R.batches), rb.ctr + 1);
   RT_TRY(cudaGetLastError());
+  cudaError_t e;
+  switch (c->N) {
+    case 2: e = launch_round_n<2>(R, s, learned); break;
+    case 3: e = launch_round_n<3>(R, s, learned); break;
+    case 4: e = launch_round_n<4>(R, s, learned); break;
+    case 5: e = launch_round_n<5>(R, s, learned); break;
+    case 6: e = launch_round_n<6>(R, s, learned); break;
+    case 7: e = launch_round_n<7>(R, s, learned); break;
+    case 8: e = launch_round_n<8>(R, s, learned); break;
+    case 9: e = launch_round_n<9>(R, s, learned); break;
+    default: e = cudaErrorInvalidValue; break;
+  }
+  RT_TRY(e);
+  return 0;
+}
+
+// The state init, `rounds` rounds and the final write-out of the queued rays.
+int enqueue_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned, int64_t n_cap, int rounds) {
+  const RoundParams R = round_params(c, P);
+  const unsigned gi = static_cast<unsigned>((n_cap + 255) / 256);
+  round_init_kernel<<<gi, 256, 0, s>>>(R.state, P.kovf, P.qcount);
+  RT_TRY(cudaGetLastError());
+  for (int r = 0; r < rounds; ++r) {
+    const int rc = enqueue_round(c, P, R, s, learned, n_cap);
+    if (rc) return rc;
+  }
+  round_finish_kernel<<<gi, 256, 0, s>>>(P, R.state);
+  RT_TRY(cudaGetLastError());
+  return 0;
+}
+
+// After the enqueued rounds ran: while the last round still found pairs, run
+// one more round (with a read-back each), then write the results again.
+int finish_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned, int64_t n_cap) {
+  const RoundParams R = round_params(c, P);
+  bool extra = false;
+  for (int guard = 0; guard < 100000; ++guard) {
+    unsigned last = 0;
+    unsigned long long rounds = 0;
+    RT_TRY(cudaMemcpyAsync(&last, c->rounds.ctr, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    RT_TRY(cudaMemcpyAsync(&rounds, &P.stats->c[ST_ROUNDS], sizeof(rounds), cudaMemcpyDeviceToHost, s));
+    RT_TRY(cudaStreamSynchronize(s));
+    c->rounds_needed = static_cast<int>(rounds);
+    if (last == 0) break;
+    extra = true;
+    const int rc = enqueue_round(c, P, R, s, learned, n_cap);
+    if (rc) return rc;
+  }
+  if (extra) {
+    round_finish_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P, R.state);
+    RT_TRY(cudaGetLastError());
+  }
   return 0;
 }
 

@@ -40,13 +40,10 @@ namespace ho {
 constexpr int kRoundBlock = 128;  // 4 warps, one batch each
 constexpr int kSamples = 17;
 
-// Pair slots per warp: the per-warp shared memory (element record, pair
-// slots, task queue) is sized so that three 4-warp blocks fit on an SM up to
-// N = 8 (two at N = 9, whose record alone is 15.5 KB).
-constexpr int round_slots(int n) { return n <= 7 ? 16 : (n == 8 ? 12 : 8); }
-// Pairs per batch: a warp admits a batch's pairs into its slots as earlier
-// pairs finish, so a batch may be several times the slot count.
-constexpr int kRoundChunk = 64;
+// Pairs per batch (HO_OPT_ROUND_CHUNK, default the slot count): a warp admits
+// a batch's pairs into its slots as earlier pairs finish, so a batch may be
+// several times the slot count; smaller batches spread an element's pairs
+// over more warps, which evens out the end of a round.
 
 template <int N>
 struct RoundCfg {

@@ -1,6 +1,8 @@
 // Dispatch of the trace kernel by modes per direction; each instantiation
 // lives in its own translation unit (ho_trace_n*.cu) so they compile in
 // parallel.
+#include <algorithm>
+
 #include "ho_trace.cuh"
 
 namespace ho {
@@ -76,11 +78,33 @@ __global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16*
   }
 }
 
-int run_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned);
+int prepare_rounds(ho_context* c, int64_t n_cap);
+int enqueue_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned, int64_t n_cap, int rounds);
+int finish_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned, int64_t n_cap);
+
+// Everything of a batched / learned call that runs on the stream: the
+// classify pass, the network (learned), the rounds and the write-out. No host
+// read-back and no allocation, so the whole sequence can be captured.
+static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool learned, int64_t n_queries, int sms) {
+  cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 2 * sizeof(unsigned), s);
+  if (e != cudaSuccess) return int(e);
+  classify_kernel<<<static_cast<unsigned>((n_queries + 255) / 256), 256, 0, s>>>(P, n_queries);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return int(e);
+  if (learned) {
+    cand_kernel<<<sms * 8, 128, 0, s>>>(P, static_cast<__nv_bfloat16*>(c->d_feat), c->d_cand);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return int(e);
+    const int rc = mlp_infer(c->mlp.dev(), c->d_feat, 0, c->d_qctr, kPredK, c->d_pred, s, sms);
+    if (rc) return rc;
+  }
+  // as many rounds as the previous call needed, plus one, within the option
+  const int rounds = c->rounds_needed > 0 ? std::min(c->round_count, c->rounds_needed + 1) : c->round_count;
+  return enqueue_rounds(c, P, s, learned, n_queries, rounds);
+}
 
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
-  c->last_rounds = 0;
-  c->last_pairs = 0;
+  c->last_graph = false;
   TraceParams P;
   P.nodes = c->d_nodes;
   P.rec = c->d_rec;
@@ -156,15 +180,8 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   P.qnext = c->d_qctr + 1;
   P.kbuf = c->d_kbuf;
   P.kovf = c->d_kovf;
-  classify_kernel<<<static_cast<unsigned>((n_queries + 255) / 256), 256, 0, s>>>(P, n_queries);
-  {
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return int(e);
-  }
   const bool learned = mode == HO_MODE_LEARNED;
-  P.desc = c->d_desc;
-  P.cand_e = nullptr;
-  P.pred = nullptr;
+  // allocate first: nothing enqueued below may allocate (it may be captured)
   if (learned) {
     const size_t rows = static_cast<size_t>(n_queries) * kPredK;
     if (rows > c->pred_cap) {
@@ -181,19 +198,57 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
       if (e != cudaSuccess) return int(e);
       c->pred_cap = rows;
     }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cand_kernel<<<sms * 8, 128, 0, s>>>(P, static_cast<__nv_bfloat16*>(c->d_feat), c->d_cand);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return int(e);
-    const int rc = mlp_infer(c->mlp.dev(), c->d_feat, 0, c->d_qctr, kPredK, c->d_pred, s, sms);
-    if (rc) return rc;
-    P.cand_e = c->d_cand;
-    P.pred = c->d_pred;
   }
-  // element-major rounds over the queued rays
-  return run_rounds(c, P, s, learned);
+  {
+    const int rc = prepare_rounds(c, n_queries);
+    if (rc) return rc;
+  }
+  P.desc = c->d_desc;
+  P.cand_e = learned ? c->d_cand : nullptr;
+  P.pred = learned ? c->d_pred : nullptr;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+
+  // The first call of a context runs its launches directly (first-use set-up
+  // of kernel attributes happens there); later calls are captured into one
+  // CUDA graph, whose executable is patched in place while the launch
+  // sequence keeps its shape.
+  bool capture = c->use_graph && c->graph_warm;
+  if (capture && cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGetLastError();
+    capture = false;
+  }
+  int rc = enqueue_batched(c, P, s, learned, n_queries, sms);
+  if (capture) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc == 0 && e != cudaSuccess) rc = int(e);
+    if (rc == 0 && c->graph_exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(c->graph_exec, g, &info) != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(c->graph_exec);
+        c->graph_exec = nullptr;
+      }
+    }
+    if (rc == 0 && !c->graph_exec) {
+      e = cudaGraphInstantiate(&c->graph_exec, g, 0);
+      if (e != cudaSuccess) {
+        c->graph_exec = nullptr;
+        rc = int(e);
+      }
+    }
+    if (g) cudaGraphDestroy(g);
+    if (rc == 0) {
+      e = cudaGraphLaunch(c->graph_exec, s);
+      if (e != cudaSuccess) rc = int(e);
+      c->last_graph = rc == 0;
+    }
+  }
+  if (rc) return rc;
+  c->graph_warm = true;
+  return finish_rounds(c, P, s, learned, n_queries);
 }
 
 }  // namespace ho

@@ -23,6 +23,7 @@ HO_OK = 0
 ERRORS = {-1: "HO_ERR_ARG", -2: "HO_ERR_CUDA", -3: "HO_ERR_STATE", -4: "HO_ERR_IO", -5: "HO_ERR_PARSE",
           -6: "HO_ERR_NOMEM", -7: "HO_ERR_RANGE", -8: "HO_ERR_DEVICE"}
 MODE_PLAIN, MODE_LEARNED, MODE_BATCHED = 0, 1, 2
+OPT_GRAPH, OPT_ROUNDS, OPT_ROUND_CHUNK = 1, 2, 3
 MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
@@ -61,7 +62,7 @@ class _Stats(C.Structure):
                                           "mlp_accepted", "mlp_rejected", "restarts")] + [
         ("max_modes", C.c_int32), ("status", C.c_int32), ("phase_cycles", C.c_uint64 * 4),
         ("rounds", C.c_uint64), ("round_pairs", C.c_uint64), ("solve_steps", C.c_uint64),
-        ("lane_steps", C.c_uint64)]
+        ("lane_steps", C.c_uint64), ("graph", C.c_uint64)]
 
 
 def _load():
@@ -87,6 +88,9 @@ def _load():
     L.ho_intersect.argtypes = [vp, i64, vp, f32, i32, vp]
     L.ho_intersect_device.argtypes = [vp, i64, vp, f32, i32, vp, vp]
     L.ho_set_mode.argtypes = [vp, i32]
+    L.ho_set_option.argtypes = [vp, i32, i64]
+    L.ho_get_option.argtypes = [vp, i32, C.POINTER(C.c_int64)]
+    L.ho_autotune.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, C.POINTER(C.c_int64), vp, vp]
     L.ho_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.ho_save_ppm.argtypes = [vp, i32, i32, C.c_char_p]
     L.ho_measure_fp32_peak.argtypes = [i32, C.POINTER(C.c_double)]
@@ -242,6 +246,25 @@ class Context:
 
     def set_mode(self, mode: int):
         self._ck(lib.ho_set_mode(self.h, int(mode)))
+
+    def set_option(self, option: int, value: int):
+        self._ck(lib.ho_set_option(self.h, int(option), int(value)))
+
+    def autotune(self, cam: "Camera", isovalues, width: int, height: int, iso_zero_disables: bool = False) -> dict:
+        """Pick the element batch size of the round kernel for this render
+        (ho_autotune); returns the chosen size and every candidate's time."""
+        iso = np.ascontiguousarray(isovalues, dtype=np.float32)
+        chunk = C.c_int64()
+        cand = np.zeros(5, np.int64)
+        ms = np.zeros(5, np.float32)
+        self._ck(lib.ho_autotune(self.h, C.byref(cam._c()), _p(iso), iso.size, int(width), int(height),
+                                 int(bool(iso_zero_disables)), C.byref(chunk), _p(cand), _p(ms)))
+        return {"chunk": chunk.value, "candidates": cand.tolist(), "ms": ms.tolist()}
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int64()
+        self._ck(lib.ho_get_option(self.h, int(option), C.byref(v)))
+        return v.value
 
     # ---- queries ---------------------------------------------------------------
     def render(self, camera: Camera, isovalues, width: int, height: int, iso_zero_disables: bool = True,

@@ -98,3 +98,24 @@ def test_save_ppm(tmp_path):
     assert data.startswith(b"P6\n3 4\n255\n") and data.endswith(rgb.tobytes())
     with pytest.raises(hr.HoError):
         hr.save_ppm(rgb, str(tmp_path / "no" / "such" / "dir.ppm"))
+
+
+def test_engine_options():
+    with hr.Context(0) as ctx:
+        assert ctx.get_option(hr.OPT_GRAPH) == 1
+        assert ctx.get_option(hr.OPT_ROUNDS) == 16
+        assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 16
+        ctx.set_option(hr.OPT_GRAPH, 0)
+        ctx.set_option(hr.OPT_ROUNDS, 3)
+        ctx.set_option(hr.OPT_ROUND_CHUNK, 200)
+        assert (ctx.get_option(hr.OPT_GRAPH), ctx.get_option(hr.OPT_ROUNDS), ctx.get_option(hr.OPT_ROUND_CHUNK)) == (
+            0, 3, 200)
+        for opt, bad in ((hr.OPT_GRAPH, 2), (hr.OPT_ROUNDS, 0), (hr.OPT_ROUNDS, 257), (hr.OPT_ROUND_CHUNK, 0),
+                         (hr.OPT_ROUND_CHUNK, 4097)):
+            with pytest.raises(hr.HoError) as ei:
+                ctx.set_option(opt, bad)
+            assert ei.value.code == -7
+        with pytest.raises(hr.HoError) as ei:
+            ctx.set_option(99, 1)
+        assert ei.value.code == -1
+        assert ctx.get_option(hr.OPT_ROUNDS) == 3  # a refused value leaves the option unchanged

@@ -90,3 +90,48 @@ def test_intersect_explicit_rays_matches_render(small):
     h1 = hits[0].reshape(-1)
     same = classify(h1, h2)
     assert same.mean() > 0.999
+
+
+def test_graph_rounds_and_chunks_give_the_same_hits(small):
+    """The same render as a CUDA graph, as direct launches, with one round per
+    launch (every further round through the completion check) and with small
+    element batches: identical hits, identical work."""
+    ctx, w, arrs, osc = small
+    W = H = 64
+    ctx.set_mode(hr.MODE_BATCHED)
+
+    def run():
+        _, h = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+        return h[0].reshape(-1).copy(), ctx.stats()
+
+    ctx.set_option(hr.OPT_GRAPH, 0)
+    h0, s0 = run()
+    assert s0["graph"] == 0 and s0["rounds"] > 1 and s0["round_pairs"] == s0["candidates"]
+    ctx.set_option(hr.OPT_GRAPH, 1)
+    run()
+    h1, s1 = run()
+    assert s1["graph"] == 1
+    ctx.set_option(hr.OPT_ROUNDS, 1)
+    h2, s2 = run()
+    ctx.set_option(hr.OPT_ROUNDS, 16)
+    ctx.set_option(hr.OPT_ROUND_CHUNK, 5)
+    h3, s3 = run()
+    ctx.set_option(hr.OPT_ROUND_CHUNK, 16)
+    for h, s in ((h1, s1), (h2, s2), (h3, s3)):
+        assert np.array_equal(h["kind"], h0["kind"]) and np.array_equal(h["elem"], h0["elem"])
+        assert np.array_equal(h["face"], h0["face"]) and np.array_equal(h["t"], h0["t"])
+        assert (s["rounds"], s["round_pairs"], s["newton_iters"], s["face_iters"]) == (
+            s0["rounds"], s0["round_pairs"], s0["newton_iters"], s0["face_iters"])
+
+
+def test_autotune_picks_a_candidate_and_keeps_results(small):
+    ctx, w, arrs, osc = small
+    W = H = 64
+    ctx.set_mode(hr.MODE_BATCHED)
+    _, h0 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    r = ctx.autotune(w.camera, w.isovalues, W, H)
+    assert r["chunk"] in r["candidates"] and all(m > 0 for m in r["ms"])
+    assert ctx.get_option(hr.OPT_ROUND_CHUNK) == r["chunk"]
+    _, h1 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    assert np.array_equal(h0["elem"], h1["elem"]) and np.array_equal(h0["t"], h1["t"])
+    ctx.set_option(hr.OPT_ROUND_CHUNK, 16)
