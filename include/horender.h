@@ -127,6 +127,10 @@ typedef struct {
   uint64_t lane_steps;       /* busy lanes summed over those steps: lane use
                                 = lane_steps / (32 * solve_steps)             */
   uint64_t graph;            /* 1: the call's launches ran as one CUDA graph   */
+  uint64_t fp64_checked;     /* batched/learned: hits re-evaluated in FP64     */
+  uint64_t fp64_failed;      /* of those, failed (traced again, plain solver) */
+  uint64_t fp64_failed_after_fallback;  /* plain answer failed too (kept,
+                                HO_FLAG_FP64_FAIL)                           */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */
@@ -228,6 +232,11 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     enqueues one more than the previous call needed; rays
  *                     still in flight afterwards get further rounds, one
  *                     read-back each.
+ * HO_OPT_FP64_CHECK   1 (default): every hit of a batched / learned call is
+ *                     re-evaluated in FP64 (position residual, and field
+ *                     residual for isosurface hits); a failing hit is traced
+ *                     again by the plain solver (HO_FLAG_FALLBACK), and is
+ *                     flagged HO_FLAG_FP64_FAIL if that fails too; 0: off.
  * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
  *                     default: the kernel's pair slots, 16 up to 7 modes per
  *                     direction, 12 at 8, 8 at 9); ho_autotune picks it.
@@ -235,6 +244,7 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_GRAPH 1
 #define HO_OPT_ROUNDS 2
 #define HO_OPT_ROUND_CHUNK 3
+#define HO_OPT_FP64_CHECK 4
 int ho_set_option(ho_context* ctx, int option, int64_t value);
 int ho_get_option(ho_context* ctx, int option, int64_t* value);
 

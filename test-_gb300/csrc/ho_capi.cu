@@ -128,6 +128,9 @@ int read_stats(ho_context* c) {
   s.rounds = ds.c[ho::ST_ROUNDS];
   s.round_pairs = ds.c[ho::ST_PAIRS];
   s.graph = c->last_graph ? 1u : 0u;
+  s.fp64_checked = ds.c[ho::ST_CHECKED];
+  s.fp64_failed = ds.c[ho::ST_CHECK_FAIL];
+  s.fp64_failed_after_fallback = ds.c[ho::ST_CHECK_FINAL];
   s.solve_steps = ds.c[ho::ST_STEPS];
   s.lane_steps = ds.c[ho::ST_LANES];
   if (ds.status != 0)
@@ -180,6 +183,7 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->rounds.ecount);
     cudaFree(c->rounds.eoff);
     cudaFree(c->rounds.ctr);
+    cudaFree(c->rounds.fail);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     cudaFree(c->d_feat);
     cudaFree(c->d_pred);
@@ -454,6 +458,10 @@ int ho_set_option(ho_context* c, int option, int64_t value) {
       if (value < 1 || value > 4096) return fail(c, HO_ERR_RANGE, "HO_OPT_ROUND_CHUNK must be in [1, 4096]");
       c->round_chunk = static_cast<int>(value);
       return HO_OK;
+    case HO_OPT_FP64_CHECK:
+      if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_FP64_CHECK takes 0 or 1");
+      c->fp64_check = value == 1;
+      return HO_OK;
     default:
       return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
@@ -463,6 +471,7 @@ int ho_get_option(ho_context* c, int option, int64_t* value) {
   if (!c || !value) return HO_ERR_ARG;
   switch (option) {
     case HO_OPT_GRAPH: *value = c->use_graph ? 1 : 0; return HO_OK;
+    case HO_OPT_FP64_CHECK: *value = c->fp64_check ? 1 : 0; return HO_OK;
     case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
     case HO_OPT_ROUND_CHUNK: *value = c->round_chunk > 0 ? c->round_chunk : ho::round_slots(c->N > 0 ? c->N : 2); return HO_OK;
     default: return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));

@@ -85,8 +85,10 @@ struct RoundBufs {
   size_t ecount_cap = 0;
   uint32_t* eoff = nullptr;
   size_t eoff_cap = 0;
-  unsigned* ctr = nullptr;   // pairs, batches, next batch
+  unsigned* ctr = nullptr;   // pairs, batches, next batch, failed FP64 checks
   size_t ctr_cap = 0;
+  uint32_t* fail = nullptr;  // queue items whose hit failed the FP64 check
+  size_t fail_cap = 0;
 };
 }  // namespace ho
 
@@ -141,6 +143,7 @@ struct ho_context {
   int round_count = 16;      // rounds enqueued before the completion check (at most)
   int rounds_needed = 0;     // non-empty rounds of the previous batched / learned call
   bool use_graph = true;     // run a call's launches as one CUDA graph
+  bool fp64_check = true;    // FP64 residual check + plain fallback of the hits
   bool graph_warm = false;   // the first call of a context runs direct
   cudaGraphExec_t graph_exec = nullptr;
   bool last_graph = false;

@@ -55,6 +55,9 @@ enum StatSlot {
   ST_LANES,
   ST_ROUNDS,
   ST_PAIRS,
+  ST_CHECKED,
+  ST_CHECK_FAIL,
+  ST_CHECK_FINAL,
   ST_COUNT
 };
 

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 
+#include "ho_check.cuh"
 #include "ho_host.h"
 #include "ho_rounds.cuh"
 
@@ -182,6 +183,30 @@ int prepare_rounds(ho_context* c, int64_t n_cap) {
   RT_TRY(grow(rb.ecount, rb.ecount_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
   RT_TRY(grow(rb.eoff, rb.eoff_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
   RT_TRY(grow(rb.ctr, rb.ctr_cap, 4, sizeof(unsigned)));
+  RT_TRY(grow(rb.fail, rb.fail_cap, n, sizeof(uint32_t)));
+  return 0;
+}
+
+// FP64 check of the rays' hits, plain fallback of the failures.
+static int enqueue_check(ho_context* c, const TraceParams& P, const RoundParams& R, cudaStream_t s, int64_t n_cap) {
+  if (!c->fp64_check) return 0;
+  RT_TRY(cudaMemsetAsync(c->rounds.ctr + 3, 0, sizeof(unsigned), s));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e;
+  switch (c->N) {
+    case 2: e = launch_check_n<2>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 3: e = launch_check_n<3>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 4: e = launch_check_n<4>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 5: e = launch_check_n<5>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 6: e = launch_check_n<6>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 7: e = launch_check_n<7>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 8: e = launch_check_n<8>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 9: e = launch_check_n<9>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    default: e = cudaErrorInvalidValue; break;
+  }
+  RT_TRY(e);
   return 0;
 }
 
@@ -256,6 +281,10 @@ int enqueue_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lea
     const int rc = enqueue_round(c, P, R, s, learned, n_cap);
     if (rc) return rc;
   }
+  {
+    const int rc = enqueue_check(c, P, R, s, n_cap);
+    if (rc) return rc;
+  }
   round_finish_kernel<<<gi, 256, 0, s>>>(P, R.state);
   RT_TRY(cudaGetLastError());
   return 0;
@@ -279,6 +308,8 @@ int finish_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lear
     if (rc) return rc;
   }
   if (extra) {
+    const int rc = enqueue_check(c, P, R, s, n_cap);
+    if (rc) return rc;
     round_finish_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P, R.state);
     RT_TRY(cudaGetLastError());
   }

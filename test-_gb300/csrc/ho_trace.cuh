@@ -149,7 +149,7 @@ __device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool act
   // warp-aggregated counters
   unsigned long long v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled,
                                     w.nodes, w.accepted, w.rejected, w.restarts, w.cyc[0], w.cyc[1], w.cyc[2],
-                                    w.cyc[3], w.steps, w.lanes, 0ull, 0ull};
+                                    w.cyc[3], w.steps, w.lanes, 0ull, 0ull, 0ull, 0ull, 0ull};
 #pragma unroll
   for (int s = 0; s < ST_COUNT; ++s) {
     unsigned long long x = v[s];
@@ -356,10 +356,61 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
   flush_work(P.stats, w, false);
 }
 
+// The reference's per-ray structure: ordered candidates, each visited with
+// the sequential cold-start algorithm (visit_candidate), walking the tree
+// again when more than kCandK candidates were in range.
+template <int N>
+__device__ HitState plain_trace(const TraceParams& P, float3 o, float3 d, float iso, bool iso_on, Work& w) {
+  HitState best = miss_state();
+  float kt = -FLT_MAX;
+  int ke = -1;
+  for (;;) {
+    float bt[kCandK];
+    int be[kCandK];
+    bool overflow;
+    if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, w)) {
+      atomicOr(&P.stats->status, kStatusStackOverflow);
+      break;
+    }
+    bool done = false;
+#pragma unroll 1
+    for (int j = 0; j < kCandK; ++j) {
+      float ct = bt[0];
+      int ce = be[0];
+#pragma unroll
+      for (int m = 1; m < kCandK; ++m)
+        if (j == m) {
+          ct = bt[m];
+          ce = be[m];
+        }
+      if (ce == INT_MAX || ct > best.t) {
+        done = true;
+        break;
+      }
+      const float* b = P.box + 6 * static_cast<int64_t>(ce);
+      const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
+      const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
+      float te, tx;
+      if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
+        Elem<N> el;
+        el.c = CoefRef<false>{P.rec + static_cast<int64_t>(ce) * record_floats(N)};
+        el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
+        visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on, best,
+                           w);
+      }
+      kt = ct;
+      ke = ce;
+    }
+    if (done || !overflow) break;
+    ++w.restarts;
+    best.flags |= HO_FLAG_OVERFLOW;
+  }
+  return best;
+}
+
 // Plain form: the reference's structure on the GPU — one thread per query
-// (camera rays: a warp covers an 8x4 pixel tile), its own ordered candidate
-// loop, each candidate visited with the sequential cold-start algorithm
-// (visit_candidate). No queue, no lane-parallel solves, no prediction.
+// (camera rays: a warp covers an 8x4 pixel tile), no queue, no lane-parallel
+// solves, no prediction.
 template <int N>
 __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64_t n_queries) {
   const int lane = threadIdx.x & 31;
@@ -384,53 +435,7 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
   if (active) query_ray(P, q, o, d, iso_idx);
   Work w;
   HitState best = miss_state();
-  if (active) {
-    const float iso = P.iso[iso_idx];
-    const bool iso_on = (P.iso_on_mask >> iso_idx) & 1u;
-    float kt = -FLT_MAX;
-    int ke = -1;
-    for (;;) {
-      float bt[kCandK];
-      int be[kCandK];
-      bool overflow;
-      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, w)) {
-        atomicOr(&P.stats->status, kStatusStackOverflow);
-        break;
-      }
-      bool done = false;
-#pragma unroll 1
-      for (int j = 0; j < kCandK; ++j) {
-        float ct = bt[0];
-        int ce = be[0];
-#pragma unroll
-        for (int m = 1; m < kCandK; ++m)
-          if (j == m) {
-            ct = bt[m];
-            ce = be[m];
-          }
-        if (ce == INT_MAX || ct > best.t) {
-          done = true;
-          break;
-        }
-        const float* b = P.box + 6 * static_cast<int64_t>(ce);
-        const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
-        const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
-        float te, tx;
-        if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
-          Elem<N> el;
-          el.c = CoefRef<false>{P.rec + static_cast<int64_t>(ce) * record_floats(N)};
-          el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
-          visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
-                             best, w);
-        }
-        kt = ct;
-        ke = ce;
-      }
-      if (done || !overflow) break;
-      ++w.restarts;
-      best.flags |= HO_FLAG_OVERFLOW;
-    }
-  }
+  if (active) best = plain_trace<N>(P, o, d, P.iso[iso_idx], (P.iso_on_mask >> iso_idx) & 1u, w);
   flush_work(P.stats, w, active);
   if (active) write_result(P, q, d, best, w.newton + w.face);
 }

@@ -105,6 +105,7 @@ def test_engine_options():
         assert ctx.get_option(hr.OPT_GRAPH) == 1
         assert ctx.get_option(hr.OPT_ROUNDS) == 16
         assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 16
+        assert ctx.get_option(hr.OPT_FP64_CHECK) == 1
         ctx.set_option(hr.OPT_GRAPH, 0)
         ctx.set_option(hr.OPT_ROUNDS, 3)
         ctx.set_option(hr.OPT_ROUND_CHUNK, 200)

@@ -135,3 +135,35 @@ def test_autotune_picks_a_candidate_and_keeps_results(small):
     _, h1 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
     assert np.array_equal(h0["elem"], h1["elem"]) and np.array_equal(h0["t"], h1["t"])
     ctx.set_option(hr.OPT_ROUND_CHUNK, 16)
+
+
+def test_fp64_check_and_plain_fallback(small):
+    """Every hit is re-evaluated in FP64; a hit that fails is traced again by
+    the plain solver. With the check on, the rays that were re-traced equal
+    plain mode's answers and every other ray equals the unchecked answer."""
+    ctx, w, arrs, osc = small
+    W = H = 96
+    ctx.set_mode(hr.MODE_BATCHED)
+    ctx.set_option(hr.OPT_FP64_CHECK, 0)
+    _, h0 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    s0 = ctx.stats()
+    ctx.set_option(hr.OPT_FP64_CHECK, 1)
+    _, h1 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    s1 = ctx.stats()
+    ctx.set_mode(hr.MODE_PLAIN)
+    _, hp = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    ctx.set_mode(hr.MODE_BATCHED)
+    h0, h1, hp = h0.reshape(-1), h1.reshape(-1), hp.reshape(-1)
+    assert s0["fp64_checked"] == 0
+    assert s1["fp64_checked"] == int((h0["kind"] > 0).sum())
+    fb = (h1["flags"] & hr.FLAG_FALLBACK) != 0
+    print("fp64: checked", s1["fp64_checked"], "failed", s1["fp64_failed"], "failed after fallback",
+          s1["fp64_failed_after_fallback"])
+    assert int(fb.sum()) == s1["fp64_failed"]
+    assert s1["fp64_failed"] <= max(2, s1["fp64_checked"] // 100)
+    for k in ("kind", "elem", "face"):
+        assert np.array_equal(h1[k][fb], hp[k][fb])
+        assert np.array_equal(h1[k][~fb], h0[k][~fb])
+    assert np.array_equal(h1["t"][~fb], h0["t"][~fb])
+    failed_final = (h1["flags"] & hr.FLAG_FP64_FAIL) != 0
+    assert int(failed_final.sum()) == s1["fp64_failed_after_fallback"]
