@@ -52,6 +52,13 @@ void free_scene(ho_context* c) {
   cudaFree(c->d_own);
   cudaFree(c->d_nodes);
   cudaFree(c->d_desc);
+  cudaFree(c->d_crec);
+  cudaFree(c->d_coff);
+  cudaFree(c->d_cord);
+  c->d_crec = nullptr;
+  c->d_coff = nullptr;
+  c->d_cord = nullptr;
+  c->orders = 0;
   c->d_desc = nullptr;
   c->d_rec = c->d_box = c->d_hull = c->d_fbox = nullptr;
   c->d_flags = nullptr;
@@ -315,6 +322,29 @@ int ho_build_bvh(ho_context* c) {
   CK(cudaMemcpyAsync(c->d_rec, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload");
   CK(cudaMemcpyAsync(c->d_flags, flags.data(), ne * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream), "upload");
   CK(cudaMemcpyAsync(c->d_own, own.data(), ne * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream), "upload");
+  {
+    // per-element orders; a mixed-order scene also gets compact records at
+    // each element's own order for the round kernels
+    std::vector<uint8_t> ord(ne);
+    for (int64_t e = 0; e < ne; ++e) {
+      ord[e] = static_cast<uint8_t>(ho::element_order(hs, e));
+      c->orders |= 1u << ord[e];
+    }
+    CK(cudaMalloc(&c->d_cord, ne * sizeof(uint8_t)), "cudaMalloc(orders)");
+    CK(cudaMemcpyAsync(c->d_cord, ord.data(), ne, cudaMemcpyHostToDevice, c->stream), "upload");
+    if (c->orders != (1u << N)) {
+      std::vector<float> crec;
+      std::vector<int64_t> coff;
+      ho::pack_compact(hs, crec, coff, ord);
+      CK(cudaMalloc(&c->d_crec, crec.size() * sizeof(float)), "cudaMalloc(compact records)");
+      CK(cudaMalloc(&c->d_coff, ne * sizeof(int64_t)), "cudaMalloc(record offsets)");
+      CK(cudaMemcpyAsync(c->d_crec, crec.data(), crec.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+         "upload");
+      CK(cudaMemcpyAsync(c->d_coff, coff.data(), ne * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream), "upload");
+      CK(cudaStreamSynchronize(c->stream), "sync");
+      c->device_bytes += static_cast<int64_t>(crec.size() * sizeof(float)) + ne * 8;
+    }
+  }
   rc = ho::launch_setup(c);
   if (rc) return cuda_fail(c, rc, "setup kernel");
   rc = ho::build_lbvh(c);
@@ -324,8 +354,8 @@ int ho_build_bvh(ho_context* c) {
   if (rc) return cuda_fail(c, rc, "descriptor kernel");
   if (c->bvh_depth + 2 > 64) return fail(c, HO_ERR_RANGE, "BVH deeper than the traversal stack");
   CK(cudaStreamSynchronize(c->stream), "sync");
-  c->device_bytes = static_cast<int64_t>(rec.size() * sizeof(float)) + ne * (4 + 4 + 24 + 24 + 144) +
-                    c->n_nodes * static_cast<int64_t>(sizeof(ho::BNode));
+  c->device_bytes += static_cast<int64_t>(rec.size() * sizeof(float)) + ne * (4 + 4 + 1 + 24 + 24 + 144) +
+                     c->n_nodes * static_cast<int64_t>(sizeof(ho::BNode));
   c->built = true;
   return HO_OK;
 }

@@ -52,6 +52,14 @@ int scene_max_modes(const HostScene& hs);
 void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vector<uint32_t>& flags,
                   std::vector<int32_t>& own);
 
+// Cube order of an element: its largest geometry or field modes count per
+// direction (trilinear: 2).
+int element_order(const HostScene& hs, int64_t e);
+// Every element's record at its own order, back to back: off[e] is its
+// first float, order[e] its modes per direction (same block layout as
+// pack_records at N = order[e]).
+void pack_compact(const HostScene& hs, std::vector<float>& rec, std::vector<int64_t>& off, std::vector<uint8_t>& order);
+
 // 1-D change of basis Modified-A -> Bernstein on [a,b] for n modes:
 // phi_i(x) = sum_k M[i*n+k] * B_k((x-a)/(b-a)).
 void modal_to_bernstein(int n, double a, double b, std::vector<double>& M);
@@ -104,6 +112,12 @@ struct ho_context {
   int N = 0;
   int64_t n_elem = 0;
   float* d_rec = nullptr;         // n_elem * record_floats(N)
+  // mixed-order scenes: every element's record at its own order (the round
+  // kernels read these; everything else reads d_rec)
+  float* d_crec = nullptr;
+  int64_t* d_coff = nullptr;      // n_elem, float offset of each record in d_crec
+  uint8_t* d_cord = nullptr;      // n_elem, modes per direction of each record
+  uint32_t orders = 0;            // bit n: some element has order n
   float* d_box = nullptr;         // n_elem * 6 padded sampled boxes
   float* d_hull = nullptr;        // n_elem * 6 Bernstein hull boxes
   float* d_fbox = nullptr;        // n_elem * 36 face hull boxes

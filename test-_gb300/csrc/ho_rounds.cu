@@ -117,16 +117,47 @@ __global__ void round_scatter_kernel(const RoundPair* __restrict__ pairs, const 
   sorted[eoff[pelem[k]] + prank[k]] = pairs[k];
 }
 
-// Each element's pairs in batches of at most B.
-__global__ void round_batch_kernel(const uint32_t* __restrict__ ecount, const uint32_t* __restrict__ eoff,
-                                   int64_t n_elem, int B, RoundBatch* __restrict__ batches,
-                                   unsigned* __restrict__ n_batches) {
+// Ctr layout: [0] pairs of the round, [3] failed FP64 checks, and per order n
+// (2..9) the batch count, region start, write cursor and take cursor.
+constexpr int kCtrOrderNb = 16, kCtrOrderOff = 26, kCtrOrderCur = 36, kCtrOrderNext = 46, kCtrWords = 64;
+
+__device__ __forceinline__ int batch_size(int chunk, int order) { return chunk > 0 ? chunk : round_slots(order); }
+
+// Batches per order: each element's pairs in batches of its order's size.
+__global__ void round_batch_count_kernel(const uint32_t* __restrict__ ecount, const uint8_t* __restrict__ order,
+                                         int64_t n_elem, int chunk, unsigned* __restrict__ ctr) {
   const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n_elem) return;
   const int c = static_cast<int>(ecount[e]);
   if (c == 0) return;
+  const int n = order[e];
+  const int B = batch_size(chunk, n);
+  atomicAdd(&ctr[kCtrOrderNb + n], static_cast<unsigned>((c + B - 1) / B));
+}
+
+// Region start of each order's batches (orders in increasing n).
+__global__ void round_order_offsets_kernel(unsigned* __restrict__ ctr) {
+  unsigned run = 0;
+  for (int n = 0; n < 10; ++n) {
+    ctr[kCtrOrderOff + n] = run;
+    ctr[kCtrOrderCur + n] = 0;
+    ctr[kCtrOrderNext + n] = 0;
+    run += ctr[kCtrOrderNb + n];
+  }
+}
+
+// Each element's pairs in batches, written into its order's region.
+__global__ void round_batch_kernel(const uint32_t* __restrict__ ecount, const uint32_t* __restrict__ eoff,
+                                   const uint8_t* __restrict__ order, int64_t n_elem, int chunk,
+                                   RoundBatch* __restrict__ batches, unsigned* __restrict__ ctr) {
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n_elem) return;
+  const int c = static_cast<int>(ecount[e]);
+  if (c == 0) return;
+  const int n = order[e];
+  const int B = batch_size(chunk, n);
   const int nb = (c + B - 1) / B;
-  const unsigned base = atomicAdd(n_batches, static_cast<unsigned>(nb));
+  const unsigned base = ctr[kCtrOrderOff + n] + atomicAdd(&ctr[kCtrOrderCur + n], static_cast<unsigned>(nb));
   for (int k = 0; k < nb; ++k) {
     RoundBatch bt;
     bt.elem = static_cast<int32_t>(e);
@@ -182,7 +213,7 @@ int prepare_rounds(ho_context* c, int64_t n_cap) {
   RT_TRY(grow(rb.batches, rb.batches_cap, n, sizeof(RoundBatch)));
   RT_TRY(grow(rb.ecount, rb.ecount_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
   RT_TRY(grow(rb.eoff, rb.eoff_cap, static_cast<size_t>(n_elem), sizeof(uint32_t)));
-  RT_TRY(grow(rb.ctr, rb.ctr_cap, 4, sizeof(unsigned)));
+  RT_TRY(grow(rb.ctr, rb.ctr_cap, kCtrWords, sizeof(unsigned)));
   RT_TRY(grow(rb.fail, rb.fail_cap, n, sizeof(uint32_t)));
   return 0;
 }
@@ -225,8 +256,11 @@ static RoundParams round_params(ho_context* c, const TraceParams& P) {
   R.state = static_cast<RayState*>(rb.state);
   R.pairs = static_cast<RoundPair*>(rb.pairs) + rb.pairs_cap / 2;
   R.batches = static_cast<RoundBatch*>(rb.batches);
-  R.n_batches = rb.ctr + 1;
-  R.next_batch = rb.ctr + 2;
+  R.batch_base = rb.ctr + kCtrOrderOff + c->N;
+  R.n_batches = rb.ctr + kCtrOrderNb + c->N;
+  R.next_batch = rb.ctr + kCtrOrderNext + c->N;
+  R.crec = c->d_crec;
+  R.coff = c->d_coff;
   R.stats = P.stats;
   R.desc = P.desc;
   R.cand_e = P.cand_e;
@@ -244,28 +278,38 @@ static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams&
   RoundPair* gathered = static_cast<RoundPair*>(rb.pairs);
   const unsigned gi = static_cast<unsigned>((n_cap + 255) / 256);
   RT_TRY(cudaMemsetAsync(rb.ecount, 0, static_cast<size_t>(n_elem) * sizeof(uint32_t), s));
-  RT_TRY(cudaMemsetAsync(rb.ctr, 0, 4 * sizeof(unsigned), s));
+  RT_TRY(cudaMemsetAsync(rb.ctr, 0, kCtrWords * sizeof(unsigned), s));
   round_gather_kernel<<<gi, 256, 0, s>>>(P, R.state, gathered, rb.pelem, rb.prank, rb.ecount, rb.ctr);
   RT_TRY(cudaMemcpyAsync(rb.eoff, rb.ecount, static_cast<size_t>(n_elem) * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
                          s));
   scan_kernel<<<1, 1024, 0, s>>>(rb.eoff, n_elem);
   round_scatter_kernel<<<gi, 256, 0, s>>>(gathered, rb.pelem, rb.prank, rb.eoff, rb.ctr,
                                           const_cast<RoundPair*>(R.pairs), P.stats);
-  round_batch_kernel<<<static_cast<unsigned>((n_elem + 255) / 256), 256, 0, s>>>(
-      rb.ecount, rb.eoff, n_elem, c->round_chunk > 0 ? c->round_chunk : round_slots(c->N),
-      const_cast<RoundBatch*>(R.batches), rb.ctr + 1);
+  const unsigned ge = static_cast<unsigned>((n_elem + 255) / 256);
+  round_batch_count_kernel<<<ge, 256, 0, s>>>(rb.ecount, c->d_cord, n_elem, c->round_chunk, rb.ctr);
+  round_order_offsets_kernel<<<1, 1, 0, s>>>(rb.ctr);
+  round_batch_kernel<<<ge, 256, 0, s>>>(rb.ecount, rb.eoff, c->d_cord, n_elem, c->round_chunk,
+                                        const_cast<RoundBatch*>(R.batches), rb.ctr);
   RT_TRY(cudaGetLastError());
-  cudaError_t e;
-  switch (c->N) {
-    case 2: e = launch_round_n<2>(R, s, learned); break;
-    case 3: e = launch_round_n<3>(R, s, learned); break;
-    case 4: e = launch_round_n<4>(R, s, learned); break;
-    case 5: e = launch_round_n<5>(R, s, learned); break;
-    case 6: e = launch_round_n<6>(R, s, learned); break;
-    case 7: e = launch_round_n<7>(R, s, learned); break;
-    case 8: e = launch_round_n<8>(R, s, learned); break;
-    case 9: e = launch_round_n<9>(R, s, learned); break;
-    default: e = cudaErrorInvalidValue; break;
+  // one launch per element order present in the scene
+  cudaError_t e = cudaSuccess;
+  for (int n = kMinModes; n <= kMaxModes && e == cudaSuccess; ++n) {
+    if (!((c->orders >> n) & 1u)) continue;
+    RoundParams Rn = R;
+    Rn.batch_base = rb.ctr + kCtrOrderOff + n;
+    Rn.n_batches = rb.ctr + kCtrOrderNb + n;
+    Rn.next_batch = rb.ctr + kCtrOrderNext + n;
+    switch (n) {
+      case 2: e = launch_round_n<2>(Rn, s, learned); break;
+      case 3: e = launch_round_n<3>(Rn, s, learned); break;
+      case 4: e = launch_round_n<4>(Rn, s, learned); break;
+      case 5: e = launch_round_n<5>(Rn, s, learned); break;
+      case 6: e = launch_round_n<6>(Rn, s, learned); break;
+      case 7: e = launch_round_n<7>(Rn, s, learned); break;
+      case 8: e = launch_round_n<8>(Rn, s, learned); break;
+      case 9: e = launch_round_n<9>(Rn, s, learned); break;
+      default: e = cudaErrorInvalidValue; break;
+    }
   }
   RT_TRY(e);
   return 0;

@@ -91,8 +91,13 @@ struct RoundParams {
   RayState* __restrict__ state;
   const RoundPair* __restrict__ pairs;  // element-sorted
   const RoundBatch* __restrict__ batches;
+  const unsigned* batch_base;  // this launch's batches: [*batch_base, *batch_base + *n_batches)
   const unsigned* n_batches;
   unsigned* next_batch;
+  // mixed-order scenes: element e's record at crec + coff[e] (its own order);
+  // coff == nullptr: rec + e * record_floats(N)
+  const float* __restrict__ crec;
+  const int64_t* __restrict__ coff;
   DevStats* stats;
   // learned mode
   const float* desc;
@@ -447,17 +452,18 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
   Elem<N, true> el;
   el.c = CoefRef<true>{static_cast<uint32_t>(__cvta_generic_to_shared(W.rec))};
   Work w;
-  const unsigned nb = *P.n_batches;
+  const unsigned nb = *P.n_batches, bbase = *P.batch_base;
   for (;;) {
     unsigned b = 0;
     if (lane == 0) b = atomicAdd(P.next_batch, 1u);
     b = __shfl_sync(kFull, b, 0);
     if (b >= nb) break;
-    const RoundBatch bt = P.batches[b];
+    const RoundBatch bt = P.batches[bbase + b];
     const unsigned count = static_cast<unsigned>(bt.count);
     const float* fbox = P.fbox + static_cast<int64_t>(bt.elem) * kFaceBoxFloats;
     {
-      const float4* src = reinterpret_cast<const float4*>(P.rec + static_cast<int64_t>(bt.elem) * record_floats(N));
+      const float* recp = P.coff ? P.crec + P.coff[bt.elem] : P.rec + static_cast<int64_t>(bt.elem) * record_floats(N);
+      const float4* src = reinterpret_cast<const float4*>(recp);
       float4* dst = reinterpret_cast<float4*>(W.rec);
       for (int q4 = lane; q4 < record_floats(N) / 4; q4 += 32) dst[q4] = __ldg(src + q4);
     }

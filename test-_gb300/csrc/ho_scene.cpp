@@ -357,50 +357,83 @@ int scene_max_modes(const HostScene& hs) {
 // (FEM-AABB/fem/HexElement.cu:107-109); the map is its own inverse.
 static const int kXml2Z[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 
+// Cube order of element e: its largest geometry or field modes count per
+// direction (a trilinear element counts as 2).
+int element_order(const HostScene& hs, int64_t e) {
+  int n = 2;
+  if (hs.goff[e] >= 0)
+    for (int a = 0; a < 3; ++a) n = std::max(n, static_cast<int>(hs.gmodes[3 * e + a]));
+  if (hs.foff[e] >= 0)
+    for (int a = 0; a < 3; ++a) n = std::max(n, static_cast<int>(hs.fmodes[3 * e + a]));
+  return n;
+}
+
+// One element's record at n modes per direction into r (record_floats(n)
+// zeroed floats); returns the element's flags and own geometry modes.
+static uint32_t pack_one(const HostScene& hs, int64_t e, int N, float* r, int32_t& own) {
+  const int64_t S = block_floats(N), RS = row_stride(N);
+  uint32_t fl = 0;
+  if (hs.goff[e] >= 0) {
+    const uint32_t mx = hs.gmodes[3 * e], my = hs.gmodes[3 * e + 1], mz = hs.gmodes[3 * e + 2];
+    const int64_t cnt = static_cast<int64_t>(mx) * my * mz;
+    for (int c = 0; c < 3; ++c) {
+      const float* src = hs.geom.data() + hs.goff[e] + c * cnt;
+      for (uint32_t k = 0; k < mz; ++k)
+        for (uint32_t j = 0; j < my; ++j)
+          for (uint32_t i = 0; i < mx; ++i) r[c * S + (k * N + j) * RS + i] = src[(k * my + j) * mx + i];
+    }
+    own = static_cast<int32_t>(std::max(mx, std::max(my, mz)));
+  } else {
+    // trilinear map == N=2 modal map with the corners as coefficients
+    const float* cv = hs.corners.data() + e * 24;
+    for (int v = 0; v < 8; ++v) {
+      const int z = kXml2Z[v];
+      const int i = z & 1, j = (z >> 1) & 1, k = (z >> 2) & 1;
+      for (int c = 0; c < 3; ++c) r[c * S + (k * N + j) * RS + i] = cv[3 * v + c];
+    }
+    fl |= 2u;
+    own = 0;
+  }
+  if (hs.foff[e] >= 0) {
+    const uint32_t mx = hs.fmodes[3 * e], my = hs.fmodes[3 * e + 1], mz = hs.fmodes[3 * e + 2];
+    if (mx > 0 && my > 0 && mz > 0) {
+      const float* src = hs.field.data() + hs.foff[e];
+      for (uint32_t k = 0; k < mz; ++k)
+        for (uint32_t j = 0; j < my; ++j)
+          for (uint32_t i = 0; i < mx; ++i) r[3 * S + (k * N + j) * RS + i] = src[(k * my + j) * mx + i];
+      fl |= 1u;
+    }
+  }
+  return fl;
+}
+
 void pack_records(const HostScene& hs, int N, std::vector<float>& rec, std::vector<uint32_t>& flags,
                   std::vector<int32_t>& own) {
   const int64_t ne = hs.size();
-  const int64_t S = block_floats(N), RS = row_stride(N);
   rec.assign(static_cast<size_t>(ne) * record_floats(N), 0.0f);
   flags.assign(ne, 0);
   own.assign(ne, 0);
   parallel_chunks(ne, [&](int64_t b, int64_t e_end) {
+    for (int64_t e = b; e < e_end; ++e) flags[e] = pack_one(hs, e, N, rec.data() + e * record_floats(N), own[e]);
+  });
+}
+
+void pack_compact(const HostScene& hs, std::vector<float>& rec, std::vector<int64_t>& off, std::vector<uint8_t>& order) {
+  const int64_t ne = hs.size();
+  off.assign(ne, 0);
+  order.assign(ne, 0);
+  int64_t total = 0;
+  for (int64_t e = 0; e < ne; ++e) {
+    const int n = element_order(hs, e);
+    order[e] = static_cast<uint8_t>(n);
+    off[e] = total;
+    total += record_floats(n);
+  }
+  rec.assign(static_cast<size_t>(total), 0.0f);
+  parallel_chunks(ne, [&](int64_t b, int64_t e_end) {
     for (int64_t e = b; e < e_end; ++e) {
-      float* r = rec.data() + e * record_floats(N);
-      uint32_t fl = 0;
-      if (hs.goff[e] >= 0) {
-        const uint32_t mx = hs.gmodes[3 * e], my = hs.gmodes[3 * e + 1], mz = hs.gmodes[3 * e + 2];
-        const int64_t cnt = static_cast<int64_t>(mx) * my * mz;
-        for (int c = 0; c < 3; ++c) {
-          const float* src = hs.geom.data() + hs.goff[e] + c * cnt;
-          for (uint32_t k = 0; k < mz; ++k)
-            for (uint32_t j = 0; j < my; ++j)
-              for (uint32_t i = 0; i < mx; ++i)
-                r[c * S + (k * N + j) * RS + i] = src[(k * my + j) * mx + i];
-        }
-        own[e] = static_cast<int32_t>(std::max(mx, std::max(my, mz)));
-      } else {
-        // trilinear map == N=2 modal map with the corners as coefficients
-        const float* cv = hs.corners.data() + e * 24;
-        for (int v = 0; v < 8; ++v) {
-          const int z = kXml2Z[v];
-          const int i = z & 1, j = (z >> 1) & 1, k = (z >> 2) & 1;
-          for (int c = 0; c < 3; ++c) r[c * S + (k * N + j) * RS + i] = cv[3 * v + c];
-        }
-        fl |= 2u;
-        own[e] = 0;
-      }
-      if (hs.foff[e] >= 0) {
-        const uint32_t mx = hs.fmodes[3 * e], my = hs.fmodes[3 * e + 1], mz = hs.fmodes[3 * e + 2];
-        if (mx > 0 && my > 0 && mz > 0) {
-          const float* src = hs.field.data() + hs.foff[e];
-          for (uint32_t k = 0; k < mz; ++k)
-            for (uint32_t j = 0; j < my; ++j)
-              for (uint32_t i = 0; i < mx; ++i) r[3 * S + (k * N + j) * RS + i] = src[(k * my + j) * mx + i];
-          fl |= 1u;
-        }
-      }
-      flags[e] = fl;
+      int32_t own;
+      pack_one(hs, e, order[e], rec.data() + off[e], own);
     }
   });
 }
