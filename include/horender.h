@@ -181,6 +181,23 @@ int ho_get_boxes(ho_context* ctx, float* out);
  * either output may be NULL. No reference counterpart (verification aid). */
 int ho_get_hull_boxes(ho_context* ctx, float* hull_out, float* face_out);
 
+/* Many camera views in one call (no reference counterpart; the reference
+ * renders one camera per render_kernel launch, FEM-AABB/main.cu:486-511).
+ * View v: camera cams[v], widths[v] x heights[v] pixel-centre rays for each
+ * of its n_isos[v] (1..8) isovalues isovalues[8*v + 0 .. n_isos[v]-1]. All
+ * views' rays run in the same classify pass and rounds. Outputs are laid out
+ * view by view, isovalue-major inside a view: view v starts at query
+ * offsets_out[v] (n_views + 1 entries, may be NULL), i.e. rgb_out + 3 *
+ * offsets_out[v] and hits_out + offsets_out[v]. */
+int ho_render_views(ho_context* ctx, int n_views, const ho_camera* cams, const int32_t* widths, const int32_t* heights,
+                    const float* isovalues, const int32_t* n_isos, int iso_zero_disables, uint8_t* rgb_out,
+                    ho_hit* hits_out, int64_t* offsets_out);
+/* Device-buffer form of ho_render_views on the given stream (NULL: the
+ * context's stream); returns without synchronising. */
+int ho_render_views_device(ho_context* ctx, int n_views, const ho_camera* cams, const int32_t* widths,
+                           const int32_t* heights, const float* isovalues, const int32_t* n_isos, int iso_zero_disables,
+                           uint8_t* rgb_dev, ho_hit* hits_dev, int64_t* offsets_out, void* stream);
+
 /* Replaces: render_kernel<<<>>> + cudaMemcpy of the framebuffer
  * (FEM-AABB/raytracer.cu:410-476, main.cu:515-543). One primary ray per
  * pixel per isovalue; rgb_out receives n_iso images of H*W*3 bytes, row 0 =

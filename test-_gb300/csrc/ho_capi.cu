@@ -178,6 +178,7 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_hits);
     cudaFree(c->d_rgb);
     cudaFree(c->d_rays);
+    cudaFree(c->d_views);
     cudaFree(c->d_work);
     cudaFree(c->d_kbuf);
     cudaFree(c->d_kovf);
@@ -415,6 +416,80 @@ int ho_render_device(ho_context* c, const ho_camera* cam, const float* iso, int 
   rc = ho::launch_trace(c, a, s);
   if (rc) return cuda_fail(c, rc, "trace kernel");
   return HO_OK;
+}
+
+int ho_render_views_device(ho_context* c, int n_views, const ho_camera* cams, const int32_t* widths,
+                           const int32_t* heights, const float* isovalues, const int32_t* n_isos, int iso_zero_disables,
+                           uint8_t* rgb_dev, ho_hit* hits_dev, int64_t* offsets_out, void* stream) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (n_views < 1 || n_views > (1 << 20)) return fail(c, HO_ERR_RANGE, "n_views must be in [1, 2^20]");
+  if (!cams || !widths || !heights || !isovalues || !n_isos) return fail(c, HO_ERR_ARG, "null argument");
+  std::vector<ho::ViewDesc> views(n_views);
+  int64_t total = 0;
+  for (int v = 0; v < n_views; ++v) {
+    if (widths[v] <= 0 || heights[v] <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
+    if (n_isos[v] < 1 || n_isos[v] > 8) return fail(c, HO_ERR_RANGE, "n_isos must be in [1, 8]");
+    ho::TraceArgs a;
+    camera_basis(cams[v], widths[v], heights[v], a);
+    ho::ViewDesc& d = views[v];
+    d.cam.origin = make_float3(a.origin[0], a.origin[1], a.origin[2]);
+    d.cam.llc = make_float3(a.llc[0], a.llc[1], a.llc[2]);
+    d.cam.horiz = make_float3(a.horiz[0], a.horiz[1], a.horiz[2]);
+    d.cam.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
+    d.cam.width = widths[v];
+    d.cam.height = heights[v];
+    d.q0 = total;
+    d.n_iso = n_isos[v];
+    d.iso_on_mask = 0;
+    for (int i = 0; i < 8; ++i) {
+      d.iso[i] = i < n_isos[v] ? isovalues[8 * v + i] : 0.f;
+      if (i < n_isos[v] && !(iso_zero_disables && d.iso[i] == 0.0f)) d.iso_on_mask |= 1u << i;
+    }
+    if (offsets_out) offsets_out[v] = total;
+    total += static_cast<int64_t>(widths[v]) * heights[v] * n_isos[v];
+  }
+  if (offsets_out) offsets_out[n_views] = total;
+  if (total > (int64_t(1) << 31)) return fail(c, HO_ERR_RANGE, "too many rays");
+  int rc;
+  if ((rc = ensure_buf(c, c->d_views, c->views_cap, views.size() * sizeof(ho::ViewDesc), "cudaMalloc(views)")))
+    return rc;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  CK(cudaMemcpyAsync(c->d_views, views.data(), views.size() * sizeof(ho::ViewDesc), cudaMemcpyHostToDevice, s),
+     "upload views");
+  ho::TraceArgs a;
+  a.views = reinterpret_cast<const ho::ViewDesc*>(c->d_views);
+  a.n_views = n_views;
+  a.n_queries_views = total;
+  a.n_iso = 1;
+  a.rgb = rgb_dev;
+  a.hits = hits_dev;
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
+  rc = ho::launch_trace(c, a, s);
+  if (rc) return cuda_fail(c, rc, "trace kernel");
+  return HO_OK;
+}
+
+int ho_render_views(ho_context* c, int n_views, const ho_camera* cams, const int32_t* widths, const int32_t* heights,
+                    const float* isovalues, const int32_t* n_isos, int iso_zero_disables, uint8_t* rgb_out,
+                    ho_hit* hits_out, int64_t* offsets_out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (n_views < 1 || !widths || !heights || !n_isos) return fail(c, HO_ERR_ARG, "null argument or no views");
+  int64_t total = 0;
+  for (int v = 0; v < n_views; ++v)
+    total += static_cast<int64_t>(std::max(widths[v], 0)) * std::max(heights[v], 0) * std::max(n_isos[v], 0);
+  const size_t nq = static_cast<size_t>(total);
+  int rc;
+  if (rgb_out && (rc = ensure_buf(c, c->d_rgb, c->rgb_cap, nq * 3, "cudaMalloc(rgb)"))) return rc;
+  if (hits_out && (rc = ensure_buf(c, c->d_hits, c->hits_cap, nq, "cudaMalloc(hits)"))) return rc;
+  rc = ho_render_views_device(c, n_views, cams, widths, heights, isovalues, n_isos, iso_zero_disables,
+                              rgb_out ? c->d_rgb : nullptr, hits_out ? c->d_hits : nullptr, offsets_out, c->stream);
+  if (rc) return rc;
+  if (rgb_out) CK(cudaMemcpyAsync(rgb_out, c->d_rgb, nq * 3, cudaMemcpyDeviceToHost, c->stream), "read images");
+  if (hits_out)
+    CK(cudaMemcpyAsync(hits_out, c->d_hits, nq * sizeof(ho_hit), cudaMemcpyDeviceToHost, c->stream), "read hits");
+  return read_stats(c);
 }
 
 int ho_render(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int iso_zero_disables,

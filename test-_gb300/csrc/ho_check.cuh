@@ -103,10 +103,11 @@ __global__ void __launch_bounds__(128) check_kernel(TraceParams P, RayState* __r
     RayState& r = st[item];
     if (r.best.kind != HO_HIT_MISS) {
       float3 o, d;
-      int iso_idx;
-      query_ray(P, P.work[item], o, d, iso_idx);
+      float iso;
+      bool iso_on;
+      query_ray(P, P.work[item], o, d, iso, iso_on);
       checked = true;
-      failed = !fp64_check<N>(P, o, d, P.iso[iso_idx], r.best);
+      failed = !fp64_check<N>(P, o, d, iso, r.best);
       if (failed) fail_list[atomicAdd(n_fail, 1u)] = item;
     }
   }
@@ -129,10 +130,10 @@ __global__ void __launch_bounds__(kTraceBlock) fallback_kernel(TraceParams P, Ra
   for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const unsigned item = fail_list[k];
     float3 o, d;
-    int iso_idx;
-    query_ray(P, P.work[item], o, d, iso_idx);
-    const float iso = P.iso[iso_idx];
-    HitState b = plain_trace<N>(P, o, d, iso, (P.iso_on_mask >> iso_idx) & 1u, w);
+    float iso;
+    bool iso_on;
+    query_ray(P, P.work[item], o, d, iso, iso_on);
+    HitState b = plain_trace<N>(P, o, d, iso, iso_on, w);
     b.flags |= HO_FLAG_FALLBACK | (st[item].best.flags & HO_FLAG_OVERFLOW);
     if (!fp64_check<N>(P, o, d, iso, b)) {
       b.flags |= HO_FLAG_FP64_FAIL;

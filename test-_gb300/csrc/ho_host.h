@@ -139,6 +139,8 @@ struct ho_context {
   size_t rgb_cap = 0;
   float* d_rays = nullptr;
   size_t rays_cap = 0;
+  uint8_t* d_views = nullptr;     // view table of a multi-view call
+  size_t views_cap = 0;
   // learned mode
   ho::Mlp mlp;
   float* d_desc = nullptr;        // n_elem * 48 element descriptors
@@ -178,6 +180,9 @@ struct TraceArgs {
   float iso[8];
   int n_iso = 0;
   uint32_t iso_on_mask = 0;     // bit i: isovalue i enabled
+  const ViewDesc* views = nullptr;  // multi-view call: device table
+  int n_views = 0;
+  int64_t n_queries_views = 0;  // total queries of the views
   ho_hit* hits = nullptr;       // optional
   uint8_t* rgb = nullptr;       // optional (camera mode)
 };

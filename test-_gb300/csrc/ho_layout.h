@@ -1,6 +1,8 @@
 // Data layouts shared by host code and kernels.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 #include "horender.h"
@@ -13,6 +15,23 @@
 #endif
 
 namespace ho {
+
+// Pinhole camera of one view: pixel (x, y) looks along
+// llc + s*horiz + t*vert - origin, s = (x + 0.5)/width, t = (y + 0.5)/height.
+struct CamArgs {
+  float3 origin, llc, horiz, vert;
+  int width, height;
+};
+
+// One camera view of a multi-view call: its pixel-centre rays are queries
+// [q0, q0 + width * height * n_iso), isovalue-major like a single view.
+struct ViewDesc {
+  CamArgs cam;
+  int64_t q0;
+  int n_iso;
+  uint32_t iso_on_mask;
+  float iso[8];
+};
 
 // BVH child record: the child's box plus its index. idx >= 0: internal node;
 // idx < 0: leaf holding element ~idx; idx == kEmptyChild: unused slot.

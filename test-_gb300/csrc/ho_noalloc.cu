@@ -119,6 +119,8 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
   P.iso[0] = iso;
   P.n_iso = 1;
   P.iso_on_mask = iso_enabled ? 1u : 0u;
+  P.views = nullptr;
+  P.n_views = 0;
   P.hits = out_dev;
   P.rgb = nullptr;
   P.stats = reinterpret_cast<DevStats*>(base + kNaStats);

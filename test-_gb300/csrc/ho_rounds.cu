@@ -44,8 +44,9 @@ __global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, Ro
   RayState& r = st[item];
   if (r.done) return;
   float3 o, d;
-  int iso_idx;
-  query_ray(P, P.work[item], o, d, iso_idx);
+  float iso;
+  bool iso_on;
+  query_ray(P, P.work[item], o, d, iso, iso_on);
   Work w;
   float2* kb = P.kbuf + static_cast<int64_t>(item) * kCandK;
   for (int guard = 0; guard < (1 << 20); ++guard) {
@@ -173,8 +174,9 @@ __global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ 
   if (item >= *P.qcount) return;
   const int64_t q = P.work[item];
   float3 o, d;
-  int iso_idx;
-  query_ray(P, q, o, d, iso_idx);
+  float iso;
+  bool iso_on;
+  query_ray(P, q, o, d, iso, iso_on);
   write_result(P, q, d, st[item].best, static_cast<uint32_t>(st[item].its));
 }
 
@@ -252,6 +254,8 @@ static RoundParams round_params(ho_context* c, const TraceParams& P) {
   R.cam = P.cam;
   for (int i = 0; i < 8; ++i) R.iso[i] = P.iso[i];
   R.iso_on_mask = P.iso_on_mask;
+  R.views = P.views;
+  R.n_views = P.n_views;
   R.work = P.work;
   R.state = static_cast<RayState*>(rb.state);
   R.pairs = static_cast<RoundPair*>(rb.pairs) + rb.pairs_cap / 2;

@@ -87,6 +87,8 @@ struct RoundParams {
   CamArgs cam;
   float iso[8];
   uint32_t iso_on_mask;
+  const ViewDesc* views;
+  int n_views;
   const int32_t* __restrict__ work;  // queue item -> query index
   RayState* __restrict__ state;
   const RoundPair* __restrict__ pairs;  // element-sorted
@@ -410,17 +412,18 @@ __device__ __noinline__ int admit_pair(WarpSm<N>* Wp, const RoundParams* P, int 
   PairSm& p = W.pr[slot];
   const int64_t q = P->work[rp.item];
   float3 o, d;
-  int iso_idx;
-  query_ray_from(P->rays, P->n_rays, P->cam, q, o, d, iso_idx);
+  float iso;
+  bool iso_on;
+  query_ray_from(P->rays, P->n_rays, P->cam, P->iso, P->iso_on_mask, P->views, P->n_views, q, o, d, iso, iso_on);
   st3(p.o, o);
   st3(p.d, d);
   p.te = rp.te;
   p.tx = rp.tx;
-  p.iso = P->iso[iso_idx];
+  p.iso = iso;
   p.best_t = P->state[rp.item].best.t;
   p.item = rp.item;
   p.elem = elem;
-  int fl = (has_field ? 1 : 0) | ((P->iso_on_mask >> iso_idx) & 1u ? 2 : 0);
+  int fl = (has_field ? 1 : 0) | (iso_on ? 2 : 0);
   if (L && rp.j >= 0 && rp.j < kPredK && P->cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == elem) {
     const float* y = P->pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
     p.pxi[0] = y[0]; p.pxi[1] = y[1]; p.pxi[2] = y[2];

@@ -19,8 +19,9 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
   int be[kCandK];
   float3 o = make_float3(0.f, 0.f, 0.f), d = make_float3(0.f, 0.f, 1.f);
   if (q < n_queries) {
-    int iso_idx;
-    query_ray(P, q, o, d, iso_idx);
+    float iso;
+    bool iso_on;
+    query_ray(P, q, o, d, iso, iso_on);
     // the ray's first kCandK ordered candidates (nothing is hit yet, so the
     // bound is infinite): the intersect pass starts from this list
     if (!collect(P, o, d, FLT_MAX, -FLT_MAX, -1, bt, be, overflow, w)) {
@@ -59,8 +60,9 @@ __global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16*
        item += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int64_t q = P.work[item];
     float3 o, d;
-    int iso_idx;
-    query_ray(P, q, o, d, iso_idx);
+    float iso;
+    bool iso_on;
+    query_ray(P, q, o, d, iso, iso_on);
     const float2* kb = P.kbuf + item * kCandK;
 #pragma unroll
     for (int j = 0; j < kPredK; ++j) {
@@ -122,12 +124,17 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   for (int i = 0; i < 8; ++i) P.iso[i] = i < a.n_iso ? a.iso[i] : 0.f;
   P.n_iso = a.n_iso;
   P.iso_on_mask = a.iso_on_mask;
+  P.views = a.views;
+  P.n_views = a.n_views;
   P.hits = a.hits;
   P.rgb = a.rgb;
   P.stats = c->d_stats;
   int64_t n_queries, n_threads;
   if (a.rays) {
     n_queries = a.n_rays * a.n_iso;
+    n_threads = n_queries;
+  } else if (a.views) {
+    n_queries = a.n_queries_views;
     n_threads = n_queries;
   } else {
     const int64_t tiles = static_cast<int64_t>((a.width + 7) / 8) * ((a.height + 3) / 4);
@@ -160,7 +167,7 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   const int mode = (c->mode == HO_MODE_LEARNED && !c->mlp.trained) ? HO_MODE_BATCHED : c->mode;
   if (mode == HO_MODE_PLAIN) {
     // one thread per query: camera queries are laid out as 8x4 pixel tiles per warp
-    if (!a.rays) n_threads = static_cast<int64_t>((a.width + 7) / 8) * ((a.height + 3) / 4) * 32 * a.n_iso;
+    if (!a.rays && !a.views) n_threads = static_cast<int64_t>((a.width + 7) / 8) * ((a.height + 3) / 4) * 32 * a.n_iso;
     cudaError_t e;
     switch (c->N) {
       case 2: e = launch_n<2>(P, n_queries, n_threads, s, mode); break;

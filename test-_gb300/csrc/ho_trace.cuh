@@ -26,10 +26,7 @@ constexpr int kCandK = 8;
 constexpr int kStack = 64;
 constexpr int kTraceBlock = 128;  // intersect pass: 4 warps, one query each
 
-struct CamArgs {
-  float3 origin, llc, horiz, vert;
-  int width, height;
-};
+
 
 struct TraceParams {
   const BNode* __restrict__ nodes;
@@ -43,6 +40,8 @@ struct TraceParams {
   float iso[8];
   int n_iso;
   uint32_t iso_on_mask;
+  const ViewDesc* views;  // multi-view call (rays == nullptr), else nullptr
+  int n_views;
   ho_hit* __restrict__ hits;
   uint8_t* __restrict__ rgb;
   DevStats* stats;
@@ -183,31 +182,57 @@ __device__ __forceinline__ void shade(const HitState& h, float3 d, uint8_t* out)
   for (int q = 0; q < 3; ++q) out[q] = static_cast<uint8_t>(255.99f * fminf(1.0f, sqrtf(c[q])));
 }
 
-// Rays as the kernels see them: query q -> (origin, direction, isovalue index).
+// Pixel-centre ray of pixel `pix` of a pinhole camera.
+__device__ __forceinline__ void camera_ray(const CamArgs& cam, int64_t pix, float3& o, float3& d) {
+  const int x = static_cast<int>(pix % cam.width), y = static_cast<int>(pix / cam.width);
+  const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(cam.width);
+  const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(cam.height);
+  o = cam.origin;
+  d = make_float3(cam.llc.x + s * cam.horiz.x + t * cam.vert.x - o.x, cam.llc.y + s * cam.horiz.y + t * cam.vert.y - o.y,
+                  cam.llc.z + s * cam.horiz.z + t * cam.vert.z - o.z);
+  d = normalize3(d);
+}
+
+// Rays as the kernels see them: query q -> (origin, direction, isovalue,
+// isosurface on). Three layouts: explicit rays (isovalue-major over the ray
+// array), one camera (isovalue-major over its pixels), or a table of views
+// (each view's queries laid out like one camera, views back to back).
 __device__ __forceinline__ void query_ray_from(const float* __restrict__ rays, int64_t n_rays, const CamArgs& cam,
-                                               int64_t q, float3& o, float3& d, int& iso_idx) {
-  if (rays == nullptr) {
-    const int64_t npix = static_cast<int64_t>(cam.width) * cam.height;
-    iso_idx = static_cast<int>(q / npix);
-    const int64_t pix = q - static_cast<int64_t>(iso_idx) * npix;
-    const int x = static_cast<int>(pix % cam.width), y = static_cast<int>(pix / cam.width);
-    const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(cam.width);
-    const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(cam.height);
-    o = cam.origin;
-    d = make_float3(cam.llc.x + s * cam.horiz.x + t * cam.vert.x - o.x,
-                    cam.llc.y + s * cam.horiz.y + t * cam.vert.y - o.y,
-                    cam.llc.z + s * cam.horiz.z + t * cam.vert.z - o.z);
-    d = normalize3(d);
-  } else {
+                                               const float* iso_tab, uint32_t iso_mask, const ViewDesc* views,
+                                               int n_views, int64_t q, float3& o, float3& d, float& iso,
+                                               bool& iso_on) {
+  int iso_idx;
+  if (rays != nullptr) {
     iso_idx = static_cast<int>(q / n_rays);
     const float* rp = rays + 6 * (q - static_cast<int64_t>(iso_idx) * n_rays);
     o = make_float3(rp[0], rp[1], rp[2]);
     d = make_float3(rp[3], rp[4], rp[5]);
+  } else if (views != nullptr) {
+    int lo = 0, hi = n_views - 1;  // the last view whose first query <= q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (views[mid].q0 <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    const ViewDesc& v = views[lo];
+    const int64_t local = q - v.q0, npix = static_cast<int64_t>(v.cam.width) * v.cam.height;
+    iso_idx = static_cast<int>(local / npix);
+    camera_ray(v.cam, local - static_cast<int64_t>(iso_idx) * npix, o, d);
+    iso = v.iso[iso_idx];
+    iso_on = (v.iso_on_mask >> iso_idx) & 1u;
+    return;
+  } else {
+    const int64_t npix = static_cast<int64_t>(cam.width) * cam.height;
+    iso_idx = static_cast<int>(q / npix);
+    camera_ray(cam, q - static_cast<int64_t>(iso_idx) * npix, o, d);
   }
+  iso = iso_tab[iso_idx];
+  iso_on = (iso_mask >> iso_idx) & 1u;
 }
 
-__device__ __forceinline__ void query_ray(const TraceParams& P, int64_t q, float3& o, float3& d, int& iso_idx) {
-  query_ray_from(P.rays, P.n_rays, P.cam, q, o, d, iso_idx);
+__device__ __forceinline__ void query_ray(const TraceParams& P, int64_t q, float3& o, float3& d, float& iso,
+                                          bool& iso_on) {
+  query_ray_from(P.rays, P.n_rays, P.cam, P.iso, P.iso_on_mask, P.views, P.n_views, q, o, d, iso, iso_on);
 }
 
 __device__ __forceinline__ void write_result(const TraceParams& P, int64_t q, float3 d, const HitState& best,
@@ -259,10 +284,9 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
     if (item >= n_work) break;
     const int64_t q = P.work[item];
     float3 o, d;
-    int iso_idx;
-    query_ray(P, q, o, d, iso_idx);
-    const float iso = P.iso[iso_idx];
-    const bool iso_on = (P.iso_on_mask >> iso_idx) & 1u;
+    float iso;
+    bool iso_on;
+    query_ray(P, q, o, d, iso, iso_on);
     HitState best = miss_state();
     const uint32_t it0 = wu.newton + wu.face + w.newton + w.face;
     float kt = -FLT_MAX;
@@ -417,9 +441,10 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
   const int64_t wid = (static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x) >> 5;
   int64_t q;
   float3 o = make_float3(0.f, 0.f, 0.f), d = make_float3(0.f, 0.f, 1.f);
-  int iso_idx = 0;
+  float iso = 0.f;
+  bool iso_on = false;
   bool active;
-  if (P.rays == nullptr) {
+  if (P.rays == nullptr && P.views == nullptr) {
     const int tx_n = (P.cam.width + 7) >> 3, ty_n = (P.cam.height + 3) >> 2;
     const int64_t tiles = static_cast<int64_t>(tx_n) * ty_n;
     const int it = static_cast<int>(wid / tiles);
@@ -432,10 +457,10 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
     q = static_cast<int64_t>(blockIdx.x) * kTraceBlock + threadIdx.x;
     active = q < n_queries;
   }
-  if (active) query_ray(P, q, o, d, iso_idx);
+  if (active) query_ray(P, q, o, d, iso, iso_on);
   Work w;
   HitState best = miss_state();
-  if (active) best = plain_trace<N>(P, o, d, P.iso[iso_idx], (P.iso_on_mask >> iso_idx) & 1u, w);
+  if (active) best = plain_trace<N>(P, o, d, iso, iso_on, w);
   flush_work(P.stats, w, active);
   if (active) write_result(P, q, d, best, w.newton + w.face);
 }

@@ -85,6 +85,8 @@ def _load():
     L.ho_get_boxes.argtypes = [vp, vp]
     L.ho_get_hull_boxes.argtypes = [vp, vp, vp]
     L.ho_render.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp]
+    L.ho_render_views.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp]
+    L.ho_render_views_device.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp]
     L.ho_render_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp, vp]
     L.ho_intersect.argtypes = [vp, i64, vp, f32, i32, vp]
     L.ho_intersect_device.argtypes = [vp, i64, vp, f32, i32, vp, vp]
@@ -282,6 +284,43 @@ class Context:
         self._ck(lib.ho_render(self.h, C.byref(cam), _p(iso), n, width, height, int(iso_zero_disables),
                                _p(rgb) if rgb is not None else None, _p(hits) if hits is not None else None))
         return rgb, hits
+
+    @staticmethod
+    def _views(cameras, widths, heights, isovalues):
+        n = len(cameras)
+        cams = (_Camera * n)(*[c._c() for c in cameras])
+        w = np.ascontiguousarray(widths, np.int32)
+        h = np.ascontiguousarray(heights, np.int32)
+        iso = np.zeros((n, 8), np.float32)
+        n_iso = np.zeros(n, np.int32)
+        for v, vals in enumerate(isovalues):
+            vals = np.atleast_1d(np.asarray(vals, np.float32))
+            iso[v, :vals.size] = vals
+            n_iso[v] = vals.size
+        total = int((w.astype(np.int64) * h * n_iso).sum())
+        return n, cams, w, h, iso, n_iso, total
+
+    def render_views(self, cameras, widths, heights, isovalues, iso_zero_disables: bool = False,
+                     want_rgb: bool = True, want_hits: bool = False):
+        """Many views in one call (ho_render_views). isovalues[v] lists view
+        v's isovalues. Returns flat rgb (total x 3) and hits (total), and the
+        query offset of each view (n + 1 entries)."""
+        n, cams, w, h, iso, n_iso, total = self._views(cameras, widths, heights, isovalues)
+        rgb = np.zeros((total, 3), np.uint8) if want_rgb else None
+        hits = np.zeros(total, HIT_DTYPE) if want_hits else None
+        offs = np.zeros(n + 1, np.int64)
+        self._ck(lib.ho_render_views(self.h, n, C.cast(cams, C.c_void_p), _p(w), _p(h), _p(iso), _p(n_iso),
+                                     int(iso_zero_disables), _p(rgb) if rgb is not None else None,
+                                     _p(hits) if hits is not None else None, _p(offs)))
+        return rgb, hits, offs
+
+    def render_views_device(self, cameras, widths, heights, isovalues, rgb_ptr, hits_ptr, stream_ptr,
+                            iso_zero_disables: bool = False) -> np.ndarray:
+        n, cams, w, h, iso, n_iso, total = self._views(cameras, widths, heights, isovalues)
+        offs = np.zeros(n + 1, np.int64)
+        self._ck(lib.ho_render_views_device(self.h, n, C.cast(cams, C.c_void_p), _p(w), _p(h), _p(iso), _p(n_iso),
+                                            int(iso_zero_disables), rgb_ptr, hits_ptr, _p(offs), stream_ptr))
+        return offs
 
     def render_device(self, camera: Camera, isovalues, width, height, rgb_ptr, hits_ptr, stream_ptr,
                       iso_zero_disables: bool = True):

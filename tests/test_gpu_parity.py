@@ -201,3 +201,24 @@ def test_mixed_orders_match_oracle(mixed, oracle, iso_on):
     _, hp = ctx.render(cam, [iso], W, H, iso_zero_disables=True, want_rgb=False, want_hits=True)
     ctx.set_mode(hr.MODE_BATCHED)
     assert classify(h, hp[0].reshape(-1)).mean() >= 0.999
+
+
+@pytest.mark.parametrize("mode", [hr.MODE_BATCHED, hr.MODE_PLAIN])
+def test_render_views_equals_single_views(small, mode):
+    """Three views of different sizes and isovalue sets in one call equal the
+    three single-camera renders (same rays, same answers)."""
+    ctx, w, arrs, osc = small
+    ctx.set_mode(mode)
+    cams = [hr.Camera((2.5, 2.0, 1.8), (0.5, 0.5, 0.5)), hr.Camera((-1.5, 1.2, 2.2), (0.5, 0.5, 0.5), vfov_deg=45.0),
+            hr.Camera((0.5, 3.0, 0.5), (0.5, 0.5, 0.5), vup=(0.0, 0.0, 1.0))]
+    sizes = [(48, 32), (40, 40), (24, 56)]
+    isos = [[0.2], [0.0, -0.1], [0.1, 0.2, 0.3]]
+    rgb, hits, offs = ctx.render_views(cams, [s[0] for s in sizes], [s[1] for s in sizes], isos,
+                                       iso_zero_disables=True, want_hits=True)
+    assert offs[-1] == hits.size
+    for v, (cam, (W, H), iv) in enumerate(zip(cams, sizes, isos)):
+        r1, h1 = ctx.render(cam, iv, W, H, iso_zero_disables=True, want_hits=True)
+        hv = hits[offs[v]:offs[v + 1]]
+        assert np.array_equal(hv["elem"], h1.reshape(-1)["elem"]) and np.array_equal(hv["t"], h1.reshape(-1)["t"])
+        assert np.array_equal(rgb[offs[v]:offs[v + 1]], r1.reshape(-1, 3))
+    ctx.set_mode(hr.MODE_BATCHED)
