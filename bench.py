@@ -216,7 +216,7 @@ def cpu_baseline(workload, seconds, n_iso_sample=None):
 def run_reference(args, rank, world):
     import horender as hr
 
-    w = hr.WORKLOADS[args.workload]
+    w = hr.WORKLOADS[hr.MULTIVIEW[args.workload][0] if args.workload in hr.MULTIVIEW else args.workload]
     if rank != 0:
         return
     per_step = []
@@ -245,7 +245,13 @@ def run_gpu(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = hr.WORKLOADS[args.workload]
+    multi = args.workload in hr.MULTIVIEW
+    if multi:  # many views of one scene in one call
+        base, view_kw = hr.MULTIVIEW[args.workload]
+        w = hr.WORKLOADS[base]
+        cams, vw, vh, visos = hr.sphere_views(**view_kw)
+    else:
+        w = hr.WORKLOADS[args.workload]
     if args.width and args.height:
         import dataclasses
 
@@ -256,14 +262,17 @@ def run_gpu(args, rank, world):
     info = ctx.info()
     n_iso = len(w.isovalues)
     W, H = w.width, w.height
-    nq = W * H * n_iso
+    nq = sum(a * b * len(c) for a, b, c in zip(vw, vh, visos)) if multi else W * H * n_iso
     rgb = torch.empty(nq * 3, dtype=torch.uint8, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
 
     def step():
-        ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
+        if multi:
+            ctx.render_views_device(cams, vw, vh, visos, rgb.data_ptr(), None, sp)
+        else:
+            ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
 
     tuned = {}
 
@@ -306,7 +315,13 @@ def run_gpu(args, rank, world):
                  "loss_last": float(losses[-50:].mean())}
     results = {}
     codes = {"plain": hr.MODE_PLAIN, "batched": hr.MODE_BATCHED, "learned": hr.MODE_LEARNED}
-    for mode in (["plain", "batched", "learned"] if args.mode == "all" else [args.mode]):
+    if args.mode != "all":
+        modes = [args.mode]
+    elif multi:  # plain (one thread per ray, padded to the largest order) would take minutes per step here
+        modes = ["batched", "learned"]
+    else:
+        modes = ["plain", "batched", "learned"]
+    for mode in modes:
         results[mode] = timed(codes[mode])
     head = "learned" if "learned" in results else ("batched" if "batched" in results else "plain")
     total_s, st, clk = results[head]
@@ -322,19 +337,24 @@ def run_gpu(args, rank, world):
         return {"value": queries / t / 1e6, "ms_per_step": t / args.steps * 1e3, "newton_iters": stt["newton_iters"],
                 "face_iters": stt["face_iters"], "geom_evals": stt["geom_evals"]}
 
-    # roofline of the trace kernel: algorithmic FP32 flops of one launch
+    # roofline of the trace kernel: algorithmic FP32 flops of one launch. The
+    # round kernel counts its own (each evaluation at the element's order);
+    # plain mode evaluates every element at the scene's largest order.
     N = info["max_modes"]
-    flops = algorithmic_flops(st, N)
+    flops = st["round_flops"] if st.get("round_flops") else algorithmic_flops(st, N)
     achieved_tflops = flops / launch_s / 1e12
 
     # e2e: public API, host image buffer, D2H inside the timed region
-    host_rgb = torch.empty((n_iso, H, W, 3), dtype=torch.uint8).pin_memory()
+    host_rgb = torch.empty((nq, 3) if multi else (n_iso, H, W, 3), dtype=torch.uint8).pin_memory()
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     ctx.set_mode(codes[head])
     for _ in range(0 if args.no_e2e else args.steps):
-        ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
+        if multi:
+            ctx.render_views(cams, vw, vh, visos, rgb_out=host_rgb.numpy())
+        else:
+            ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = None if args.no_e2e else queries / e2e_s / 1e6
     del host_rgb
@@ -357,9 +377,12 @@ def run_gpu(args, rank, world):
         else None,
         "training": train,
         "autotune": tuned,
-        "config": {"workload": w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes", "order": w.order_max,
+        "config": {"workload": args.workload if multi else w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes",
+                   "order": w.order_max if w.order_min == w.order_max else f"P in {w.order_min}..{w.order_max}",
                    "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
-                   "rays": f"{W}x{H}", "isovalues": w.isovalues, "queries_per_step": nq,
+                   "rays": (f"{len(cams)} views on a radius-2.5 sphere, resolutions "
+                            f"{sorted(set(zip(vw, vh)))}, 1-4 isovalues each") if multi else f"{W}x{H}",
+                   "isovalues": "per view" if multi else w.isovalues, "queries_per_step": nq,
                    "l2": "flushed (256 MiB write) before every timed step",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",

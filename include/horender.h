@@ -131,6 +131,9 @@ typedef struct {
   uint64_t fp64_failed;      /* of those, failed (traced again, plain solver) */
   uint64_t fp64_failed_after_fallback;  /* plain answer failed too (kept,
                                 HO_FLAG_FP64_FAIL)                           */
+  uint64_t round_flops;      /* batched/learned: algorithmic FP32 flops of the
+                                round kernel's evaluations (at each element's
+                                order) and Newton solves                     */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

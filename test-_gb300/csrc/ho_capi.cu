@@ -138,6 +138,7 @@ int read_stats(ho_context* c) {
   s.fp64_checked = ds.c[ho::ST_CHECKED];
   s.fp64_failed = ds.c[ho::ST_CHECK_FAIL];
   s.fp64_failed_after_fallback = ds.c[ho::ST_CHECK_FINAL];
+  s.round_flops = ds.c[ho::ST_FLOPS];
   s.solve_steps = ds.c[ho::ST_STEPS];
   s.lane_steps = ds.c[ho::ST_LANES];
   if (ds.status != 0)

@@ -34,7 +34,18 @@ struct Work {
   unsigned long long cyc[4] = {0, 0, 0, 0};
   // round kernel: loop steps and busy lanes over them (counted on lane 0)
   unsigned long long steps = 0, lanes = 0;
+  // round kernel: algorithmic FP32 flops of the evaluations and solves done
+  unsigned long long flops = 0;
 };
+
+// Algorithmic flops of one sum-factorised point evaluation of `comps`
+// components (value and three partials each) at n modes per direction: the
+// 1-D basis values and derivatives (3 x 8n) plus 2(2n^3 + 3n^2 + 4n) per
+// component; and of one 3x3 Newton solve and update.
+__host__ __device__ constexpr unsigned long long eval_flops(int n, int comps) {
+  return 3ull * 8 * n + 2ull * comps * (2ull * n * n * n + 3ull * n * n + 4ull * n);
+}
+constexpr unsigned long long kSolveFlops = 60;
 
 // ---------------------------------------------------------------------------
 // 1-D Modified-A basis: phi_0 = (1-x)/2, phi_1 = (1+x)/2,

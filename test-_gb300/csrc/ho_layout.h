@@ -77,6 +77,7 @@ enum StatSlot {
   ST_CHECKED,
   ST_CHECK_FAIL,
   ST_CHECK_FINAL,
+  ST_FLOPS,
   ST_COUNT
 };
 

@@ -132,6 +132,7 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
   P.desc = nullptr;
   P.cand_e = nullptr;
   P.pred = nullptr;
+  P.pred_items = 0;
   classify_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(P, n);
   e = cudaGetLastError();
   if (e == cudaSuccess) {

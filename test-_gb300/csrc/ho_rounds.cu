@@ -269,6 +269,7 @@ static RoundParams round_params(ho_context* c, const TraceParams& P) {
   R.desc = P.desc;
   R.cand_e = P.cand_e;
   R.pred = P.pred;
+  R.pred_items = P.pred_items;
   return R;
 }
 

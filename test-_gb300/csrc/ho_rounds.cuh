@@ -105,6 +105,7 @@ struct RoundParams {
   const float* desc;
   const int32_t* cand_e;
   const float* pred;
+  unsigned pred_items;
 };
 
 // Task word: kind (3 bits) | pair (5 bits) | argument (8 bits).
@@ -424,7 +425,8 @@ __device__ __noinline__ int admit_pair(WarpSm<N>* Wp, const RoundParams* P, int 
   p.item = rp.item;
   p.elem = elem;
   int fl = (has_field ? 1 : 0) | (iso_on ? 2 : 0);
-  if (L && rp.j >= 0 && rp.j < kPredK && P->cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == elem) {
+  if (L && rp.j >= 0 && rp.j < kPredK && static_cast<unsigned>(rp.item) < P->pred_items &&
+      P->cand_e[static_cast<int64_t>(rp.item) * kPredK + rp.j] == elem) {
     const float* y = P->pred + (static_cast<int64_t>(rp.item) * kPredK + rp.j) * kMlpOut;
     p.pxi[0] = y[0]; p.pxi[1] = y[1]; p.pxi[2] = y[2];
     p.pv[0] = y[3]; p.pv[1] = y[4]; p.pv[2] = y[5];
@@ -567,6 +569,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
         const bool want_field = s.post && (s.kind != TK_FPOST || has_field);
         float4 r[4];
         eval_comps<N, true>(el.c, s.xi, want_geom ? 0 : 3, want_field ? 4 : 3, r);
+        w.flops += eval_flops(N, (want_geom ? 3 : 0) + (want_field ? 1 : 0));
         if (want_geom) {
           X = make_float3(r[0].x, r[1].x, r[2].x);
           J[0] = r[0].y; J[1] = r[0].z; J[2] = r[0].w;
@@ -594,6 +597,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
           invert3(J, K);
           if (!s.post) {
             ++w.newton;
+            w.flops += kSolveFlops;
             const float rx = X.x - (p.o[0] + s.t * p.d[0]), ry = X.y - (p.o[1] + s.t * p.d[1]),
                         rz = X.z - (p.o[2] + s.t * p.d[2]);
             const float d0 = K[0] * rx + K[1] * ry + K[2] * rz;
@@ -642,6 +646,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             s.inited = true;
           }
           ++w.face;
+          w.flops += kSolveFlops;
           const float rx = X.x - (p.o[0] + s.t * p.d[0]), ry = X.y - (p.o[1] + s.t * p.d[1]),
                       rz = X.z - (p.o[2] + s.t * p.d[2]);
           const float m = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));

@@ -54,7 +54,10 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
 // hit yet) and the network input of each (ray, candidate) pair.
 __global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16* __restrict__ X,
                                                    int32_t* __restrict__ cand_e) {
-  const unsigned n_work = *P.qcount;
+  // predictions for the first pred_items queued rays (the buffers' size); the
+  // rest start cold
+  const unsigned n_work = min(*P.qcount, P.pred_items);
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.qcount[2] = n_work;
   Work w;
   for (int64_t item = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; item < n_work;
        item += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -88,7 +91,7 @@ int finish_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lear
 // classify pass, the network (learned), the rounds and the write-out. No host
 // read-back and no allocation, so the whole sequence can be captured.
 static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool learned, int64_t n_queries, int sms) {
-  cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 2 * sizeof(unsigned), s);
+  cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 4 * sizeof(unsigned), s);
   if (e != cudaSuccess) return int(e);
   classify_kernel<<<static_cast<unsigned>((n_queries + 255) / 256), 256, 0, s>>>(P, n_queries);
   e = cudaGetLastError();
@@ -97,7 +100,7 @@ static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool l
     cand_kernel<<<sms * 8, 128, 0, s>>>(P, static_cast<__nv_bfloat16*>(c->d_feat), c->d_cand);
     e = cudaGetLastError();
     if (e != cudaSuccess) return int(e);
-    const int rc = mlp_infer(c->mlp.dev(), c->d_feat, 0, c->d_qctr, kPredK, c->d_pred, s, sms);
+    const int rc = mlp_infer(c->mlp.dev(), c->d_feat, 0, c->d_qctr + 2, kPredK, c->d_pred, s, sms);
     if (rc) return rc;
   }
   // as many rounds as the previous call needed, plus one, within the option
@@ -157,11 +160,11 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
     c->work_cap = static_cast<size_t>(n_queries);
   }
   if (!c->d_qctr) {
-    cudaError_t e = cudaMalloc(&c->d_qctr, 2 * sizeof(unsigned));
+    cudaError_t e = cudaMalloc(&c->d_qctr, 4 * sizeof(unsigned));
     if (e != cudaSuccess) return int(e);
   }
   {
-    cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 2 * sizeof(unsigned), s);
+    cudaError_t e = cudaMemsetAsync(c->d_qctr, 0, 4 * sizeof(unsigned), s);
     if (e != cudaSuccess) return int(e);
   }
   const int mode = (c->mode == HO_MODE_LEARNED && !c->mlp.trained) ? HO_MODE_BATCHED : c->mode;
@@ -189,8 +192,9 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   P.kovf = c->d_kovf;
   const bool learned = mode == HO_MODE_LEARNED;
   // allocate first: nothing enqueued below may allocate (it may be captured)
+  P.pred_items = static_cast<unsigned>(std::min<int64_t>(n_queries, kPredItemsCap));
   if (learned) {
-    const size_t rows = static_cast<size_t>(n_queries) * kPredK;
+    const size_t rows = static_cast<size_t>(P.pred_items) * kPredK;
     if (rows > c->pred_cap) {
       cudaFree(c->d_feat);
       cudaFree(c->d_pred);

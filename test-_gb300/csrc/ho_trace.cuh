@@ -23,6 +23,8 @@
 namespace ho {
 
 constexpr int kCandK = 8;
+// learned mode: predictions for at most this many queued rays per call
+constexpr int64_t kPredItemsCap = int64_t(8) << 20;
 constexpr int kStack = 64;
 constexpr int kTraceBlock = 128;  // intersect pass: 4 warps, one query each
 
@@ -48,7 +50,8 @@ struct TraceParams {
   int32_t* work;      // queue of query indices that meet at least one box
   float2* kbuf;       // [queue slot][kCandK] first ordered candidates (t entry, element bits)
   uint8_t* kovf;      // [queue slot] more candidates than kCandK were in range
-  unsigned* qcount;   // queue length (written by the classify pass)
+  unsigned* qcount;   // [0] queue length (classify pass), [2] rays with predictions
+  unsigned pred_items;  // learned: predictions exist for queue items below this
   unsigned* qnext;    // next queue item to take (intersect pass)
   // learned mode
   const float* desc;      // element descriptors (scale k at [45])
@@ -148,7 +151,7 @@ __device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool act
   // warp-aggregated counters
   unsigned long long v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled,
                                     w.nodes, w.accepted, w.rejected, w.restarts, w.cyc[0], w.cyc[1], w.cyc[2],
-                                    w.cyc[3], w.steps, w.lanes, 0ull, 0ull, 0ull, 0ull, 0ull};
+                                    w.cyc[3], w.steps, w.lanes, 0ull, 0ull, 0ull, 0ull, 0ull, w.flops};
 #pragma unroll
   for (int s = 0; s < ST_COUNT; ++s) {
     unsigned long long x = v[s];

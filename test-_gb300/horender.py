@@ -63,7 +63,7 @@ class _Stats(C.Structure):
         ("max_modes", C.c_int32), ("status", C.c_int32), ("phase_cycles", C.c_uint64 * 4),
         ("rounds", C.c_uint64), ("round_pairs", C.c_uint64), ("solve_steps", C.c_uint64),
         ("lane_steps", C.c_uint64), ("graph", C.c_uint64), ("fp64_checked", C.c_uint64),
-        ("fp64_failed", C.c_uint64), ("fp64_failed_after_fallback", C.c_uint64)]
+        ("fp64_failed", C.c_uint64), ("fp64_failed_after_fallback", C.c_uint64), ("round_flops", C.c_uint64)]
 
 
 def _load():
@@ -301,12 +301,16 @@ class Context:
         return n, cams, w, h, iso, n_iso, total
 
     def render_views(self, cameras, widths, heights, isovalues, iso_zero_disables: bool = False,
-                     want_rgb: bool = True, want_hits: bool = False):
+                     want_rgb: bool = True, want_hits: bool = False, rgb_out: np.ndarray | None = None):
         """Many views in one call (ho_render_views). isovalues[v] lists view
         v's isovalues. Returns flat rgb (total x 3) and hits (total), and the
         query offset of each view (n + 1 entries)."""
         n, cams, w, h, iso, n_iso, total = self._views(cameras, widths, heights, isovalues)
-        rgb = np.zeros((total, 3), np.uint8) if want_rgb else None
+        if rgb_out is not None:
+            assert rgb_out.dtype == np.uint8 and rgb_out.size == total * 3 and rgb_out.flags.c_contiguous
+            rgb = rgb_out
+        else:
+            rgb = np.zeros((total, 3), np.uint8) if want_rgb else None
         hits = np.zeros(total, HIT_DTYPE) if want_hits else None
         offs = np.zeros(n + 1, np.int64)
         self._ck(lib.ho_render_views(self.h, n, C.cast(cams, C.c_void_p), _p(w), _p(h), _p(iso), _p(n_iso),
@@ -415,6 +419,38 @@ def save_ppm(rgb: np.ndarray, path: str):
     rc = lib.ho_save_ppm(_p(rgb), w, h, str(path).encode())
     if rc != HO_OK:
         raise HoError(rc, f"cannot write {path}")
+
+
+RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+ISO_POOL = [-0.3, -0.2, -0.1, 0.0, 0.1, 0.2, 0.3]
+
+
+def sphere_views(n_views: int = 64, radius: float = 2.5, centre=(0.5, 0.5, 0.5), seed: int = 7,
+                 shrink: int = 1) -> tuple[list, list, list, list]:
+    """n seeded camera views on a Fibonacci sphere around the cube centre, each
+    with a resolution drawn from RESOLUTIONS (divided by `shrink`) and 1-4
+    distinct isovalues drawn from ISO_POOL. Returns cameras, widths, heights,
+    isovalue lists (the uneven multi-view workload)."""
+    rng = np.random.default_rng(seed)
+    golden = np.pi * (3.0 - np.sqrt(5.0))
+    cams, ws, hs, isos = [], [], [], []
+    for i in range(n_views):
+        y = 1.0 - 2.0 * (i + 0.5) / n_views
+        r = np.sqrt(max(0.0, 1.0 - y * y))
+        phi = golden * i
+        pos = tuple(float(c + radius * v) for c, v in zip(centre, (r * np.cos(phi), y, r * np.sin(phi))))
+        vup = (0.0, 0.0, 1.0) if abs(y) > 0.99 else (0.0, 1.0, 0.0)
+        cams.append(Camera(pos, tuple(centre), vup, 60.0))
+        wdt, hgt = RESOLUTIONS[int(rng.integers(len(RESOLUTIONS)))]
+        ws.append(max(1, wdt // shrink))
+        hs.append(max(1, hgt // shrink))
+        k = int(rng.integers(1, 5))
+        isos.append(sorted(float(v) for v in rng.choice(ISO_POOL, size=k, replace=False)))
+    return cams, ws, hs, isos
+
+
+# multi-view workloads: scene workload + views
+MULTIVIEW = {"views64": ("hex48_mixed", dict(n_views=64, seed=7))}
 
 
 def workload_context(name: str, device: int = 0, build: bool = True) -> tuple[Context, Workload]:

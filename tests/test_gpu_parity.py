@@ -222,3 +222,27 @@ def test_render_views_equals_single_views(small, mode):
         assert np.array_equal(hv["elem"], h1.reshape(-1)["elem"]) and np.array_equal(hv["t"], h1.reshape(-1)["t"])
         assert np.array_equal(rgb[offs[v]:offs[v + 1]], r1.reshape(-1, 3))
     ctx.set_mode(hr.MODE_BATCHED)
+
+
+def test_uneven_multiview_matches_oracle(mixed, oracle):
+    """The uneven-work configuration at small scale: mixed orders, 8 seeded
+    sphere views of different resolutions and 1-4 isovalues each, all in one
+    call, batched and learned, against the oracle view by view."""
+    ctx, arrs, osc = mixed
+    cams, ws, hs, isos = hr.sphere_views(n_views=8, seed=3, shrink=16)
+    ctx.train_mlp(n_samples=200_000, steps=300, batch=2048, lr=2e-3, seed=5)
+    for mode in (hr.MODE_BATCHED, hr.MODE_LEARNED):
+        ctx.set_mode(mode)
+        _, hits, offs = ctx.render_views(cams, ws, hs, isos, want_rgb=False, want_hits=True)
+        bad = total = 0
+        for v in range(len(cams)):
+            rays = oracle.camera_rays(cams[v].lookfrom, cams[v].lookat, cams[v].vup, cams[v].vfov_deg, ws[v], hs[v])
+            npix = ws[v] * hs[v]
+            for k, iso in enumerate(isos[v]):
+                h = hits[offs[v] + k * npix:offs[v] + (k + 1) * npix]
+                ref, _ = osc.trace(rays, iso, True, precision=32)
+                bad += int((~classify(h, ref)).sum())
+                total += npix
+        print(f"uneven multi-view, mode {mode}: {total} queries, {bad} differ from the oracle")
+        assert bad <= max(2, int(0.005 * total))
+    ctx.set_mode(hr.MODE_BATCHED)
