@@ -110,13 +110,13 @@ def flops_field(n):  # u and grad: (2n^3 + 3n^2 + 4n) FMA + basis (3 x 8n)
     return 2 * (2 * n**3 + 3 * n**2 + 4 * n) + 3 * 8 * n
 
 
-# DRAM bytes (read + write) of one intersect launch, from an ncu capture of the
-# same workload (dram__bytes_read.sum + dram__bytes_write.sum; the capture
-# command is in profiles/isect_learned_hex32_p6.md). Keyed by workload, image
-# size and mode; absent -> null.
+# DRAM bytes (read + write) per round-kernel launch, averaged over the 12
+# launches of one step, from an ncu capture of the same workload
+# (dram__bytes_read.sum + dram__bytes_write.sum; the capture command is in
+# profiles/launches_hex32_p6.md). Keyed by workload, image size and mode;
+# absent -> null.
 ISECT_TRAFFIC = {
-    ("hex32_p6", 1920, 1080, "learned"): 159.22e6 + 4.99e6,
-    ("hex32_p6", 480, 272, "learned"): 28.74e6 + 1.60e6,
+    ("hex32_p6", 1920, 1080, "learned"): (432.09e6 + 26.47e6) / 12,
 }
 
 
@@ -281,6 +281,10 @@ def run_gpu(args, rank, world):
         if mode != hr.MODE_PLAIN:  # the round kernel's element batch size, picked on this workload
             tuned[{hr.MODE_BATCHED: "batched", hr.MODE_LEARNED: "learned"}[mode]] = ctx.autotune(
                 w.camera, w.isovalues, W, H)
+        # CUDA events around each round's intersection launches (event nodes of the call's graph)
+        ctx.set_option(hr.OPT_TIME_ROUNDS, 0 if mode == hr.MODE_PLAIN else 1)
+        keys = ("round_kernel_ns", "round_launches", "round_flops", "kernel_launches")
+        per = dict.fromkeys(keys, 0)
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
                 flush.zero_()
@@ -300,9 +304,13 @@ def run_gpu(args, rank, world):
                     step()
                     b.record(stream)
                     evs.append((a, b))
+                    s_step = ctx.stats()  # the call has synchronised; this reads its host copy
+                    for k in keys:
+                        per[k] += s_step[k]
             torch.cuda.synchronize()
         barrier(world)
         total = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / 1e3, world)
+        st = dict(st, timed=per)
         return total, st, clk
 
     train = None
@@ -337,12 +345,24 @@ def run_gpu(args, rank, world):
         return {"value": queries / t / 1e6, "ms_per_step": t / args.steps * 1e3, "newton_iters": stt["newton_iters"],
                 "face_iters": stt["face_iters"], "geom_evals": stt["geom_evals"]}
 
-    # roofline of the trace kernel: algorithmic FP32 flops of one launch. The
-    # round kernel counts its own (each evaluation at the element's order);
-    # plain mode evaluates every element at the scene's largest order.
+    # roofline of the intersection kernel. Batched / learned: the round kernel
+    # counts its own algorithmic flops (each evaluation at the element's order)
+    # and CUDA events around its launches give its device time over the timed
+    # steps. Plain: one launch per step, flops from the work counters at the
+    # scene's largest order, over the step time.
     N = info["max_modes"]
-    flops = st["round_flops"] if st.get("round_flops") else algorithmic_flops(st, N)
-    achieved_tflops = flops / launch_s / 1e12
+    tm = st["timed"]
+    if head != "plain" and tm["round_kernel_ns"] > 0 and tm["round_launches"] > 0:
+        n_launch = tm["round_launches"]
+        flops = tm["round_flops"] / n_launch
+        kernel_s = tm["round_kernel_ns"] * 1e-9 / n_launch
+        kernel_name = "round_kernel"
+    else:
+        n_launch = args.steps
+        flops = algorithmic_flops(st, N)
+        kernel_s = launch_s
+        kernel_name = "plain_kernel"
+    achieved_tflops = flops / kernel_s / 1e12
 
     # e2e: public API, host image buffer, D2H inside the timed region
     host_rgb = torch.empty((nq, 3) if multi else (n_iso, H, W, 3), dtype=torch.uint8).pin_memory()
@@ -389,10 +409,12 @@ def run_gpu(args, rank, world):
                      "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,
                      "traffic": ISECT_TRAFFIC.get((w.name, W, H, head)),
                      "peak_source": "FP32 FMA loop measured in this run (peaks file has HBM and bf16 only)",
-                     "flops_per_launch": flops},
+                     "kernel": kernel_name, "flops_per_launch": flops, "launches": n_launch,
+                     "ms_per_launch": kernel_s * 1e3,
+                     "share_of_step": kernel_s * n_launch / total_s},
         "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4 * n_iso,
                                          "d2h_bytes_per_step": nq * 3},
-        "gpu_launches": args.steps * {"learned": 4, "batched": 2, "plain": 1}[head],
+        "gpu_launches": tm["kernel_launches"],
         "clocks": clk.summary(),
         "work": st,
         "scene": info,

@@ -134,6 +134,11 @@ typedef struct {
   uint64_t round_flops;      /* batched/learned: algorithmic FP32 flops of the
                                 round kernel's evaluations (at each element's
                                 order) and Newton solves                     */
+  uint64_t kernel_launches;  /* kernels the last trace call launched (graph
+                                nodes included)                              */
+  uint64_t round_kernel_ns;  /* HO_OPT_TIME_ROUNDS: device time of the round
+                                kernels' launches (CUDA events), else 0      */
+  uint64_t round_launches;   /* HO_OPT_TIME_ROUNDS: round kernel launches     */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */
@@ -260,11 +265,16 @@ int ho_set_mode(ho_context* ctx, int mode);
  * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
  *                     default: the kernel's pair slots, 16 up to 7 modes per
  *                     direction, 12 at 8, 8 at 9); ho_autotune picks it.
+ * HO_OPT_TIME_ROUNDS  0 (default); 1: a pair of CUDA events brackets each
+ *                     round's intersection launches (event nodes of the graph)
+ *                     and ho_stats.round_kernel_ns / round_launches report
+ *                     their device time.
  * HO_ERR_ARG for an unknown option, HO_ERR_RANGE for a value out of range. */
 #define HO_OPT_GRAPH 1
 #define HO_OPT_ROUNDS 2
 #define HO_OPT_ROUND_CHUNK 3
 #define HO_OPT_FP64_CHECK 4
+#define HO_OPT_TIME_ROUNDS 5
 int ho_set_option(ho_context* ctx, int option, int64_t value);
 int ho_get_option(ho_context* ctx, int option, int64_t* value);
 

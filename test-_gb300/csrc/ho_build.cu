@@ -263,26 +263,45 @@ __global__ void __launch_bounds__(kSortTile) radix_hist_kernel(const uint32_t* _
   hist[static_cast<int64_t>(threadIdx.x) * n_tiles + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// Exclusive scan of len values with one block of 1024 threads.
+// Exclusive scan of len values with one block of 1024 threads, in tiles of
+// 4096 (4 consecutive values per thread, warp shuffles, then the 32 warp
+// totals), carrying the running total from tile to tile.
 __global__ void __launch_bounds__(1024) scan_kernel(uint32_t* __restrict__ data, int64_t len) {
-  __shared__ uint32_t part[1024];
-  const int64_t per = (len + 1023) / 1024;
-  const int64_t b = threadIdx.x * per, e = min(len, b + per);
-  uint32_t s = 0;
-  for (int64_t i = b; i < e; ++i) s += data[i];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+  __shared__ uint32_t wsum[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t carry = 0;
+  for (int64_t base = 0; base < len; base += 4096) {
+    const int64_t i0 = base + static_cast<int64_t>(threadIdx.x) * 4;
+    uint32_t v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = i0 + k < len ? data[i0 + k] : 0u;
+    const uint32_t t = v[0] + v[1] + v[2] + v[3];
+    uint32_t x = t;  // inclusive scan over the warp
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
     __syncthreads();
-    part[threadIdx.x] += v;
+    if (wid == 0) {
+      uint32_t ws = wsum[lane];
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, ws, off);
+        if (lane >= off) ws += y;
+      }
+      wsum[lane] = ws;
+    }
     __syncthreads();
-  }
-  uint32_t run = part[threadIdx.x] - s;
-  for (int64_t i = b; i < e; ++i) {
-    const uint32_t v = data[i];
-    data[i] = run;
-    run += v;
+    uint32_t run = carry + (wid > 0 ? wsum[wid - 1] : 0u) + (x - t);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (i0 + k < len) data[i0 + k] = run;
+      run += v[k];
+    }
+    carry += wsum[31];
+    __syncthreads();  // every thread has read wsum before the next tile writes it
   }
 }
 

@@ -141,6 +141,18 @@ int read_stats(ho_context* c) {
   s.round_flops = ds.c[ho::ST_FLOPS];
   s.solve_steps = ds.c[ho::ST_STEPS];
   s.lane_steps = ds.c[ho::ST_LANES];
+  s.kernel_launches = static_cast<uint64_t>(c->launches);
+  s.round_kernel_ns = 0;
+  s.round_launches = 0;
+  for (int k = 0; k + 1 < c->round_events_used; k += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->round_events[k], c->round_events[k + 1]) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, HO_ERR_CUDA, "round timing events could not be read");
+    }
+    s.round_kernel_ns += static_cast<uint64_t>(static_cast<double>(ms) * 1e6 + 0.5);
+    s.round_launches += static_cast<uint64_t>(__builtin_popcount(c->orders));
+  }
   if (ds.status != 0)
     return fail(c, HO_ERR_DEVICE, "kernel reported status " + std::to_string(ds.status) +
                                       (ds.status & ho::kStatusStackOverflow ? " (traversal stack overflow)" : "") +
@@ -194,6 +206,7 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->rounds.ctr);
     cudaFree(c->rounds.fail);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    for (cudaEvent_t ev : c->round_events) cudaEventDestroy(ev);
     cudaFree(c->d_feat);
     cudaFree(c->d_pred);
     cudaFree(c->d_cand);
@@ -568,6 +581,10 @@ int ho_set_option(ho_context* c, int option, int64_t value) {
       if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_FP64_CHECK takes 0 or 1");
       c->fp64_check = value == 1;
       return HO_OK;
+    case HO_OPT_TIME_ROUNDS:
+      if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_TIME_ROUNDS takes 0 or 1");
+      c->time_rounds = value == 1;
+      return HO_OK;
     default:
       return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
@@ -578,6 +595,7 @@ int ho_get_option(ho_context* c, int option, int64_t* value) {
   switch (option) {
     case HO_OPT_GRAPH: *value = c->use_graph ? 1 : 0; return HO_OK;
     case HO_OPT_FP64_CHECK: *value = c->fp64_check ? 1 : 0; return HO_OK;
+    case HO_OPT_TIME_ROUNDS: *value = c->time_rounds ? 1 : 0; return HO_OK;
     case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
     case HO_OPT_ROUND_CHUNK: *value = c->round_chunk > 0 ? c->round_chunk : ho::round_slots(c->N > 0 ? c->N : 2); return HO_OK;
     default: return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));

@@ -49,24 +49,43 @@ __device__ __forceinline__ void basis_val64(double x, double (&a)[N]) {
   }
 }
 
-// Value of one coefficient block (rows padded to row_stride(N)) in FP64.
+// Value of one coefficient block (rows padded to row_stride(N), a multiple of
+// 4 floats, so a row is RS/4 aligned float4 loads) in FP64. The rows of one k
+// are independent and unrolled; each row sums even and odd terms separately
+// to halve the dependent FMA chain.
 template <int N>
 __device__ double value64(const float* __restrict__ blk, const double (&ar)[N], const double (&as)[N],
                           const double (&at)[N]) {
   constexpr int RS = row_stride(N);
+  static_assert(RS % 4 == 0, "rows are whole float4s");
   double v = 0.0;
 #pragma unroll 1
   for (int k = 0; k < N; ++k) {
     double q = 0.0;
-#pragma unroll 1
-    for (int j = 0; j < N; ++j) {
-      const float* row = blk + (k * N + j) * RS;
-      double sum = 0.0;
 #pragma unroll
-      for (int i = 0; i < N; ++i) sum = fma(static_cast<double>(__ldg(row + i)), ar[i], sum);
-      q = fma(sum, as[j], q);
+    for (int j = 0; j < N; ++j) {
+      const float4* row = reinterpret_cast<const float4*>(blk + (k * N + j) * RS);
+      float c[RS];
+#pragma unroll
+      for (int i4 = 0; i4 < RS / 4; ++i4) {
+        const float4 t4 = __ldg(row + i4);
+        c[4 * i4] = t4.x;
+        c[4 * i4 + 1] = t4.y;
+        c[4 * i4 + 2] = t4.z;
+        c[4 * i4 + 3] = t4.w;
+      }
+      double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+      for (int i = 0; i < N; i += 2) s0 = fma(static_cast<double>(c[i]), ar[i], s0);
+#pragma unroll
+      for (int i = 1; i < N; i += 2) s1 = fma(static_cast<double>(c[i]), ar[i], s1);
+      q = fma(s0 + s1, as[j], q);
     }
-    v = fma(q, at[k], v);
+    double atk = 0.0;  // at[k] by selection: the array stays in registers
+#pragma unroll
+    for (int kk = 0; kk < N; ++kk)
+      if (kk == k) atk = at[kk];
+    v = fma(q, atk, v);
   }
   return v;
 }

@@ -157,6 +157,10 @@ struct ho_context {
   // batched / learned engine options (ho_set_option)
   int round_chunk = 0;       // pairs per element batch (0: the kernel's pair slots)
   int round_count = 16;      // rounds enqueued before the completion check (at most)
+  int64_t launches = 0;      // kernels enqueued by the last trace call
+  bool time_rounds = false;  // event pairs around each round's intersection launches
+  std::vector<cudaEvent_t> round_events;
+  int round_events_used = 0;  // events recorded by the last trace call
   int rounds_needed = 0;     // non-empty rounds of the previous batched / learned call
   bool use_graph = true;     // run a call's launches as one CUDA graph
   bool fp64_check = true;    // FP64 residual check + plain fallback of the hits

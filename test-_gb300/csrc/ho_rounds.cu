@@ -224,6 +224,7 @@ int prepare_rounds(ho_context* c, int64_t n_cap) {
 static int enqueue_check(ho_context* c, const TraceParams& P, const RoundParams& R, cudaStream_t s, int64_t n_cap) {
   if (!c->fp64_check) return 0;
   RT_TRY(cudaMemsetAsync(c->rounds.ctr + 3, 0, sizeof(unsigned), s));
+  c->launches += 2;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -273,6 +274,30 @@ static RoundParams round_params(ho_context* c, const TraceParams& P) {
   return R;
 }
 
+// Records an event on s; inside a stream capture the event becomes an event
+// record node of the graph, so its time is taken when the graph runs.
+static cudaError_t record_event(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
+  if (e != cudaSuccess) return e;
+  return cudaEventRecordWithFlags(ev, s, cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                               : cudaEventRecordDefault);
+}
+
+// The next pair of timing events of this call (created on first use).
+static cudaError_t next_events(ho_context* c, cudaEvent_t* a, cudaEvent_t* b) {
+  while (static_cast<int>(c->round_events.size()) < c->round_events_used + 2) {
+    cudaEvent_t ev = nullptr;
+    const cudaError_t e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return e;
+    c->round_events.push_back(ev);
+  }
+  *a = c->round_events[c->round_events_used];
+  *b = c->round_events[c->round_events_used + 1];
+  c->round_events_used += 2;
+  return cudaSuccess;
+}
+
 // One round: gather each ray's next pair, bucket by element, intersect. Every
 // launch has a fixed size and reads its counts on the device, so rounds can
 // be enqueued (and captured) without reading anything back.
@@ -296,7 +321,13 @@ static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams&
   round_batch_kernel<<<ge, 256, 0, s>>>(rb.ecount, rb.eoff, c->d_cord, n_elem, c->round_chunk,
                                         const_cast<RoundBatch*>(R.batches), rb.ctr);
   RT_TRY(cudaGetLastError());
+  c->launches += 6 + __builtin_popcount(c->orders);
   // one launch per element order present in the scene
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  if (c->time_rounds) {
+    RT_TRY(next_events(c, &t0, &t1));
+    RT_TRY(record_event(t0, s));
+  }
   cudaError_t e = cudaSuccess;
   for (int n = kMinModes; n <= kMaxModes && e == cudaSuccess; ++n) {
     if (!((c->orders >> n) & 1u)) continue;
@@ -317,6 +348,7 @@ static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams&
     }
   }
   RT_TRY(e);
+  if (t1) RT_TRY(record_event(t1, s));
   return 0;
 }
 
@@ -326,6 +358,7 @@ int enqueue_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lea
   const unsigned gi = static_cast<unsigned>((n_cap + 255) / 256);
   round_init_kernel<<<gi, 256, 0, s>>>(R.state, P.kovf, P.qcount);
   RT_TRY(cudaGetLastError());
+  c->launches += 2;  // init and finish
   for (int r = 0; r < rounds; ++r) {
     const int rc = enqueue_round(c, P, R, s, learned, n_cap);
     if (rc) return rc;
@@ -361,6 +394,7 @@ int finish_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lear
     if (rc) return rc;
     round_finish_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P, R.state);
     RT_TRY(cudaGetLastError());
+    ++c->launches;
   }
   return 0;
 }

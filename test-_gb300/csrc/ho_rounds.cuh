@@ -182,8 +182,18 @@ struct LaneSolve {
   float t;    // inverse map: the sample's t; face Newton: tau
   int it, cap;
   bool warm, post, inited;
-  float prev;
+  float prev;  // face Newton: residual of the last iteration
 };
+
+// Every inverse-map iteration of an isosurface solve also evaluates the field
+// (value and xi-gradient) at its point. When the step converges (all
+// components below 1e-5), the field at the converged point follows from
+// these to first order: u(xi - step) = u(xi) - grad u . step, with an error
+// of O(|step|^2 |d2u|), below 1e-9 here. The reference evaluates the field
+// once more at the converged point instead. A warp pays for its slowest lane,
+// and that extra evaluation was one more 4-component step on some lane of
+// nearly every warp step; the field's fourth component costs the warp the
+// same whether one lane or all evaluate it.
 
 __device__ __forceinline__ void push_task(unsigned* tail, uint16_t* ring, int cap, uint32_t w) {
   const unsigned s = atomicAdd(tail, 1u);
@@ -564,9 +574,11 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
       float J[9];
       float u = 0.f;
       float3 gr = make_float3(0.f, 0.f, 0.f);
+      // inverse-map iteration of an isosurface solve: the field comes with it
+      const bool ahead = (s.kind == TK_SAMPLE || s.kind == TK_REFINE) && !s.post;
       if (act) {
         const bool want_geom = s.kind != TK_IPOST;
-        const bool want_field = s.post && (s.kind != TK_FPOST || has_field);
+        const bool want_field = (s.post && (s.kind != TK_FPOST || has_field)) || ahead;
         float4 r[4];
         eval_comps<N, true>(el.c, s.xi, want_geom ? 0 : 3, want_field ? 4 : 3, r);
         w.flops += eval_flops(N, (want_geom ? 3 : 0) + (want_field ? 1 : 0));
@@ -607,9 +619,21 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             s.xi.y -= d1;
             s.xi.z -= d2;
             ++s.it;
-            if (fabsf(d0) < 1e-5f && fabsf(d1) < 1e-5f && fabsf(d2) < 1e-5f) s.post = true;
-            else if (!(fabsf(d0) + fabsf(d1) + fabsf(d2) < FLT_MAX)) end = 2;
-            else if (s.it >= s.cap) end = 2;
+            if (fabsf(d0) < 1e-5f && fabsf(d1) < 1e-5f && fabsf(d2) < 1e-5f) {
+              if (ahead) {  // value and gradient at the converged point, first order
+                sg = make_float3(K[0] * gr.x + K[3] * gr.y + K[6] * gr.z, K[1] * gr.x + K[4] * gr.y + K[7] * gr.z,
+                                 K[2] * gr.x + K[5] * gr.y + K[8] * gr.z);
+                sf = (u - (gr.x * d0 + gr.y * d1 + gr.z * d2)) - p.iso;
+                sdf = sg.x * p.d[0] + sg.y * p.d[1] + sg.z * p.d[2];
+                end = 1;
+              } else {
+                s.post = true;
+              }
+            } else if (!(fabsf(d0) + fabsf(d1) + fabsf(d2) < FLT_MAX)) {
+              end = 2;
+            } else if (s.it >= s.cap) {
+              end = 2;
+            }
           } else {
             sg = make_float3(K[0] * gr.x + K[3] * gr.y + K[6] * gr.z, K[1] * gr.x + K[4] * gr.y + K[7] * gr.z,
                              K[2] * gr.x + K[5] * gr.y + K[8] * gr.z);

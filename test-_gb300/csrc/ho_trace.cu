@@ -96,7 +96,9 @@ static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool l
   classify_kernel<<<static_cast<unsigned>((n_queries + 255) / 256), 256, 0, s>>>(P, n_queries);
   e = cudaGetLastError();
   if (e != cudaSuccess) return int(e);
+  ++c->launches;
   if (learned) {
+    c->launches += 2;
     cand_kernel<<<sms * 8, 128, 0, s>>>(P, static_cast<__nv_bfloat16*>(c->d_feat), c->d_cand);
     e = cudaGetLastError();
     if (e != cudaSuccess) return int(e);
@@ -110,6 +112,8 @@ static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool l
 
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   c->last_graph = false;
+  c->launches = 0;
+  c->round_events_used = 0;
   TraceParams P;
   P.nodes = c->d_nodes;
   P.rec = c->d_rec;
@@ -183,6 +187,7 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
       case 9: e = launch_n<9>(P, n_queries, n_threads, s, mode); break;
       default: return int(cudaErrorInvalidValue);
     }
+    c->launches = 1;
     return int(e);
   }
   P.work = c->d_work;

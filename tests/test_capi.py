@@ -106,13 +106,16 @@ def test_engine_options():
         assert ctx.get_option(hr.OPT_ROUNDS) == 16
         assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 16
         assert ctx.get_option(hr.OPT_FP64_CHECK) == 1
+        assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 0
+        ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
+        assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 1
         ctx.set_option(hr.OPT_GRAPH, 0)
         ctx.set_option(hr.OPT_ROUNDS, 3)
         ctx.set_option(hr.OPT_ROUND_CHUNK, 200)
         assert (ctx.get_option(hr.OPT_GRAPH), ctx.get_option(hr.OPT_ROUNDS), ctx.get_option(hr.OPT_ROUND_CHUNK)) == (
             0, 3, 200)
         for opt, bad in ((hr.OPT_GRAPH, 2), (hr.OPT_ROUNDS, 0), (hr.OPT_ROUNDS, 257), (hr.OPT_ROUND_CHUNK, 0),
-                         (hr.OPT_ROUND_CHUNK, 4097)):
+                         (hr.OPT_ROUND_CHUNK, 4097), (hr.OPT_TIME_ROUNDS, 2)):
             with pytest.raises(hr.HoError) as ei:
                 ctx.set_option(opt, bad)
             assert ei.value.code == -7

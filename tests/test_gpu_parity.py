@@ -117,7 +117,20 @@ def test_graph_rounds_and_chunks_give_the_same_hits(small):
     ctx.set_option(hr.OPT_ROUND_CHUNK, 5)
     h3, s3 = run()
     ctx.set_option(hr.OPT_ROUND_CHUNK, 16)
-    for h, s in ((h1, s1), (h2, s2), (h3, s3)):
+    # event timing of the round kernels, inside the graph and direct
+    ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
+    h4, s4 = run()
+    assert s4["graph"] == 1 and s4["round_kernel_ns"] > 0 and s4["round_launches"] >= s4["rounds"]
+    # classify, init, finish, check + fallback, and per round 6 set-up kernels + 1 round kernel
+    assert s4["kernel_launches"] >= 5 + 7 * s4["round_launches"]
+    ctx.set_option(hr.OPT_GRAPH, 0)
+    h5, s5 = run()
+    assert s5["graph"] == 0 and s5["round_kernel_ns"] > 0
+    ctx.set_option(hr.OPT_GRAPH, 1)
+    ctx.set_option(hr.OPT_TIME_ROUNDS, 0)
+    h6, s6 = run()
+    assert s6["round_kernel_ns"] == 0 and s6["round_launches"] == 0
+    for h, s in ((h1, s1), (h2, s2), (h3, s3), (h4, s4), (h5, s5), (h6, s6)):
         assert np.array_equal(h["kind"], h0["kind"]) and np.array_equal(h["elem"], h0["elem"])
         assert np.array_equal(h["face"], h0["face"]) and np.array_equal(h["t"], h0["t"])
         assert (s["rounds"], s["round_pairs"], s["newton_iters"], s["face_iters"]) == (
