@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--tensor", type=int, default=0, choices=[0, 1],
+                    help="1: tensor-core round kernel (orders up to 8), 0: FP32 CUDA-core round kernel")
     ap.add_argument("--mode", default="all", choices=["all", "plain", "batched", "learned"],
                     help="learned: learned-init + batched (the headline); batched: the same kernels with cold "
                          "starts; plain: one thread per ray, the reference algorithm's structure")
@@ -259,6 +261,7 @@ def run_gpu(args, rank, world):
     ctx = hr.Context(local)
     ctx.generate_synthetic(**w.synth())
     ctx.build_bvh()
+    ctx.set_option(hr.OPT_TENSOR, args.tensor)
     info = ctx.info()
     n_iso = len(w.isovalues)
     W, H = w.width, w.height
@@ -404,6 +407,8 @@ def run_gpu(args, rank, world):
                             f"{sorted(set(zip(vw, vh)))}, 1-4 isovalues each") if multi else f"{W}x{H}",
                    "isovalues": "per view" if multi else w.isovalues, "queries_per_step": nq,
                    "l2": "flushed (256 MiB write) before every timed step",
+                   "round_kernel": ("tcgen05 TF32 hi/lo MMAs + FP32 (orders <= 8)" if args.tensor
+                                    else "FP32 CUDA cores"),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,

@@ -263,8 +263,18 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     again by the plain solver (HO_FLAG_FALLBACK), and is
  *                     flagged HO_FLAG_FP64_FAIL if that fails too; 0: off.
  * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
- *                     default: the kernel's pair slots, 16 up to 7 modes per
- *                     direction, 12 at 8, 8 at 9); ho_autotune picks it.
+ *                     default: the kernel's pair slots, 16 per warp up to 7
+ *                     modes per direction, 12 at 8, 8 at 9, times 4 warps in
+ *                     the tensor-core form); ho_autotune picks it.
+ * HO_OPT_TENSOR      0 (default): the FP32 CUDA-core round kernel for every
+ *                     order; 1: elements of up to 8 modes per direction are
+ *                     intersected by the tensor-core round kernel (tcgen05
+ *                     TF32 MMAs, split into hi + lo parts, for the first
+ *                     contraction; one CTA per element batch). The
+ *                     tensor-core form is slower on the benchmark scenes: its
+ *                     accumulators take 416 of an SM's 512 tensor-memory
+ *                     columns, so one CTA of 4 warps runs per SM, in lockstep,
+ *                     and its steps are latency-bound.
  * HO_OPT_TIME_ROUNDS  0 (default); 1: a pair of CUDA events brackets each
  *                     round's intersection launches (event nodes of the graph)
  *                     and ho_stats.round_kernel_ns / round_launches report
@@ -275,6 +285,7 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_ROUND_CHUNK 3
 #define HO_OPT_FP64_CHECK 4
 #define HO_OPT_TIME_ROUNDS 5
+#define HO_OPT_TENSOR 6
 int ho_set_option(ho_context* ctx, int option, int64_t value);
 int ho_get_option(ho_context* ctx, int option, int64_t* value);
 

@@ -585,6 +585,10 @@ int ho_set_option(ho_context* c, int option, int64_t value) {
       if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_TIME_ROUNDS takes 0 or 1");
       c->time_rounds = value == 1;
       return HO_OK;
+    case HO_OPT_TENSOR:
+      if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_TENSOR takes 0 or 1");
+      c->use_tc = value == 1;
+      return HO_OK;
     default:
       return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
@@ -596,8 +600,11 @@ int ho_get_option(ho_context* c, int option, int64_t* value) {
     case HO_OPT_GRAPH: *value = c->use_graph ? 1 : 0; return HO_OK;
     case HO_OPT_FP64_CHECK: *value = c->fp64_check ? 1 : 0; return HO_OK;
     case HO_OPT_TIME_ROUNDS: *value = c->time_rounds ? 1 : 0; return HO_OK;
+    case HO_OPT_TENSOR: *value = c->use_tc ? 1 : 0; return HO_OK;
     case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
-    case HO_OPT_ROUND_CHUNK: *value = c->round_chunk > 0 ? c->round_chunk : ho::round_slots(c->N > 0 ? c->N : 2); return HO_OK;
+    case HO_OPT_ROUND_CHUNK:
+      *value = c->round_chunk > 0 ? c->round_chunk : ho::round_batch_default(c->N > 0 ? c->N : 2, c->use_tc);
+      return HO_OK;
     default: return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
 }
@@ -612,7 +619,7 @@ int ho_autotune(ho_context* c, const ho_camera* cam, const float* iso, int n_iso
   if (W <= 0 || H <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
   const size_t nq = static_cast<size_t>(W) * H * n_iso;
   if ((rc = ensure_buf(c, c->d_rgb, c->rgb_cap, nq * 3, "cudaMalloc(rgb)"))) return rc;
-  const int slots = ho::round_slots(c->N);
+  const int slots = ho::round_batch_default(c->N, c->use_tc);
   const int64_t cand[HO_AUTOTUNE_N] = {slots / 2, slots, 2 * slots, 4 * slots, 8 * slots};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   CK(cudaEventCreate(&ev0), "cudaEventCreate");

@@ -164,6 +164,7 @@ struct ho_context {
   int rounds_needed = 0;     // non-empty rounds of the previous batched / learned call
   bool use_graph = true;     // run a call's launches as one CUDA graph
   bool fp64_check = true;    // FP64 residual check + plain fallback of the hits
+  bool use_tc = false;       // tensor-core round kernel for orders up to kTcMaxModes
   bool graph_warm = false;   // the first call of a context runs direct
   cudaGraphExec_t graph_exec = nullptr;
   bool last_graph = false;

@@ -100,6 +100,13 @@ constexpr int kMaxModes = 9;
 // record, pair slots, task queue) is sized so that three 4-warp blocks fit on
 // an SM up to N = 8 (two at N = 9, whose record alone is 15.5 KB).
 constexpr int round_slots(int n) { return n <= 7 ? 16 : (n == 8 ? 12 : 8); }
+// The round kernel's tensor-core form takes orders up to this (N*N <= 64
+// accumulator columns per component); one CTA of 4 warps per element batch.
+constexpr int kTcMaxModes = 8;
+// Default pairs per element batch: a warp's slots, or a CTA's with tc.
+__host__ __device__ constexpr int round_batch_default(int n, bool tc) {
+  return tc && n <= kTcMaxModes ? 4 * round_slots(n) : round_slots(n);
+}
 constexpr int kMinModes = 2;
 
 // Element record layout: x, y, z geometry blocks then the field block; in a

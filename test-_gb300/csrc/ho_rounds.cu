@@ -122,17 +122,19 @@ __global__ void round_scatter_kernel(const RoundPair* __restrict__ pairs, const 
 // (2..9) the batch count, region start, write cursor and take cursor.
 constexpr int kCtrOrderNb = 16, kCtrOrderOff = 26, kCtrOrderCur = 36, kCtrOrderNext = 46, kCtrWords = 64;
 
-__device__ __forceinline__ int batch_size(int chunk, int order) { return chunk > 0 ? chunk : round_slots(order); }
+__device__ __forceinline__ int batch_size(int chunk, int order, bool tc) {
+  return chunk > 0 ? chunk : round_batch_default(order, tc);
+}
 
 // Batches per order: each element's pairs in batches of its order's size.
 __global__ void round_batch_count_kernel(const uint32_t* __restrict__ ecount, const uint8_t* __restrict__ order,
-                                         int64_t n_elem, int chunk, unsigned* __restrict__ ctr) {
+                                         int64_t n_elem, int chunk, bool tc, unsigned* __restrict__ ctr) {
   const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n_elem) return;
   const int c = static_cast<int>(ecount[e]);
   if (c == 0) return;
   const int n = order[e];
-  const int B = batch_size(chunk, n);
+  const int B = batch_size(chunk, n, tc);
   atomicAdd(&ctr[kCtrOrderNb + n], static_cast<unsigned>((c + B - 1) / B));
 }
 
@@ -149,14 +151,14 @@ __global__ void round_order_offsets_kernel(unsigned* __restrict__ ctr) {
 
 // Each element's pairs in batches, written into its order's region.
 __global__ void round_batch_kernel(const uint32_t* __restrict__ ecount, const uint32_t* __restrict__ eoff,
-                                   const uint8_t* __restrict__ order, int64_t n_elem, int chunk,
+                                   const uint8_t* __restrict__ order, int64_t n_elem, int chunk, bool tc,
                                    RoundBatch* __restrict__ batches, unsigned* __restrict__ ctr) {
   const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n_elem) return;
   const int c = static_cast<int>(ecount[e]);
   if (c == 0) return;
   const int n = order[e];
-  const int B = batch_size(chunk, n);
+  const int B = batch_size(chunk, n, tc);
   const int nb = (c + B - 1) / B;
   const unsigned base = ctr[kCtrOrderOff + n] + atomicAdd(&ctr[kCtrOrderCur + n], static_cast<unsigned>(nb));
   for (int k = 0; k < nb; ++k) {
@@ -316,9 +318,9 @@ static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams&
   round_scatter_kernel<<<gi, 256, 0, s>>>(gathered, rb.pelem, rb.prank, rb.eoff, rb.ctr,
                                           const_cast<RoundPair*>(R.pairs), P.stats);
   const unsigned ge = static_cast<unsigned>((n_elem + 255) / 256);
-  round_batch_count_kernel<<<ge, 256, 0, s>>>(rb.ecount, c->d_cord, n_elem, c->round_chunk, rb.ctr);
+  round_batch_count_kernel<<<ge, 256, 0, s>>>(rb.ecount, c->d_cord, n_elem, c->round_chunk, c->use_tc, rb.ctr);
   round_order_offsets_kernel<<<1, 1, 0, s>>>(rb.ctr);
-  round_batch_kernel<<<ge, 256, 0, s>>>(rb.ecount, rb.eoff, c->d_cord, n_elem, c->round_chunk,
+  round_batch_kernel<<<ge, 256, 0, s>>>(rb.ecount, rb.eoff, c->d_cord, n_elem, c->round_chunk, c->use_tc,
                                         const_cast<RoundBatch*>(R.batches), rb.ctr);
   RT_TRY(cudaGetLastError());
   c->launches += 6 + __builtin_popcount(c->orders);
@@ -336,14 +338,14 @@ static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams&
     Rn.n_batches = rb.ctr + kCtrOrderNb + n;
     Rn.next_batch = rb.ctr + kCtrOrderNext + n;
     switch (n) {
-      case 2: e = launch_round_n<2>(Rn, s, learned); break;
-      case 3: e = launch_round_n<3>(Rn, s, learned); break;
-      case 4: e = launch_round_n<4>(Rn, s, learned); break;
-      case 5: e = launch_round_n<5>(Rn, s, learned); break;
-      case 6: e = launch_round_n<6>(Rn, s, learned); break;
-      case 7: e = launch_round_n<7>(Rn, s, learned); break;
-      case 8: e = launch_round_n<8>(Rn, s, learned); break;
-      case 9: e = launch_round_n<9>(Rn, s, learned); break;
+      case 2: e = launch_round_n<2>(Rn, s, learned, c->use_tc); break;
+      case 3: e = launch_round_n<3>(Rn, s, learned, c->use_tc); break;
+      case 4: e = launch_round_n<4>(Rn, s, learned, c->use_tc); break;
+      case 5: e = launch_round_n<5>(Rn, s, learned, c->use_tc); break;
+      case 6: e = launch_round_n<6>(Rn, s, learned, c->use_tc); break;
+      case 7: e = launch_round_n<7>(Rn, s, learned, c->use_tc); break;
+      case 8: e = launch_round_n<8>(Rn, s, learned, c->use_tc); break;
+      case 9: e = launch_round_n<9>(Rn, s, learned, c->use_tc); break;
       default: e = cudaErrorInvalidValue; break;
     }
   }

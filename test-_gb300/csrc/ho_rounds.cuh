@@ -33,6 +33,7 @@
 #include "ho_device.cuh"
 #include "ho_host.h"
 #include "ho_learn.h"
+#include "ho_tc.cuh"
 #include "ho_trace.cuh"
 
 namespace ho {
@@ -149,9 +150,11 @@ struct PairSm {
   };
 };
 
-template <int N>
+// Rec = false: the tensor-core form keeps the element's coefficients once per
+// CTA as its MMA operand instead.
+template <int N, bool Rec = true>
 struct WarpSm {
-  float rec[record_floats(N)];
+  float rec[Rec ? record_floats(N) : 4];
   PairSm pr[RoundCfg<N>::B];
   uint16_t ring[RoundCfg<N>::Ring];
   unsigned head, tail;
@@ -224,8 +227,8 @@ __device__ __forceinline__ Pred pair_pred(const PairSm& p) {
 }
 
 // A pair is finished: its iterations go to its ray and its slot is free.
-template <int N>
-__device__ __forceinline__ void pair_done(WarpSm<N>& W, int pp, const RoundParams* P) {
+template <int N, class WS>
+__device__ __forceinline__ void pair_done(WS& W, int pp, const RoundParams* P) {
   const PairSm& p = W.pr[pp];
   atomicAdd(&P->state[p.item].its, p.its);
   atomicOr(&W.freem, 1u << pp);
@@ -237,9 +240,9 @@ __device__ __forceinline__ void pair_done(WarpSm<N>& W, int pp, const RoundParam
 
 // Queue the 9 seeds of every face (other than the learned face) whose hull
 // box meets [0.001, cull_hi]; returns the number of faces culled.
-template <int N>
-__device__ __noinline__ int start_seeds(WarpSm<N>* Wp, int pp, const float* __restrict__ fbox, float cull_hi) {
-  WarpSm<N>& W = *Wp;
+template <int N, class WS>
+__device__ __noinline__ int start_seeds(WS* Wp, int pp, const float* __restrict__ fbox, float cull_hi) {
+  WS& W = *Wp;
   PairSm& p = W.pr[pp];
   const float3 o = ld3(p.o), d = ld3(p.d);
   int n = 0, culled = 0;
@@ -267,9 +270,9 @@ __device__ __noinline__ int start_seeds(WarpSm<N>* Wp, int pp, const float* __re
 // Nearest face over the learned face and every face's first accepted seed,
 // in face order. A hit is left in the pair's result fields (the caller
 // starts its post evaluation); no hit finishes the pair.
-template <int N>
-__device__ __noinline__ bool finalize_faces(WarpSm<N>* Wp, int pp, const RoundParams* P) {
-  WarpSm<N>& W = *Wp;
+template <int N, class WS>
+__device__ __noinline__ bool finalize_faces(WS* Wp, int pp, const RoundParams* P) {
+  WS& W = *Wp;
   PairSm& p = W.pr[pp];
   float best = p.best_t;
   int face = -1;
@@ -317,9 +320,9 @@ __device__ __forceinline__ void start_post(LaneSolve& s, int kind, int pp, float
 // the faces whose hull box meets [0.001, closest]. Returns culled faces |
 // 256 when a learned start was rejected | 65536 when the pair needs its face
 // post evaluation now.
-template <int N, bool L>
-__device__ __noinline__ int start_faces(WarpSm<N>* Wp, int pp, const float* __restrict__ fbox, const RoundParams* P) {
-  WarpSm<N>& W = *Wp;
+template <int N, bool L, class WS>
+__device__ __noinline__ int start_faces(WS* Wp, int pp, const float* __restrict__ fbox, const RoundParams* P) {
+  WS& W = *Wp;
   PairSm& p = W.pr[pp];
   p.lf = -1;
   for (int f = 0; f < 6; ++f) p.fseed[f] = 9;
@@ -340,8 +343,8 @@ __device__ __noinline__ int start_faces(WarpSm<N>* Wp, int pp, const float* __re
   return code;
 }
 
-template <int N, bool L>
-__device__ __forceinline__ void face_phase(WarpSm<N>& W, int pp, const float* __restrict__ fbox, const RoundParams* P,
+template <int N, bool L, class WS>
+__device__ __forceinline__ void face_phase(WS& W, int pp, const float* __restrict__ fbox, const RoundParams* P,
                                            Work& w, LaneSolve& s) {
   const int code = start_faces<N, L>(&W, pp, fbox, P);
   w.culled += code & 255;
@@ -350,8 +353,8 @@ __device__ __forceinline__ void face_phase(WarpSm<N>& W, int pp, const float* __
 }
 
 // Begin a popped task.
-template <int N, bool L>
-__device__ __forceinline__ void begin_task(WarpSm<N>& W, uint32_t tw, LaneSolve& s) {
+template <int N, bool L, class WS>
+__device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s) {
   s.task = static_cast<int>(tw);
   s.kind = static_cast<int>(tw >> 13);
   s.pp = static_cast<int>((tw >> 8) & 31u);
@@ -415,11 +418,11 @@ __device__ __forceinline__ void commit_hit(const RoundParams& P, const PairSm& p
 
 // Fill a free slot with a pair of the batch and queue its first tasks.
 // Returns start_faces' code for pairs that go straight to the face search.
-template <int N, bool L>
-__device__ __noinline__ int admit_pair(WarpSm<N>* Wp, const RoundParams* P, int slot, RoundPair rp, int elem,
+template <int N, bool L, class WS>
+__device__ __noinline__ int admit_pair(WS* Wp, const RoundParams* P, int slot, RoundPair rp, int elem,
                                        bool has_field, const float* __restrict__ fbox) {
   constexpr int R = RoundCfg<N>::Ring;
-  WarpSm<N>& W = *Wp;
+  WS& W = *Wp;
   PairSm& p = W.pr[slot];
   const int64_t q = P->work[rp.item];
   float3 o, d;
@@ -456,31 +459,74 @@ __device__ __noinline__ int admit_pair(WarpSm<N>* Wp, const RoundParams* P, int 
   return start_faces<N, L>(Wp, slot, fbox, P);
 }
 
-template <int N, bool L>
+// Shared memory of the tensor-core form: the CTA's TcSm, then the warps'
+// workspaces (no per-warp record).
+template <int N, bool TC>
+constexpr size_t round_tc_off() {
+  return TC ? (sizeof(TcSm) + 127) / 128 * 128 : 0;
+}
+
+// TC = false: one warp per element batch, contractions on the CUDA cores from
+// the warp's staged record (eval_comps).
+// TC = true: one CTA (4 warps) per element batch. Each warp keeps its own pair
+// slots and task queue and admits pairs from the CTA's batch; every step the
+// 128 threads' points are evaluated together by tcgen05 MMAs against the
+// element's coefficients (ho_tc.cuh), so the CTA steps in lockstep: a warp
+// with no task joins the step with idle lanes, and the CTA leaves the batch
+// when no warp has work and no pair is left.
+template <int N, bool L, bool TC>
 __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
   constexpr int B = RoundCfg<N>::B, R = RoundCfg<N>::Ring;
   constexpr unsigned kAllSlots = B >= 32 ? 0xffffffffu : ((1u << B) - 1u);
-  constexpr size_t kWarpBytes = (sizeof(WarpSm<N>) + 15) / 16 * 16;
-  const int lane = threadIdx.x & 31;
-  extern __shared__ __align__(16) unsigned char round_smem[];
-  WarpSm<N>& W = *reinterpret_cast<WarpSm<N>*>(round_smem + (threadIdx.x >> 5) * kWarpBytes);
+  constexpr size_t kWarpBytes = (sizeof(WarpSm<N, !TC>) + 15) / 16 * 16;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  extern __shared__ __align__(128) unsigned char round_smem[];
+  WarpSm<N, !TC>& W = *reinterpret_cast<WarpSm<N, !TC>*>(round_smem + round_tc_off<N, TC>() + warp * kWarpBytes);
+  TcSm& T = *reinterpret_cast<TcSm*>(round_smem);
   Elem<N, true> el;
   el.c = CoefRef<true>{static_cast<uint32_t>(__cvta_generic_to_shared(W.rec))};
   Work w;
   const unsigned nb = *P.n_batches, bbase = *P.batch_base;
+  uint32_t tmem = 0, phase = 0;
+  bool tc_ok = true;
+  if constexpr (TC) {
+    if (warp == 0) tc_alloc(&T.tslot);
+    if (threadIdx.x == 0) {
+      tc_mbar_init(&T.mbar);
+      T.ctl[2] = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    tmem = T.tslot;
+  }
   for (;;) {
     unsigned b = 0;
-    if (lane == 0) b = atomicAdd(P.next_batch, 1u);
-    b = __shfl_sync(kFull, b, 0);
-    if (b >= nb) break;
+    if constexpr (TC) {
+      __syncthreads();  // the previous batch is done in every warp
+      if (threadIdx.x == 0) {
+        T.ctl[0] = atomicAdd(P.next_batch, 1u);
+        T.ctl[1] = 0;
+      }
+      __syncthreads();
+      b = T.ctl[0];
+    } else {
+      if (lane == 0) b = atomicAdd(P.next_batch, 1u);
+      b = __shfl_sync(kFull, b, 0);
+    }
+    if (b >= nb || !tc_ok) break;
     const RoundBatch bt = P.batches[bbase + b];
     const unsigned count = static_cast<unsigned>(bt.count);
     const float* fbox = P.fbox + static_cast<int64_t>(bt.elem) * kFaceBoxFloats;
     {
       const float* recp = P.coff ? P.crec + P.coff[bt.elem] : P.rec + static_cast<int64_t>(bt.elem) * record_floats(N);
-      const float4* src = reinterpret_cast<const float4*>(recp);
-      float4* dst = reinterpret_cast<float4*>(W.rec);
-      for (int q4 = lane; q4 < record_floats(N) / 4; q4 += 32) dst[q4] = __ldg(src + q4);
+      if constexpr (TC) {
+        tc_stage_b<N>(T, recp, threadIdx.x, kRoundBlock);
+      } else {
+        const float4* src = reinterpret_cast<const float4*>(recp);
+        float4* dst = reinterpret_cast<float4*>(W.rec);
+        for (int q4 = lane; q4 < record_floats(N) / 4; q4 += 32) dst[q4] = __ldg(src + q4);
+      }
     }
     const bool has_field = (__ldg(P.flags + bt.elem) & 1u) != 0;
     el.has_field = has_field;
@@ -490,7 +536,12 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
       W.freem = kAllSlots;
       W.admitted = 0;
     }
-    __syncwarp();
+    if constexpr (TC) {
+      tc_proxy_fence();  // the B operand, for the MMAs
+      __syncthreads();
+    } else {
+      __syncwarp();
+    }
     LaneSolve s;
     s.task = -1;
     s.kind = 0;
@@ -511,14 +562,21 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
       }
       // -- admit the batch's next pairs into free slots
       {
-        unsigned fm = 0u, adm = 0u;  // lane 0 reads, every lane uses the same values
+        unsigned fm = 0u, adm = 0u, nadm = 0u;  // lane 0 reads, every lane uses the same values
         if (lane == 0) {
           fm = ld_ctl(&W.freem);
-          adm = ld_ctl(&W.admitted);
+          if constexpr (TC) {  // claim pairs of the CTA's batch for this warp's free slots
+            const unsigned want = static_cast<unsigned>(__popc(fm));
+            adm = want > 0u && ld_ctl(&T.ctl[1]) < count ? atomicAdd(&T.ctl[1], want) : count;
+            nadm = adm < count ? min(want, count - adm) : 0u;
+          } else {
+            adm = ld_ctl(&W.admitted);
+            nadm = min(static_cast<unsigned>(__popc(fm)), count - adm);
+          }
         }
         fm = __shfl_sync(kFull, fm, 0);
         adm = __shfl_sync(kFull, adm, 0);
-        const unsigned nadm = min(static_cast<unsigned>(__popc(fm)), count - adm);
+        nadm = __shfl_sync(kFull, nadm, 0);
         __syncwarp();  // every lane has read freem / admitted before any lane changes them
         if (nadm > 0u) {
           if (lane < static_cast<int>(nadm)) {
@@ -535,7 +593,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
               atomicOr(&P.stats->status, kStatusRoundGuard);
             }
           }
-          if (lane == 0) W.admitted = adm + nadm;
+          if (!TC && lane == 0) W.admitted = adm + nadm;
         }
         __syncwarp();
       }
@@ -550,15 +608,26 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
       head = __shfl_sync(kFull, head, 0);
       tail = __shfl_sync(kFull, tail, 0);
       admitted = __shfl_sync(kFull, admitted, 0);
-      const unsigned avail = tail - head;
-      if (avail > static_cast<unsigned>(R)) {  // the queue can never hold more: a broken invariant
-        if (lane == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
-        break;
-      }
-      if (avail == 0u && idle == kFull) {
-        if (admitted >= count) break;
-        __syncwarp();
-        continue;
+      unsigned avail = tail - head;
+      if constexpr (TC) {
+        // a warp whose queue broke its bound stops taking tasks (the status says why)
+        if (avail > static_cast<unsigned>(R)) {
+          if (lane == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
+          avail = 0u;
+        }
+        const bool warp_busy = !(avail == 0u && idle == kFull);
+        const bool more = warp_busy || ld_ctl(&T.ctl[1]) < count;
+        if (!__syncthreads_or(lane == 0 && more)) break;  // no warp has work, no pair is left
+      } else {
+        if (avail > static_cast<unsigned>(R)) {  // the queue can never hold more: a broken invariant
+          if (lane == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
+          break;
+        }
+        if (avail == 0u && idle == kFull) {
+          if (admitted >= count) break;
+          __syncwarp();
+          continue;
+        }
       }
       const unsigned rank = __popc(idle & ((1u << lane) - 1u));
       if (s.task < 0 && rank < avail) begin_task<N, L>(W, W.ring[(head + rank) % R], s);
@@ -576,11 +645,40 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
       float3 gr = make_float3(0.f, 0.f, 0.f);
       // inverse-map iteration of an isosurface solve: the field comes with it
       const bool ahead = (s.kind == TK_SAMPLE || s.kind == TK_REFINE) && !s.post;
+      const bool want_geom = act && s.kind != TK_IPOST;
+      const bool want_field = act && ((s.post && (s.kind != TK_FPOST || has_field)) || ahead);
+      float4 r[4];
+      if constexpr (TC) {
+        // every thread's point as a row of the step's MMAs; idle lanes give a
+        // row at xi = 0 whose results are not used
+        const float3 xi = act ? s.xi : make_float3(0.f, 0.f, 0.f);
+        float ar[N], dr[N], as[N], ds[N], at[N], dt[N];
+        basis_val_der<N>(xi.x, ar, dr);
+        basis_val_der<N>(xi.y, as, ds);
+        basis_val_der<N>(xi.z, at, dt);
+        tc_stage_a<N>(T, threadIdx.x, ar, dr);
+        tc_proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (threadIdx.x == 0) tc_issue(T, tmem);
+        const bool done = tc_mbar_wait(&T.mbar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!done)) {  // the MMAs did not complete in time: give up the round
+          if (threadIdx.x == 0) atomicOr(&P.stats->status, kStatusRoundGuard);
+          tc_ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+        if (__any_sync(kFull, want_geom)) {
+#pragma unroll 1
+          for (int comp = 0; comp < 3; ++comp) r[comp] = tc_finish_comp<N>(taddr, comp, as, ds, at, dt);
+        }
+        if (__any_sync(kFull, want_field)) r[3] = tc_finish_comp<N>(taddr, 3, as, ds, at, dt);
+      }
       if (act) {
-        const bool want_geom = s.kind != TK_IPOST;
-        const bool want_field = (s.post && (s.kind != TK_FPOST || has_field)) || ahead;
-        float4 r[4];
-        eval_comps<N, true>(el.c, s.xi, want_geom ? 0 : 3, want_field ? 4 : 3, r);
+        if constexpr (!TC) eval_comps<N, true>(el.c, s.xi, want_geom ? 0 : 3, want_field ? 4 : 3, r);
         w.flops += eval_flops(N, (want_geom ? 3 : 0) + (want_field ? 1 : 0));
         if (want_geom) {
           X = make_float3(r[0].x, r[1].x, r[2].x);
@@ -874,41 +972,59 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
       __syncwarp();
     }
   }
+  if constexpr (TC) {
+    // MMAs still in flight after a timed-out wait complete before the
+    // accumulator columns are freed (bounded again)
+    if (!tc_ok && threadIdx.x == 0) tc_mbar_wait(&T.mbar, phase ^ 1u);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem);
+  }
   flush_work(P.stats, w, false);
 }
 
-template <int N>
-cudaError_t launch_round_n(const RoundParams& R, cudaStream_t s, bool learned) {
-  static int grid[2] = {0, 0};  // persistent grid: resident blocks per SM x SMs
-  const size_t smem = round_smem_bytes<N>();
-  int& g = grid[learned ? 1 : 0];
-  if (g == 0) {
+template <int N, bool L, bool TC>
+static cudaError_t launch_round_kernel(const RoundParams& R, cudaStream_t s) {
+  // persistent grid: resident blocks per SM x SMs (the tensor-core form holds
+  // all of an SM's tensor memory, so one CTA per SM: its shared memory request
+  // is raised to more than half of the SM's)
+  static int grid = 0;
+  static size_t smem = 0;
+  if (grid == 0) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (learned) {
-      cudaFuncSetAttribute(round_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, round_kernel<N, true>, kRoundBlock, smem);
-    } else {
-      cudaFuncSetAttribute(round_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(smem));
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, round_kernel<N, false>, kRoundBlock, smem);
+    smem = round_tc_off<N, TC>() + (kRoundBlock / 32) * ((sizeof(WarpSm<N, !TC>) + 15) / 16 * 16);
+    if (TC) {
+      int max_optin = 0;
+      cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      smem = std::max<size_t>(smem, static_cast<size_t>(max_optin) / 2 + 1024);
     }
-    g = sms * (per > 0 ? per : 1);
+    cudaFuncSetAttribute(round_kernel<N, L, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, round_kernel<N, L, TC>, kRoundBlock, smem);
+    grid = sms * (TC ? 1 : (per > 0 ? per : 1));
   }
-  if (learned) round_kernel<N, true><<<g, kRoundBlock, smem, s>>>(R);
-  else round_kernel<N, false><<<g, kRoundBlock, smem, s>>>(R);
+  round_kernel<N, L, TC><<<grid, kRoundBlock, smem, s>>>(R);
   return cudaGetLastError();
 }
 
+// tc: the tensor-core form (orders up to kTcMaxModes).
+template <int N>
+cudaError_t launch_round_n(const RoundParams& R, cudaStream_t s, bool learned, bool tc) {
+  if constexpr (N <= kTcMaxModes) {
+    if (tc) return learned ? launch_round_kernel<N, true, true>(R, s) : launch_round_kernel<N, false, true>(R, s);
+  }
+  return learned ? launch_round_kernel<N, true, false>(R, s) : launch_round_kernel<N, false, false>(R, s);
+}
+
 // explicit instantiations live in ho_trace_n*.cu
-extern template cudaError_t launch_round_n<2>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<3>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<4>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<5>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<6>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<7>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<8>(const RoundParams& R, cudaStream_t s, bool learned);
-extern template cudaError_t launch_round_n<9>(const RoundParams& R, cudaStream_t s, bool learned);
+extern template cudaError_t launch_round_n<2>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<3>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<4>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<5>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<6>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<7>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<8>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+extern template cudaError_t launch_round_n<9>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
 
 }  // namespace ho

@@ -79,6 +79,36 @@ def test_plain_and_batched_modes_agree(small):
     assert sp["rays"] == W * H
 
 
+@pytest.mark.parametrize("mode", ["batched", "learned"])
+def test_tensor_core_and_cuda_core_rounds_agree(small, mode):
+    """The tensor-core round kernel (TF32 hi/lo MMAs for the first contraction)
+    and the FP32 CUDA-core kernel run the same solves; their answers differ
+    only by rounding, so hit identity agrees on >= 99.9% of rays and t within
+    the solvers' tolerance where it does."""
+    ctx, w, arrs, osc = small
+    W = H = 96
+    if mode == "learned":
+        ctx.train_mlp(n_samples=200_000, steps=300, batch=2048, lr=2e-3, seed=3)
+        ctx.set_mode(hr.MODE_LEARNED)
+    else:
+        ctx.set_mode(hr.MODE_BATCHED)
+    try:
+        ctx.set_option(hr.OPT_TENSOR, 0)
+        _, h0 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+        ctx.set_option(hr.OPT_TENSOR, 1)
+        _, h1 = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+        s1 = ctx.stats()
+    finally:
+        ctx.set_option(hr.OPT_TENSOR, 0)
+        ctx.set_mode(hr.MODE_BATCHED)
+    a, b = h0[0].reshape(-1), h1[0].reshape(-1)
+    same = classify(a, b)
+    assert same.mean() >= 0.999, f"identity agreement {same.mean():.4f}"
+    m = same & (a["kind"] > 0)
+    assert np.abs(a["t"][m] - b["t"][m]).max() < 2e-4
+    assert s1["status"] == 0 and s1["fp64_failed_after_fallback"] == 0
+
+
 def test_intersect_explicit_rays_matches_render(small):
     ctx, w, arrs, osc = small
     W = H = 64
@@ -192,15 +222,22 @@ def mixed(oracle):
     return ctx, arrs, oracle.OracleScene(arrs)
 
 
+@pytest.mark.parametrize("tensor", [0, 1])
 @pytest.mark.parametrize("iso_on", [True, False])
-def test_mixed_orders_match_oracle(mixed, oracle, iso_on):
+def test_mixed_orders_match_oracle(mixed, oracle, iso_on, tensor):
+    """tensor = 1: orders 3..8 run the tensor-core round kernel, order 9 the
+    CUDA-core one, in the same call."""
     ctx, arrs, osc = mixed
     assert len(set(arrs.geom_modes[:, 0].tolist())) >= 5
     cam = hr.Camera((2.5, 2.0, 1.8), (0.5, 0.5, 0.5))
     W = H = 96
     iso = 0.1 if iso_on else 0.0
     ctx.set_mode(hr.MODE_BATCHED)
-    _, hits = ctx.render(cam, [iso], W, H, iso_zero_disables=True, want_rgb=False, want_hits=True)
+    ctx.set_option(hr.OPT_TENSOR, tensor)
+    try:
+        _, hits = ctx.render(cam, [iso], W, H, iso_zero_disables=True, want_rgb=False, want_hits=True)
+    finally:
+        ctx.set_option(hr.OPT_TENSOR, 0)
     h = hits[0].reshape(-1)
     rays = oracle.camera_rays(cam.lookfrom, cam.lookat, cam.vup, cam.vfov_deg, W, H)
     ref, _ = osc.trace(rays, iso, iso_on, precision=32)
