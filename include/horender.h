@@ -287,6 +287,12 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_TIME_ROUNDS 5
 #define HO_OPT_TENSOR 6
 int ho_set_option(ho_context* ctx, int option, int64_t value);
+/* The FP64 residuals that the batched / learned engines' final check
+ * computes, for caller-given hits (no reference counterpart): for hit i on
+ * ray i (rays as in ho_intersect), out[2i] = the largest component of
+ * |x(xi) - (o + t d)| and out[2i+1] = the field value u(xi) (0 for misses and
+ * elements without field). HO_ERR_RANGE when a hit names no element. */
+int ho_hit_residuals(ho_context* ctx, int64_t n, const float* rays, const ho_hit* hits, double* out);
 int ho_get_option(ho_context* ctx, int option, int64_t* value);
 
 /* Autotuner of the batched / learned engine (no reference counterpart): times

@@ -562,6 +562,31 @@ int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso
   return read_stats(c);
 }
 
+int ho_hit_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (n < 0) return fail(c, HO_ERR_ARG, "n must be >= 0");
+  if (n == 0) return HO_OK;
+  if (!rays || !hits || !out) return fail(c, HO_ERR_ARG, "null buffer");
+  for (int64_t i = 0; i < n; ++i)
+    if (hits[i].kind != HO_HIT_MISS && (hits[i].elem < 0 || hits[i].elem >= c->n_elem))
+      return fail(c, HO_ERR_RANGE, "hit " + std::to_string(i) + " names no element of the scene");
+  int rc;
+  if ((rc = ensure_buf(c, c->d_rays, c->rays_cap, static_cast<size_t>(n) * 6, "cudaMalloc(rays)"))) return rc;
+  if ((rc = ensure_buf(c, c->d_hits, c->hits_cap, static_cast<size_t>(n), "cudaMalloc(hits)"))) return rc;
+  double* d_out = nullptr;
+  CK(cudaMalloc(&d_out, static_cast<size_t>(n) * 2 * sizeof(double)), "cudaMalloc(residuals)");
+  cudaError_t e = cudaMemcpyAsync(c->d_rays, rays, n * 6 * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_hits, hits, n * sizeof(ho_hit), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = static_cast<cudaError_t>(ho::launch_residuals(c, n, c->d_rays, c->d_hits, d_out, c->stream));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d_out, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_out);
+  CK(e, "hit residuals");
+  return HO_OK;
+}
+
 int ho_set_option(ho_context* c, int option, int64_t value) {
   if (!c) return HO_ERR_ARG;
   switch (option) {

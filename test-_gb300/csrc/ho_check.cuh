@@ -49,13 +49,28 @@ __device__ __forceinline__ void basis_val64(double x, double (&a)[N]) {
   }
 }
 
+// Knuth's TwoSum: s + e == a + b exactly (round-to-nearest FP32; the
+// intrinsics keep the compiler from fusing or reordering the steps).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 // Value of one coefficient block (rows padded to row_stride(N), a multiple of
-// 4 floats, so a row is RS/4 aligned float4 loads) in FP64. The rows of one k
-// are independent and unrolled; each row sums even and odd terms separately
-// to halve the dependent FMA chain.
+// 4 floats, so a row is RS/4 aligned float4 loads), FP64-accurate.
+//
+// The coefficients are FP32, so the innermost sums sum_i c_i a_i are formed
+// in double-single arithmetic on the FP32 pipes: a_i = ah_i + al_i (two
+// floats), c_i ah_i = p + ep exactly (FMA-based TwoProduct), the running sum
+// kept as sh + sl with TwoSum, the small parts added in FP32. That is about
+// 2^-44 relative per row, below FP64's own rounding of the outer sums, and
+// avoids an FP64 conversion and FMA per coefficient (FP64 runs at a small
+// fraction of the FP32 rate here). The sums over j and k, and the residuals,
+// are FP64.
 template <int N>
-__device__ double value64(const float* __restrict__ blk, const double (&ar)[N], const double (&as)[N],
-                          const double (&at)[N]) {
+__device__ double value64(const float* __restrict__ blk, const float (&ah)[N], const float (&al)[N],
+                          const double (&as)[N], const double (&at)[N]) {
   constexpr int RS = row_stride(N);
   static_assert(RS % 4 == 0, "rows are whole float4s");
   double v = 0.0;
@@ -74,12 +89,17 @@ __device__ double value64(const float* __restrict__ blk, const double (&ar)[N], 
         c[4 * i4 + 2] = t4.z;
         c[4 * i4 + 3] = t4.w;
       }
-      double s0 = 0.0, s1 = 0.0;
+      float sh = 0.f, sl = 0.f;
 #pragma unroll
-      for (int i = 0; i < N; i += 2) s0 = fma(static_cast<double>(c[i]), ar[i], s0);
-#pragma unroll
-      for (int i = 1; i < N; i += 2) s1 = fma(static_cast<double>(c[i]), ar[i], s1);
-      q = fma(s0 + s1, as[j], q);
+      for (int i = 0; i < N; ++i) {
+        const float p = __fmul_rn(c[i], ah[i]);
+        const float ep = __fmaf_rn(c[i], ah[i], -p);
+        float s, es;
+        two_sum(sh, p, s, es);
+        sh = s;
+        sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(es, ep), __fmul_rn(c[i], al[i])));
+      }
+      q = fma(static_cast<double>(sh) + static_cast<double>(sl), as[j], q);
     }
     double atk = 0.0;  // at[k] by selection: the array stays in registers
 #pragma unroll
@@ -90,26 +110,68 @@ __device__ double value64(const float* __restrict__ blk, const double (&ar)[N], 
   return v;
 }
 
+// The FP64 residuals of a hit at xi in element elem: the largest component
+// of x(xi) - (o + t d), and the field value u(xi) (0 when unused).
+template <int N>
+__device__ void fp64_residuals(const float* __restrict__ rec_all, int elem, float3 o, float3 d, float t, float3 xi,
+                               bool want_field, double& rpos, double& u) {
+  const float* rec = rec_all + static_cast<int64_t>(elem) * record_floats(N);
+  double ar[N], as[N], at[N];
+  basis_val64<N>(static_cast<double>(xi.x), ar);
+  basis_val64<N>(static_cast<double>(xi.y), as);
+  basis_val64<N>(static_cast<double>(xi.z), at);
+  float ah[N], al[N];  // ar as two floats
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    ah[i] = static_cast<float>(ar[i]);
+    al[i] = static_cast<float>(ar[i] - static_cast<double>(ah[i]));
+  }
+  const double td = t;
+  const double px = static_cast<double>(o.x) + td * d.x, py = static_cast<double>(o.y) + td * d.y,
+               pz = static_cast<double>(o.z) + td * d.z;
+  const double rx = fabs(value64<N>(rec, ah, al, as, at) - px);
+  const double ry = fabs(value64<N>(rec + block_floats(N), ah, al, as, at) - py);
+  const double rz = fabs(value64<N>(rec + 2 * block_floats(N), ah, al, as, at) - pz);
+  rpos = fmax(rx, fmax(ry, rz));
+  u = want_field ? value64<N>(rec + 3 * block_floats(N), ah, al, as, at) : 0.0;
+}
+
 // True when the hit passes the FP64 check (a miss always passes).
 template <int N>
 __device__ bool fp64_check(const TraceParams& P, float3 o, float3 d, float iso, const HitState& h) {
   if (h.kind == HO_HIT_MISS) return true;
-  const float* rec = P.rec + static_cast<int64_t>(h.elem) * record_floats(N);
-  double ar[N], as[N], at[N];
-  basis_val64<N>(static_cast<double>(h.xi.x), ar);
-  basis_val64<N>(static_cast<double>(h.xi.y), as);
-  basis_val64<N>(static_cast<double>(h.xi.z), at);
-  const double t = h.t;
-  const double px = static_cast<double>(o.x) + t * d.x, py = static_cast<double>(o.y) + t * d.y,
-               pz = static_cast<double>(o.z) + t * d.z;
-  const double rx = fabs(value64<N>(rec, ar, as, at) - px);
-  const double ry = fabs(value64<N>(rec + block_floats(N), ar, as, at) - py);
-  const double rz = fabs(value64<N>(rec + 2 * block_floats(N), ar, as, at) - pz);
-  const double r = fmax(rx, fmax(ry, rz));
-  if (h.kind == HO_HIT_FACE) return r <= kCheckFaceTol;
+  const bool iso_hit = h.kind != HO_HIT_FACE;
+  double r, u;
+  fp64_residuals<N>(P.rec, h.elem, o, d, h.t, h.xi, iso_hit, r, u);
+  if (!iso_hit) return r <= kCheckFaceTol;
   if (r > kCheckIsoPosTol) return false;
-  const double u = value64<N>(rec + 3 * block_floats(N), ar, as, at);
   return fabs(u - static_cast<double>(iso)) <= kCheckIsoFieldTol;
+}
+
+// The check's residuals for given hits (ho_hit_residuals): per hit the
+// position residual and the field value at its xi.
+template <int N>
+__global__ void __launch_bounds__(128) residual_kernel(const float* __restrict__ rec, const uint32_t* __restrict__ flags,
+                                                       int64_t n, const float* __restrict__ rays,
+                                                       const ho_hit* __restrict__ hits, double* __restrict__ out) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const ho_hit h = hits[i];
+  double r = 0.0, u = 0.0;
+  if (h.kind != HO_HIT_MISS && h.elem >= 0) {
+    const float* ray = rays + 6 * i;
+    fp64_residuals<N>(rec, h.elem, make_float3(ray[0], ray[1], ray[2]), make_float3(ray[3], ray[4], ray[5]), h.t,
+                      make_float3(h.xi[0], h.xi[1], h.xi[2]), (flags[h.elem] & 1u) != 0, r, u);
+  }
+  out[2 * i] = r;
+  out[2 * i + 1] = u;
+}
+
+template <int N>
+cudaError_t launch_residuals_n(const float* rec, const uint32_t* flags, int64_t n, const float* rays, const ho_hit* hits,
+                               double* out, cudaStream_t s) {
+  if (n > 0) residual_kernel<N><<<static_cast<unsigned>((n + 127) / 128), 128, 0, s>>>(rec, flags, n, rays, hits, out);
+  return cudaGetLastError();
 }
 
 // One thread per queued ray with a hit: FP64 check; failures are listed.
@@ -196,5 +258,22 @@ extern template cudaError_t launch_check_n<8>(const TraceParams&, RayState*, uin
                                               cudaStream_t);
 extern template cudaError_t launch_check_n<9>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
                                               cudaStream_t);
+
+extern template cudaError_t launch_residuals_n<2>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<3>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<4>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<5>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<6>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<7>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<8>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
+extern template cudaError_t launch_residuals_n<9>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
+                                                  double*, cudaStream_t);
 
 }  // namespace ho

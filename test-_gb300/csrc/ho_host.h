@@ -192,4 +192,6 @@ struct TraceArgs {
   uint8_t* rgb = nullptr;       // optional (camera mode)
 };
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s);
+// The FP64 check's residuals for caller-given hits (ho_rounds.cu).
+int launch_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out, cudaStream_t s);
 }  // namespace ho

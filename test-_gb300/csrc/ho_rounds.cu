@@ -222,6 +222,23 @@ int prepare_rounds(ho_context* c, int64_t n_cap) {
   return 0;
 }
 
+// The check's residuals for caller-given hits (ho_hit_residuals).
+int launch_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out, cudaStream_t s) {
+  cudaError_t e;
+  switch (c->N) {
+    case 2: e = launch_residuals_n<2>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 3: e = launch_residuals_n<3>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 4: e = launch_residuals_n<4>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 5: e = launch_residuals_n<5>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 6: e = launch_residuals_n<6>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 7: e = launch_residuals_n<7>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 8: e = launch_residuals_n<8>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    case 9: e = launch_residuals_n<9>(c->d_rec, c->d_flags, n, rays, hits, out, s); break;
+    default: e = cudaErrorInvalidValue; break;
+  }
+  return int(e);
+}
+
 // FP64 check of the rays' hits, plain fallback of the failures.
 static int enqueue_check(ho_context* c, const TraceParams& P, const RoundParams& R, cudaStream_t s, int64_t n_cap) {
   if (!c->fp64_check) return 0;

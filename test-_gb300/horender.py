@@ -90,6 +90,7 @@ def _load():
     L.ho_render_views_device.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp]
     L.ho_render_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp, vp]
     L.ho_intersect.argtypes = [vp, i64, vp, f32, i32, vp]
+    L.ho_hit_residuals.argtypes = [vp, i64, vp, vp, vp]
     L.ho_intersect_device.argtypes = [vp, i64, vp, f32, i32, vp, vp]
     L.ho_set_mode.argtypes = [vp, i32]
     L.ho_set_option.argtypes = [vp, i32, i64]
@@ -338,6 +339,15 @@ class Context:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
         out = np.zeros(rays.shape[0], HIT_DTYPE)
         self._ck(lib.ho_intersect(self.h, rays.shape[0], _p(rays), float(iso), int(iso_enabled), _p(out)))
+        return out
+
+    def hit_residuals(self, rays: np.ndarray, hits: np.ndarray) -> np.ndarray:
+        """The final FP64 check's residuals for the given hits: (n, 2) with
+        the largest position-residual component and the field value at xi."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        hits = np.ascontiguousarray(hits, HIT_DTYPE).reshape(-1)
+        out = np.zeros((rays.shape[0], 2), np.float64)
+        self._ck(lib.ho_hit_residuals(self.h, rays.shape[0], _p(rays), _p(hits), _p(out)))
         return out
 
     def intersect_device(self, n: int, rays_ptr: int, iso: float, iso_enabled: bool, out_ptr: int, stream_ptr):

@@ -212,6 +212,35 @@ def test_fp64_check_and_plain_fallback(small):
     assert int(failed_final.sum()) == s1["fp64_failed_after_fallback"]
 
 
+def test_fp64_check_residuals_match_oracle(small, oracle):
+    """The final check's residuals (double-single inner sums, FP64 outer sums)
+    equal the FP64 oracle's x(xi) and u(xi) at the returned hits to 1e-10."""
+    ctx, w, arrs, osc = small
+    W = H = 64
+    ctx.set_mode(hr.MODE_BATCHED)
+    _, hits = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+    h = hits[0].reshape(-1)
+    rays = oracle.camera_rays(w.camera.lookfrom, w.camera.lookat, w.camera.vup, w.camera.vfov_deg, W, H)
+    res = ctx.hit_residuals(rays, h)
+    hit = np.nonzero(h["kind"] > 0)[0]
+    assert hit.size > 100 and (res[h["kind"] == 0] == 0).all()
+    r32 = rays.astype(np.float32).astype(np.float64)
+    worst_x = worst_u = 0.0
+    for e in np.unique(h["elem"][hit]):
+        idx = hit[h["elem"][hit] == e]
+        xi = h["xi"][idx].astype(np.float64)
+        x = osc.map_point(int(e), xi)
+        p = r32[idx, :3] + h["t"][idx].astype(np.float64)[:, None] * r32[idx, 3:]
+        rpos = np.abs(x - p).max(axis=1)
+        worst_x = max(worst_x, float(np.abs(rpos - res[idx, 0]).max()))
+        u = osc.eval_point(int(e), xi)[:, 9]
+        worst_u = max(worst_u, float(np.abs(u - res[idx, 1]).max()))
+    assert worst_x < 1e-10 and worst_u < 1e-10, (worst_x, worst_u)
+    # every checked hit passes the tolerances it was checked against
+    face = h["kind"][hit] == hr.HIT_FACE
+    assert (res[hit[face], 0] <= 1.5e-4).all() and (res[hit[~face], 0] <= 1e-4).all()
+
+
 @pytest.fixture(scope="module")
 def mixed(oracle):
     """Mixed orders: 5^3 hexes with P drawn from 2..8 (modes 3..9 per element)."""
