@@ -139,6 +139,7 @@ typedef struct {
   uint64_t round_kernel_ns;  /* HO_OPT_TIME_ROUNDS: device time of the round
                                 kernels' launches (CUDA events), else 0      */
   uint64_t round_launches;   /* HO_OPT_TIME_ROUNDS: round kernel launches     */
+  uint64_t tail_rays;        /* rays finished by the tail (HO_OPT_TAIL)       */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */
@@ -275,6 +276,11 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     accumulators take 416 of an SM's 512 tensor-memory
  *                     columns, so one CTA of 4 warps runs per SM, in lockstep,
  *                     and its steps are latency-bound.
+ * HO_OPT_TAIL        rounds before the tail (default 4, 0..256; 0: no tail):
+ *                     after them, every ray still in flight is finished by
+ *                     one warp walking the rest of its candidates (the same
+ *                     solves), so the last rays do not wait round by round
+ *                     for each round's slowest pair.
  * HO_OPT_TIME_ROUNDS  0 (default); 1: a pair of CUDA events brackets each
  *                     round's intersection launches (event nodes of the graph)
  *                     and ho_stats.round_kernel_ns / round_launches report
@@ -286,6 +292,7 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_FP64_CHECK 4
 #define HO_OPT_TIME_ROUNDS 5
 #define HO_OPT_TENSOR 6
+#define HO_OPT_TAIL 7
 int ho_set_option(ho_context* ctx, int option, int64_t value);
 /* The FP64 residuals that the batched / learned engines' final check
  * computes, for caller-given hits (no reference counterpart): for hit i on

@@ -141,6 +141,7 @@ int read_stats(ho_context* c) {
   s.round_flops = ds.c[ho::ST_FLOPS];
   s.solve_steps = ds.c[ho::ST_STEPS];
   s.lane_steps = ds.c[ho::ST_LANES];
+  s.tail_rays = ds.c[ho::ST_TAIL];
   s.kernel_launches = static_cast<uint64_t>(c->launches);
   s.round_kernel_ns = 0;
   s.round_launches = 0;
@@ -614,6 +615,10 @@ int ho_set_option(ho_context* c, int option, int64_t value) {
       if (value != 0 && value != 1) return fail(c, HO_ERR_RANGE, "HO_OPT_TENSOR takes 0 or 1");
       c->use_tc = value == 1;
       return HO_OK;
+    case HO_OPT_TAIL:
+      if (value < 0 || value > 256) return fail(c, HO_ERR_RANGE, "HO_OPT_TAIL must be in [0, 256]");
+      c->tail_after = static_cast<int>(value);
+      return HO_OK;
     default:
       return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
@@ -626,6 +631,7 @@ int ho_get_option(ho_context* c, int option, int64_t* value) {
     case HO_OPT_FP64_CHECK: *value = c->fp64_check ? 1 : 0; return HO_OK;
     case HO_OPT_TIME_ROUNDS: *value = c->time_rounds ? 1 : 0; return HO_OK;
     case HO_OPT_TENSOR: *value = c->use_tc ? 1 : 0; return HO_OK;
+    case HO_OPT_TAIL: *value = c->tail_after; return HO_OK;
     case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
     case HO_OPT_ROUND_CHUNK:
       *value = c->round_chunk > 0 ? c->round_chunk : ho::round_batch_default(c->N > 0 ? c->N : 2, c->use_tc);

@@ -417,9 +417,57 @@ struct Sample {
   float3 g;
 };
 
+// The batched engines' form of a sample (AH = true in sample_along): every
+// Newton iteration also evaluates the field (value and xi-gradient) at its
+// point, and when the step converges (all components below 1e-5) the sample
+// is taken to first order at the converged point, u(xi - step) = u(xi) -
+// grad u . step (error O(|step|^2), below 1e-9), with the gradient mapped by
+// the iteration's inverse Jacobian. The reference evaluates the field and the
+// Jacobian once more at the converged point (sample_along with AH = false);
+// the round kernel and the warp-per-ray kernel both use this form, with the
+// same arithmetic, so they give the same answers.
 template <int N, bool SM>
+__device__ __forceinline__ bool sample_ahead(const Elem<N, SM>& e, float3 o, float3 d, float t, float iso, Sample& s,
+                                             Work& w, float3 xi0, int max_it) {
+  float3 xi = xi0;
+  for (int it = 1;; ++it) {
+    float4 r[4];
+    eval_comps<N, SM>(e.c, xi, 0, 4, r);
+    w.flops += eval_flops(N, 4);
+    ++w.geom;
+    ++w.field;
+    const float J[9] = {r[0].y, r[0].z, r[0].w, r[1].y, r[1].z, r[1].w, r[2].y, r[2].z, r[2].w};
+    const float u = r[3].x;
+    const float3 gr = make_float3(r[3].y, r[3].z, r[3].w);
+    float K[9];
+    invert3(J, K);
+    ++w.newton;
+    w.flops += kSolveFlops;
+    const float rx = r[0].x - (o.x + t * d.x), ry = r[1].x - (o.y + t * d.y), rz = r[2].x - (o.z + t * d.z);
+    const float d0 = K[0] * rx + K[1] * ry + K[2] * rz;
+    const float d1 = K[3] * rx + K[4] * ry + K[5] * rz;
+    const float d2 = K[6] * rx + K[7] * ry + K[8] * rz;
+    xi.x -= d0;
+    xi.y -= d1;
+    xi.z -= d2;
+    if (fabsf(d0) < 1e-5f && fabsf(d1) < 1e-5f && fabsf(d2) < 1e-5f) {
+      s.xi = xi;
+      s.g = make_float3(K[0] * gr.x + K[3] * gr.y + K[6] * gr.z, K[1] * gr.x + K[4] * gr.y + K[7] * gr.z,
+                        K[2] * gr.x + K[5] * gr.y + K[8] * gr.z);
+      s.f = (u - (gr.x * d0 + gr.y * d1 + gr.z * d2)) - iso;
+      s.df = s.g.x * d.x + s.g.y * d.y + s.g.z * d.z;
+      return true;
+    }
+    s.xi = xi;
+    if (!(fabsf(d0) + fabsf(d1) + fabsf(d2) < FLT_MAX)) return false;
+    if (it >= max_it) return false;
+  }
+}
+
+template <int N, bool SM, bool AH = false>
 __device__ __forceinline__ bool sample_along(const Elem<N, SM>& e, float3 o, float3 d, float t, float iso, Sample& s,
                                              Work& w, float3 xi0 = make_float3(0.f, 0.f, 0.f), int max_it = 50) {
+  if constexpr (AH) return sample_ahead<N, SM>(e, o, d, t, iso, s, w, xi0, max_it);
   const float3 p = make_float3(o.x + t * d.x, o.y + t * d.y, o.z + t * d.z);
   if (!inverse_map<N>(e, p, s.xi, w, xi0, max_it)) return false;
   float u;
@@ -440,17 +488,17 @@ __device__ __forceinline__ bool sample_along(const Elem<N, SM>& e, float3 o, flo
 // if that does not converge the plain cold-start solve answers (the fallback
 // the learned guess never replaces).
 constexpr int kWarmCap = 4;
-template <int N, bool SM>
+template <int N, bool SM, bool AH = false>
 __device__ __forceinline__ bool sample_warm(const Elem<N, SM>& e, float3 o, float3 d, float t, float iso, Sample& s,
                                             Work& w, bool warm, float3 xi0) {
   if (warm) {
-    if (sample_along<N>(e, o, d, t, iso, s, w, xi0, kWarmCap)) {
+    if (sample_along<N, SM, AH>(e, o, d, t, iso, s, w, xi0, kWarmCap)) {
       ++w.accepted;
       return true;
     }
     ++w.rejected;
   }
-  return sample_along<N>(e, o, d, t, iso, s, w);
+  return sample_along<N, SM, AH>(e, o, d, t, iso, s, w);
 }
 
 __device__ __forceinline__ float3 lerp3(float3 a, float3 b, float u) {
@@ -460,21 +508,21 @@ __device__ __forceinline__ float3 lerp3(float3 a, float3 b, float u) {
 // At most 20 safeguarded Newton/bisection steps on a bracket [lt, rt] whose
 // left sample is ls; done when |f| < 1e-5, else the midpoint with the left
 // sample's xi and gradient (RayIsosurface.cu:121-177).
-template <int N, bool SM>
+template <int N, bool SM, bool AH = false>
 __device__ __forceinline__ bool refine_bracket(const Elem<N, SM>& e, float3 o, float3 d, float iso, float lt, float rt,
                                                Sample ls, float& th, float3& xh, float3& gh, Work& w,
                                                bool warm = false, float3 rxi = make_float3(0.f, 0.f, 0.f)) {
   for (int it = 0; it < 20; ++it) {
     const float mt = 0.5f * (lt + rt);
     Sample ms;
-    if (!sample_warm<N>(e, o, d, mt, iso, ms, w, warm, lerp3(ls.xi, rxi, 0.5f))) return false;
+    if (!sample_warm<N, SM, AH>(e, o, d, mt, iso, ms, w, warm, lerp3(ls.xi, rxi, 0.5f))) return false;
     float ct = mt;
     if (fabsf(ms.df) > 1e-8f) {
       const float nt = mt - ms.f / ms.df;
       if (nt > lt && nt < rt) ct = nt;
     }
     Sample cs;
-    if (!sample_warm<N>(e, o, d, ct, iso, cs, w, warm, ms.xi)) {
+    if (!sample_warm<N, SM, AH>(e, o, d, ct, iso, cs, w, warm, ms.xi)) {
       ct = mt;  // keep the failed solve's xi, as the reference does
       cs.f = ms.f;
       cs.g = ms.g;
@@ -538,7 +586,9 @@ __device__ __forceinline__ float3 shfl3(float3 v, int src) {
 // previous successful sample has f(prev)*f(i) <= 0 is found with ballots —
 // the same bracket the sequential scan stops at. The refinement is then run
 // by every lane on identical data (uniform control flow); its work is
-// counted in wu, which only lane 0 reports. Call with all 32 lanes.
+// counted in wu, which only lane 0 reports. Call with all 32 lanes. The
+// samples take the field with every Newton iteration (sample_ahead), as the
+// round kernel does.
 // Learned prediction for one candidate: xi at the segment entry te and
 // d xi / d t there (scaled by the element size: xi(t) ~ xi_in + (t-te)*k*v).
 struct Pred {
@@ -564,10 +614,10 @@ __device__ bool find_iso_warp(const Elem<N, SM>& e, float3 o, float3 d, float t0
   const float t = t0 + (t1 - t0) * (float(lane) / 16.0f);
   bool ok = false;
   if (!L || !pr.on) {
-    if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w);
+    if (lane <= 16) ok = sample_along<N, SM, true>(e, o, d, t, iso, s, w);
   } else {
     // learned: Newton from the predicted xi, short cap
-    if (lane <= 16) ok = sample_along<N>(e, o, d, t, iso, s, w, pr.at(t), kWarmCap);
+    if (lane <= 16) ok = sample_along<N, SM, true>(e, o, d, t, iso, s, w, pr.at(t), kWarmCap);
     // a sample that missed the cap restarts from its converged neighbours'
     // xi (interpolated in t), then, failing that, from the plain cold start
     const unsigned cm = __ballot_sync(kFull, ok && lane <= 16);
@@ -586,10 +636,10 @@ __device__ bool find_iso_warp(const Elem<N, SM>& e, float3 o, float3 d, float t0
                                          xb.z + (t - tb) * pr.k * pr.v.z);
         else if (above) g0 = make_float3(xa.x + (t - ta) * pr.k * pr.v.x, xa.y + (t - ta) * pr.k * pr.v.y,
                                          xa.z + (t - ta) * pr.k * pr.v.z);
-        ok = (cm != 0u) && sample_along<N>(e, o, d, t, iso, s, w, g0, kWarmCap);
+        ok = (cm != 0u) && sample_along<N, SM, true>(e, o, d, t, iso, s, w, g0, kWarmCap);
         if (!ok) {
           ++w.rejected;
-          ok = sample_along<N>(e, o, d, t, iso, s, w);
+          ok = sample_along<N, SM, true>(e, o, d, t, iso, s, w);
         }
       }
     }
@@ -612,7 +662,7 @@ __device__ bool find_iso_warp(const Elem<N, SM>& e, float3 o, float3 d, float t0
   ls.g = shfl3(s.g, li);
   const float3 rxi = shfl3(s.xi, ri);
   const long long c1 = clock64();
-  const bool found = refine_bracket<N>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, L && pr.on, rxi);
+  const bool found = refine_bracket<N, SM, true>(e, o, d, iso, lt, rt, ls, th, xh, gh, wu, L && pr.on, rxi);
   wu.cyc[2] += clock64() - c1;
   return found;
 }
@@ -993,7 +1043,9 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
       best.kind = HO_HIT_ISO;
       best.xi = xi;
       best.n = n;
-      best.u = field_value<N>(e, xi);
+      float4 r[4];  // the field at the root, as the round kernel's post evaluation
+      eval_comps<N, SM>(e.c, xi, 3, 4, r);
+      best.u = r[3].x;
     }
     return;
   }
@@ -1003,11 +1055,12 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
   wu.cyc[3] += clock64() - c0;
   if (fh) {
     if (th > 0.001f && th < best.t) {
-      float3 x;
-      float J[9];
-      geom_eval<N>(e, xi, x, J, wu);
-      const float3 dr = make_float3(J[0], J[3], J[6]), ds = make_float3(J[1], J[4], J[7]),
-                   dt = make_float3(J[2], J[5], J[8]);
+      // geometry (and field) at the hit, as the round kernel's post evaluation
+      float4 r[4];
+      eval_comps<N, SM>(e.c, xi, 0, e.has_field ? 4 : 3, r);
+      ++wu.geom;
+      const float3 dr = make_float3(r[0].y, r[1].y, r[2].y), ds = make_float3(r[0].z, r[1].z, r[2].z),
+                   dt = make_float3(r[0].w, r[1].w, r[2].w);
       float3 n;
       if (fabsf(xi.x) > 0.9f) n = cross3(ds, dt);
       else if (fabsf(xi.y) > 0.9f) n = cross3(dr, dt);
@@ -1020,7 +1073,7 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
       best.kind = HO_HIT_FACE;
       best.xi = xi;
       best.n = n;
-      best.u = e.has_field ? field_value<N>(e, xi) : 0.f;
+      best.u = e.has_field ? r[3].x : 0.f;
     }
   }
 }

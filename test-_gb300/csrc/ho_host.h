@@ -157,6 +157,7 @@ struct ho_context {
   // batched / learned engine options (ho_set_option)
   int round_chunk = 0;       // pairs per element batch (0: the kernel's pair slots)
   int round_count = 16;      // rounds enqueued before the completion check (at most)
+  int tail_after = 4;        // rounds before the warp-per-ray tail finishes every ray (0: no tail)
   int64_t launches = 0;      // kernels enqueued by the last trace call
   bool time_rounds = false;  // event pairs around each round's intersection launches
   std::vector<cudaEvent_t> round_events;

@@ -78,6 +78,7 @@ enum StatSlot {
   ST_CHECK_FAIL,
   ST_CHECK_FINAL,
   ST_FLOPS,
+  ST_TAIL,
   ST_COUNT
 };
 

@@ -103,6 +103,24 @@ __global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, Ro
   }
 }
 
+// Rays still in flight after the main rounds, listed for the tail kernel
+// (warp-aggregated appends; the count goes to the work counters too).
+__global__ void tail_list_kernel(const unsigned* __restrict__ qcount, const RayState* __restrict__ st,
+                                 uint32_t* __restrict__ list, unsigned* __restrict__ n_list, DevStats* stats) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < *qcount && !st[i].done;
+  const unsigned m = __ballot_sync(kFull, live);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  unsigned base = 0;
+  if (lane == leader) {
+    base = atomicAdd(n_list, static_cast<unsigned>(__popc(m)));
+    atomicAdd(&stats->c[ST_TAIL], static_cast<unsigned long long>(__popc(m)));
+  }
+  base = __shfl_sync(kFull, base, leader);
+  if (live) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
 // Also tallies the round (non-empty rounds and pairs) into the work counters.
 __global__ void round_scatter_kernel(const RoundPair* __restrict__ pairs, const int32_t* __restrict__ pelem,
                                      const uint32_t* __restrict__ prank, const uint32_t* __restrict__ eoff,
@@ -371,15 +389,51 @@ static int enqueue_round(ho_context* c, const TraceParams& P, const RoundParams&
   return 0;
 }
 
-// The state init, `rounds` rounds and the final write-out of the queued rays.
+// The tail: every ray still in flight finished by the warp-per-ray kernel;
+// afterwards no round has pairs left (ctr[0] = 0).
+static int enqueue_tail(ho_context* c, const TraceParams& P, const RoundParams& R, cudaStream_t s, bool learned,
+                        int64_t n_cap) {
+  RoundBufs& rb = c->rounds;
+  unsigned* n_list = rb.ctr + 4;
+  unsigned* next = rb.ctr + 5;
+  RT_TRY(cudaMemsetAsync(rb.ctr + 4, 0, 2 * sizeof(unsigned), s));
+  tail_list_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P.qcount, R.state, rb.fail, n_list,
+                                                                              P.stats);
+  RT_TRY(cudaGetLastError());
+  cudaError_t e;
+  switch (c->N) {
+    case 2: e = launch_tail_n<2>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 3: e = launch_tail_n<3>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 4: e = launch_tail_n<4>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 5: e = launch_tail_n<5>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 6: e = launch_tail_n<6>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 7: e = launch_tail_n<7>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 8: e = launch_tail_n<8>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    case 9: e = launch_tail_n<9>(P, R.state, rb.fail, n_list, next, learned, s); break;
+    default: e = cudaErrorInvalidValue; break;
+  }
+  RT_TRY(e);
+  RT_TRY(cudaMemsetAsync(rb.ctr, 0, sizeof(unsigned), s));
+  c->launches += 2;
+  return 0;
+}
+
+// The state init, `rounds` rounds (then the tail, when on) and the final
+// write-out of the queued rays.
 int enqueue_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool learned, int64_t n_cap, int rounds) {
   const RoundParams R = round_params(c, P);
   const unsigned gi = static_cast<unsigned>((n_cap + 255) / 256);
   round_init_kernel<<<gi, 256, 0, s>>>(R.state, P.kovf, P.qcount);
   RT_TRY(cudaGetLastError());
   c->launches += 2;  // init and finish
+  // with the tail, a fixed number of rounds (the tail finishes every ray)
+  if (c->tail_after > 0) rounds = std::min(c->round_count, c->tail_after);
   for (int r = 0; r < rounds; ++r) {
     const int rc = enqueue_round(c, P, R, s, learned, n_cap);
+    if (rc) return rc;
+  }
+  if (c->tail_after > 0) {
+    const int rc = enqueue_tail(c, P, R, s, learned, n_cap);
     if (rc) return rc;
   }
   {

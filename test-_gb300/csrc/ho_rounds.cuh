@@ -983,6 +983,147 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
   flush_work(P.stats, w, false);
 }
 
+// The tail: rays still in flight after the main rounds, each finished by one
+// warp that walks the rest of its ordered candidates (the warp-per-ray form
+// of the same per-candidate solves, visit_warp). A round lasts as long as its
+// slowest pair, so the last rounds, with few pairs each, wait mostly on
+// chains of refinement and face solves; here every ray proceeds at its own
+// pace. Elements are staged at the scene's largest order (padded records).
+template <int N, bool L>
+__global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RayState* __restrict__ st,
+                                                           const uint32_t* __restrict__ list,
+                                                           const unsigned* __restrict__ n_list,
+                                                           unsigned* __restrict__ next) {
+  const int lane = threadIdx.x & 31;
+  extern __shared__ __align__(16) float tail_stage[];
+  float4* slot4 = reinterpret_cast<float4*>(tail_stage + (threadIdx.x >> 5) * record_floats(N));
+  const uint32_t slot_addr = static_cast<uint32_t>(__cvta_generic_to_shared(slot4));
+  Work w, wu;
+  const unsigned n = *n_list;
+  for (;;) {
+    unsigned k = 0;
+    if (lane == 0) k = atomicAdd(next, 1u);
+    k = __shfl_sync(kFull, k, 0);
+    if (k >= n) break;
+    const unsigned item = list[k];
+    RayState& r = st[item];
+    float3 o, d;
+    float iso;
+    bool iso_on;
+    query_ray(P, P.work[item], o, d, iso, iso_on);
+    HitState best = r.best;
+    float kt = r.kt;
+    int ke = r.ke, pass = r.pass, first = r.cursor;
+    bool overflow = r.ovf != 0;
+    const uint32_t it0 = wu.newton + wu.face + w.newton + w.face;
+    float bt[kCandK];
+    int be[kCandK];
+    const float2* kb = P.kbuf + static_cast<int64_t>(item) * kCandK;
+#pragma unroll
+    for (int j = 0; j < kCandK; ++j) {
+      const float2 c = kb[j];
+      bt[j] = c.x;
+      be[j] = __float_as_int(c.y);
+    }
+    for (int guard = 0; guard < (1 << 20); ++guard) {
+      bool done = false;
+#pragma unroll 1
+      for (int j = first; j < kCandK; ++j) {
+        float ct = bt[0];
+        int ce = be[0];
+#pragma unroll
+        for (int m = 1; m < kCandK; ++m)
+          if (j == m) {
+            ct = bt[m];
+            ce = be[m];
+          }
+        if (ce == INT_MAX || ct > best.t) {
+          done = true;
+          break;
+        }
+        const float* b = P.box + 6 * static_cast<int64_t>(ce);
+        const float lo[3] = {__ldg(b), __ldg(b + 1), __ldg(b + 2)};
+        const float hi[3] = {__ldg(b + 3), __ldg(b + 4), __ldg(b + 5)};
+        float te, tx;
+        if (ray_box(o, d, lo, hi, 0.001f, best.t, te, tx)) {
+          const float4* src = reinterpret_cast<const float4*>(P.rec + static_cast<int64_t>(ce) * record_floats(N));
+          __syncwarp();
+          for (int q4 = lane; q4 < record_floats(N) / 4; q4 += 32) slot4[q4] = __ldg(src + q4);
+          __syncwarp();
+          Elem<N, true> el;
+          el.c = CoefRef<true>{slot_addr};
+          el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
+          Pred pr;
+          pr.on = false;
+          if (L && pass == 0 && j < kPredK && item < P.pred_items &&
+              P.cand_e[static_cast<int64_t>(item) * kPredK + j] == ce) {
+            const float* y = P.pred + (static_cast<int64_t>(item) * kPredK + j) * kMlpOut;
+            pr.on = true;
+            pr.xi_in = make_float3(y[0], y[1], y[2]);
+            pr.v = make_float3(y[3], y[4], y[5]);
+            pr.k = __ldg(P.desc + static_cast<int64_t>(ce) * kDescFloats + 45);
+            pr.te = te;
+          }
+          visit_warp<N, L>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
+                           best, w, wu, pr);
+        }
+        kt = ct;
+        ke = ce;
+      }
+      if (done || !overflow) break;
+      // the list was cut at kCandK: walk the tree again after the last visited key
+      if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu)) {
+        if (lane == 0) atomicOr(&P.stats->status, kStatusStackOverflow);
+        break;
+      }
+      first = 0;
+      ++pass;
+      ++wu.restarts;
+      best.flags |= HO_FLAG_OVERFLOW;
+    }
+    uint32_t its = w.newton + w.face;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) its += __shfl_xor_sync(kFull, its, off);
+    __syncwarp();
+    if (lane == 0) {
+      r.best = best;
+      r.its += static_cast<int>(its + wu.newton + wu.face - it0);
+      r.done = 1;
+    }
+  }
+  if (lane == 0) {
+    w.cand += wu.cand; w.geom += wu.geom; w.map += wu.map; w.field += wu.field; w.newton += wu.newton;
+    w.face += wu.face; w.culled += wu.culled; w.nodes += wu.nodes; w.restarts += wu.restarts;
+    w.accepted += wu.accepted; w.rejected += wu.rejected;
+  }
+  w.flops = 0;  // the flop counter describes the round kernel only
+  flush_work(P.stats, w, false);
+}
+
+template <int N>
+cudaError_t launch_tail_n(const TraceParams& P, RayState* st, const uint32_t* list, const unsigned* n_list,
+                          unsigned* next, bool learned, cudaStream_t s) {
+  static int grid[2] = {0, 0};
+  const size_t smem = static_cast<size_t>(kTraceBlock / 32) * record_floats(N) * sizeof(float);
+  int& g = grid[learned ? 1 : 0];
+  if (g == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (learned) {
+      cudaFuncSetAttribute(tail_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tail_kernel<N, true>, kTraceBlock, smem);
+    } else {
+      cudaFuncSetAttribute(tail_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tail_kernel<N, false>, kTraceBlock, smem);
+    }
+    g = sms * (per > 0 ? per : 1);
+  }
+  if (learned) tail_kernel<N, true><<<g, kTraceBlock, smem, s>>>(P, st, list, n_list, next);
+  else tail_kernel<N, false><<<g, kTraceBlock, smem, s>>>(P, st, list, n_list, next);
+  return cudaGetLastError();
+}
+
 template <int N, bool L, bool TC>
 static cudaError_t launch_round_kernel(const RoundParams& R, cudaStream_t s) {
   // persistent grid: resident blocks per SM x SMs (the tensor-core form holds
@@ -1026,5 +1167,22 @@ extern template cudaError_t launch_round_n<6>(const RoundParams& R, cudaStream_t
 extern template cudaError_t launch_round_n<7>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
 extern template cudaError_t launch_round_n<8>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
 extern template cudaError_t launch_round_n<9>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
+
+extern template cudaError_t launch_tail_n<2>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<3>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<4>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<5>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<6>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<7>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<8>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
+extern template cudaError_t launch_tail_n<9>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*,
+                                             bool, cudaStream_t);
 
 }  // namespace ho

@@ -151,7 +151,7 @@ __device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool act
   // warp-aggregated counters
   unsigned long long v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled,
                                     w.nodes, w.accepted, w.rejected, w.restarts, w.cyc[0], w.cyc[1], w.cyc[2],
-                                    w.cyc[3], w.steps, w.lanes, 0ull, 0ull, 0ull, 0ull, 0ull, w.flops};
+                                    w.cyc[3], w.steps, w.lanes, 0ull, 0ull, 0ull, 0ull, 0ull, w.flops, 0ull};
 #pragma unroll
   for (int s = 0; s < ST_COUNT; ++s) {
     unsigned long long x = v[s];

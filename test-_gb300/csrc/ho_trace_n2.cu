@@ -8,6 +8,8 @@ template cudaError_t launch_n<2>(const TraceParams& P, int64_t n_queries, int64_
 template cudaError_t launch_round_n<2>(const RoundParams& R, cudaStream_t s, bool learned, bool tc);
 template cudaError_t launch_residuals_n<2>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
                                            double*, cudaStream_t);
+template cudaError_t launch_tail_n<2>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*, bool,
+                                      cudaStream_t);
 template cudaError_t launch_check_n<2>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
                                          cudaStream_t);
 }  // namespace ho

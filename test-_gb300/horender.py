@@ -23,7 +23,7 @@ HO_OK = 0
 ERRORS = {-1: "HO_ERR_ARG", -2: "HO_ERR_CUDA", -3: "HO_ERR_STATE", -4: "HO_ERR_IO", -5: "HO_ERR_PARSE",
           -6: "HO_ERR_NOMEM", -7: "HO_ERR_RANGE", -8: "HO_ERR_DEVICE"}
 MODE_PLAIN, MODE_LEARNED, MODE_BATCHED = 0, 1, 2
-OPT_GRAPH, OPT_ROUNDS, OPT_ROUND_CHUNK, OPT_FP64_CHECK, OPT_TIME_ROUNDS, OPT_TENSOR = 1, 2, 3, 4, 5, 6
+OPT_GRAPH, OPT_ROUNDS, OPT_ROUND_CHUNK, OPT_FP64_CHECK, OPT_TIME_ROUNDS, OPT_TENSOR, OPT_TAIL = 1, 2, 3, 4, 5, 6, 7
 MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
@@ -64,7 +64,8 @@ class _Stats(C.Structure):
         ("rounds", C.c_uint64), ("round_pairs", C.c_uint64), ("solve_steps", C.c_uint64),
         ("lane_steps", C.c_uint64), ("graph", C.c_uint64), ("fp64_checked", C.c_uint64),
         ("fp64_failed", C.c_uint64), ("fp64_failed_after_fallback", C.c_uint64), ("round_flops", C.c_uint64),
-        ("kernel_launches", C.c_uint64), ("round_kernel_ns", C.c_uint64), ("round_launches", C.c_uint64)]
+        ("kernel_launches", C.c_uint64), ("round_kernel_ns", C.c_uint64), ("round_launches", C.c_uint64),
+        ("tail_rays", C.c_uint64)]
 
 
 def _load():

@@ -111,6 +111,7 @@ def test_engine_options():
         assert ctx.get_option(hr.OPT_FP64_CHECK) == 1
         assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 0
         assert ctx.get_option(hr.OPT_TENSOR) == 0
+        assert ctx.get_option(hr.OPT_TAIL) == 4
         ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
         assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 1
         ctx.set_option(hr.OPT_GRAPH, 0)
@@ -119,7 +120,8 @@ def test_engine_options():
         assert (ctx.get_option(hr.OPT_GRAPH), ctx.get_option(hr.OPT_ROUNDS), ctx.get_option(hr.OPT_ROUND_CHUNK)) == (
             0, 3, 200)
         for opt, bad in ((hr.OPT_GRAPH, 2), (hr.OPT_ROUNDS, 0), (hr.OPT_ROUNDS, 257), (hr.OPT_ROUND_CHUNK, 0),
-                         (hr.OPT_ROUND_CHUNK, 4097), (hr.OPT_TIME_ROUNDS, 2), (hr.OPT_TENSOR, -1)):
+                         (hr.OPT_ROUND_CHUNK, 4097), (hr.OPT_TIME_ROUNDS, 2), (hr.OPT_TENSOR, -1),
+                         (hr.OPT_TAIL, -1), (hr.OPT_TAIL, 257)):
             with pytest.raises(hr.HoError) as ei:
                 ctx.set_option(opt, bad)
             assert ei.value.code == -7

@@ -136,7 +136,7 @@ def test_graph_rounds_and_chunks_give_the_same_hits(small):
 
     ctx.set_option(hr.OPT_GRAPH, 0)
     h0, s0 = run()
-    assert s0["graph"] == 0 and s0["rounds"] > 1 and s0["round_pairs"] == s0["candidates"]
+    assert s0["graph"] == 0 and s0["rounds"] > 1 and s0["round_pairs"] <= s0["candidates"]
     ctx.set_option(hr.OPT_GRAPH, 1)
     run()
     h1, s1 = run()
@@ -163,8 +163,52 @@ def test_graph_rounds_and_chunks_give_the_same_hits(small):
     for h, s in ((h1, s1), (h2, s2), (h3, s3), (h4, s4), (h5, s5), (h6, s6)):
         assert np.array_equal(h["kind"], h0["kind"]) and np.array_equal(h["elem"], h0["elem"])
         assert np.array_equal(h["face"], h0["face"]) and np.array_equal(h["t"], h0["t"])
-        assert (s["rounds"], s["round_pairs"], s["newton_iters"], s["face_iters"]) == (
-            s0["rounds"], s0["round_pairs"], s0["newton_iters"], s0["face_iters"])
+        assert (s["candidates"], s["newton_iters"], s["face_iters"]) == (
+            s0["candidates"], s0["newton_iters"], s0["face_iters"])
+        if s is not s2:  # one round before the tail leaves more rays to it
+            assert (s["rounds"], s["round_pairs"], s["tail_rays"]) == (s0["rounds"], s0["round_pairs"], s0["tail_rays"])
+
+
+@pytest.mark.parametrize("mode", ["batched", "learned"])
+def test_tail_gives_the_same_hits(small, mode):
+    """Rays finished by the warp-per-ray tail get the answers the rounds
+    would have, with the tail after 1 or 2 rounds and without a tail
+    (batched): the same hit kind, element, face and t; xi and u within 1e-5
+    (the face Newton of the two kernels rounds differently in the last bits
+    on a few rays). Learned: a tail
+    that starts before the 4th round also takes network starts, and the
+    warp-per-ray kernel restarts a missed warm sample from its converged
+    neighbours where the round kernel restarts cold, so the answers agree to
+    the solvers' tolerance."""
+    ctx, w, arrs, osc = small
+    W = H = 80
+    if mode == "learned":
+        ctx.train_mlp(n_samples=200_000, steps=300, batch=2048, lr=2e-3, seed=4)
+        ctx.set_mode(hr.MODE_LEARNED)
+    else:
+        ctx.set_mode(hr.MODE_BATCHED)
+    runs = []
+    try:
+        for tail in (0, 1, 2):
+            ctx.set_option(hr.OPT_TAIL, tail)
+            _, h = ctx.render(w.camera, w.isovalues, W, H, want_rgb=False, want_hits=True)
+            runs.append((h[0].reshape(-1).copy(), ctx.stats()))
+    finally:
+        ctx.set_option(hr.OPT_TAIL, 4)
+        ctx.set_mode(hr.MODE_BATCHED)
+    (h0, s0), (h1, s1), (h2, s2) = runs
+    assert s0["tail_rays"] == 0 and s1["tail_rays"] > 0 and s1["tail_rays"] >= s2["tail_rays"]
+    for h, s in ((h1, s1), (h2, s2)):
+        if mode == "batched":
+            for k in ("kind", "elem", "face", "t"):
+                assert np.array_equal(h[k], h0[k]), k
+            assert np.abs(h["xi"] - h0["xi"]).max() < 1e-5 and np.abs(h["u"] - h0["u"]).max() < 1e-5
+            assert s["candidates"] == s0["candidates"]
+        else:
+            same = classify(h, h0)
+            assert same.mean() >= 0.999
+            m = same & (h0["kind"] > 0)
+            assert np.abs(h["t"][m] - h0["t"][m]).max() < 2e-4
 
 
 def test_autotune_picks_a_candidate_and_keeps_results(small):
