@@ -1,12 +1,11 @@
 """Float64 CPU restatement of the learned mode's network (test
-infrastructure): 48 -> 128 -> 128 -> 128 -> 8, GELU (erf form), masked MSE on
+infrastructure): 48 -> 128 -> 128 -> 128 -> 8, GELU (tanh form), masked MSE on
 outputs 0..5. Operands are rounded to BF16 where the GPU kernels keep BF16
 (inputs, weights, hidden activations, output and hidden gradients), so the
 comparison isolates the kernels' arithmetic from the storage format."""
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
 
 DIMS = [(48, 128), (128, 128), (128, 128), (128, 8)]
 N_PARAMS = sum(i * o + o for i, o in DIMS)
@@ -30,12 +29,16 @@ def unflatten(flat):
     return out
 
 
-def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+A, B = np.sqrt(2.0 / np.pi), 0.044715
+
+
+def gelu(z):  # tanh form (Hendrycks and Gimpel)
+    return 0.5 * z * (1.0 + np.tanh(A * (z + B * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    th = np.tanh(A * (z + B * z ** 3))
+    return 0.5 * (1.0 + th) + 0.5 * z * (1.0 - th * th) * A * (1.0 + 3.0 * B * z * z)
 
 
 def forward(flat, X):
