@@ -294,6 +294,27 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_TENSOR 6
 #define HO_OPT_TAIL 7
 int ho_set_option(ho_context* ctx, int option, int64_t value);
+/* Path tracing with Lambertian bounces (replaces: render_kernel at spp
+ * samples and depth max_depth, FEM-AABB/raytracer.cu:410-476, with
+ * ray_color :362-406 and scatter :60-98). Per pixel and sample one path
+ * through a jittered point of the pixel; each intersection multiplies the
+ * path's attenuation by the albedo (boundary face 0 of a hex 0.1/0.2/0.8,
+ * every other hit 0.5 grey, as main.cu:39-41 and raytracer.cu:248 assign);
+ * a miss adds attenuation x sky; a path still going after max_depth
+ * intersections adds black. Image = gamma-2 average over the samples, 8 bits,
+ * rows as ho_render, one image per isovalue. Random numbers are hashed from
+ * (seed, path, bounce), so an image is reproducible for a given seed (the
+ * reference seeds curand with the time). Every bounce is one call of the
+ * intersection engine in the context's solver mode. rays_traced (may be
+ * NULL): ray queries over all bounces. W * H * spp must stay below 2^32. */
+int ho_path_trace(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int W, int H, int spp,
+                  int max_depth, uint64_t seed, int iso_zero_disables, uint8_t* rgb_out, int64_t* rays_traced);
+/* Device-buffer form; synchronises the stream once per bounce (it reads the
+ * number of paths still alive). */
+int ho_path_trace_device(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int W, int H,
+                         int spp, int max_depth, uint64_t seed, int iso_zero_disables, uint8_t* rgb_dev,
+                         int64_t* rays_traced, void* stream);
+
 /* The FP64 residuals that the batched / learned engines' final check
  * computes, for caller-given hits (no reference counterpart): for hit i on
  * ray i (rays as in ho_intersect), out[2i] = the largest component of

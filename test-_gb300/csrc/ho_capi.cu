@@ -563,6 +563,59 @@ int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso
   return read_stats(c);
 }
 
+int ho_path_trace_device(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int spp,
+                         int max_depth, uint64_t seed, int iso_zero_disables, uint8_t* rgb_dev, int64_t* rays_traced,
+                         void* stream) {
+  if (!c) return HO_ERR_ARG;
+  if (!cam || !rgb_dev) return fail(c, HO_ERR_ARG, "null argument");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (W <= 0 || H <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
+  if (spp < 1 || spp > 65536) return fail(c, HO_ERR_RANGE, "spp must be in [1, 65536]");
+  if (max_depth < 1 || max_depth > 64) return fail(c, HO_ERR_RANGE, "max_depth must be in [1, 64]");
+  const int64_t npix = static_cast<int64_t>(W) * H;
+  if (npix > (int64_t(1) << 30) || npix * spp > (int64_t(1) << 32))
+    return fail(c, HO_ERR_RANGE, "too many paths (W * H * spp must stay below 2^32)");
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  ho::TraceArgs a;
+  camera_basis(*cam, W, H, a);
+  ho::CamArgs ca;
+  ca.origin = make_float3(a.origin[0], a.origin[1], a.origin[2]);
+  ca.llc = make_float3(a.llc[0], a.llc[1], a.llc[2]);
+  ca.horiz = make_float3(a.horiz[0], a.horiz[1], a.horiz[2]);
+  ca.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
+  ca.width = W;
+  ca.height = H;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  int64_t rays = 0;
+  for (int k = 0; k < n_iso; ++k) {
+    const bool on = !(iso_zero_disables && iso[k] == 0.0f);
+    rc = ho::path_trace(c, ca, iso[k], on, spp, max_depth, seed, rgb_dev + static_cast<size_t>(k) * npix * 3, &rays,
+                        s);
+    if (rc < 0) return rc;
+    if (rc > 0) return cuda_fail(c, rc, "path tracing");
+  }
+  if (rays_traced) *rays_traced = rays;
+  return HO_OK;
+}
+
+int ho_path_trace(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int spp,
+                  int max_depth, uint64_t seed, int iso_zero_disables, uint8_t* rgb_out, int64_t* rays_traced) {
+  if (!c) return HO_ERR_ARG;
+  if (!rgb_out) return fail(c, HO_ERR_ARG, "rgb_out is NULL");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (W <= 0 || H <= 0) return fail(c, HO_ERR_ARG, "image size must be positive");
+  const size_t bytes = static_cast<size_t>(W) * H * n_iso * 3;
+  if ((rc = ensure_buf(c, c->d_rgb, c->rgb_cap, bytes, "cudaMalloc(rgb)"))) return rc;
+  rc = ho_path_trace_device(c, cam, iso, n_iso, W, H, spp, max_depth, seed, iso_zero_disables, c->d_rgb, rays_traced,
+                            c->stream);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(rgb_out, c->d_rgb, bytes, cudaMemcpyDeviceToHost, c->stream), "read image");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return HO_OK;
+}
+
 int ho_hit_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out) {
   if (!c) return HO_ERR_ARG;
   if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");

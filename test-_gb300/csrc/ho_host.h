@@ -193,6 +193,10 @@ struct TraceArgs {
   uint8_t* rgb = nullptr;       // optional (camera mode)
 };
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s);
+// Path tracing of one image at one isovalue (ho_path.cu); returns a
+// cudaError_t, or a negative HO_ status from the engine (message set).
+int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int spp, int max_depth, uint64_t seed,
+               uint8_t* rgb, int64_t* rays_traced, cudaStream_t s);
 // The FP64 check's residuals for caller-given hits (ho_rounds.cu).
 int launch_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out, cudaStream_t s);
 }  // namespace ho

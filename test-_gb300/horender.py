@@ -90,6 +90,10 @@ def _load():
     L.ho_render_views.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp]
     L.ho_render_views_device.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp]
     L.ho_render_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp, vp]
+    L.ho_path_trace.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, i32, C.c_uint64, i32, vp,
+                                C.POINTER(i64)]
+    L.ho_path_trace_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, i32, C.c_uint64, i32, vp,
+                                       C.POINTER(i64), vp]
     L.ho_intersect.argtypes = [vp, i64, vp, f32, i32, vp]
     L.ho_hit_residuals.argtypes = [vp, i64, vp, vp, vp]
     L.ho_intersect_device.argtypes = [vp, i64, vp, f32, i32, vp, vp]
@@ -335,6 +339,27 @@ class Context:
         cam = camera._c()
         self._ck(lib.ho_render_device(self.h, C.byref(cam), _p(iso), iso.size, width, height,
                                       int(iso_zero_disables), rgb_ptr, hits_ptr, stream_ptr))
+
+    def path_trace(self, camera: Camera, isovalues, width, height, spp=1, max_depth=4, seed=1,
+                   iso_zero_disables: bool = True):
+        """Path-traced images (n_iso, H, W, 3) uint8 and the ray queries traced."""
+        iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
+        out = np.zeros((iso.size, height, width, 3), np.uint8)
+        rays = C.c_int64(0)
+        cam = camera._c()
+        self._ck(lib.ho_path_trace(self.h, C.byref(cam), _p(iso), iso.size, width, height, int(spp), int(max_depth),
+                                   int(seed), int(iso_zero_disables), _p(out), C.byref(rays)))
+        return out, int(rays.value)
+
+    def path_trace_device(self, camera: Camera, isovalues, width, height, rgb_ptr, stream_ptr, spp=1, max_depth=4,
+                          seed=1, iso_zero_disables: bool = True) -> int:
+        iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
+        rays = C.c_int64(0)
+        cam = camera._c()
+        self._ck(lib.ho_path_trace_device(self.h, C.byref(cam), _p(iso), iso.size, width, height, int(spp),
+                                          int(max_depth), int(seed), int(iso_zero_disables), rgb_ptr, C.byref(rays),
+                                          stream_ptr))
+        return int(rays.value)
 
     def intersect(self, rays: np.ndarray, iso: float, iso_enabled: bool = True) -> np.ndarray:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)

@@ -1,0 +1,70 @@
+"""The path-tracing layer (ho_path_trace) against its CPU restatement with the
+oracle tracing every bounce (tests/path_ref.py), on the small curved-hex
+workload. Paths whose hit differs from the oracle's (a near-tie, see
+test_gpu_parity) take a different direction afterwards, so the images are
+compared per pixel with a tolerance: at least 97% of the pixels within 3
+levels of 255 and a mean difference below 1 level; the ray counts agree
+within 1%."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import horender as hr
+import path_ref
+from conftest import scene_arrays_from_ctx
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small(oracle):
+    ctx, w = hr.workload_context("hex4_p4")
+    arrs = scene_arrays_from_ctx(ctx)
+    return ctx, w, oracle.OracleScene(arrs)
+
+
+@pytest.mark.parametrize("iso_on", [True, False])
+def test_path_trace_matches_cpu_restatement(small, iso_on):
+    ctx, w, osc = small
+    W, H, spp, depth, seed = 40, 32, 2, 4, 7
+    iso = w.isovalues[0] if iso_on else 0.0
+    ctx.set_mode(hr.MODE_BATCHED)
+    img, rays = ctx.path_trace(w.camera, [iso], W, H, spp=spp, max_depth=depth, seed=seed, iso_zero_disables=True)
+    ref, rays_ref = path_ref.path_trace(osc, w.camera, W, H, iso, iso_on, spp, depth, seed)
+    diff = np.abs(img[0].astype(np.int32) - ref.astype(np.int32))
+    print(f"path trace iso {iso_on}: rays {rays} / {rays_ref}, within 3: {(diff.max(axis=2) <= 3).mean():.4f}, "
+          f"mean {diff.mean():.3f}")
+    assert abs(rays - rays_ref) <= max(10, rays_ref // 100)
+    assert (diff.max(axis=2) <= 3).mean() >= 0.97
+    assert diff.mean() < 1.0
+    assert rays > W * H * spp  # secondary rays were traced
+
+
+def test_path_trace_is_reproducible_and_seeded(small):
+    ctx, w, osc = small
+    ctx.set_mode(hr.MODE_BATCHED)
+    a, ra = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=2, max_depth=3, seed=11)
+    b, rb = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=2, max_depth=3, seed=11)
+    c, _ = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=2, max_depth=3, seed=12)
+    assert np.array_equal(a, b) and ra == rb
+    assert not np.array_equal(a, c)
+
+
+def test_path_trace_depth_one_is_sky_or_black(small):
+    """One intersection per path: a path that hits anything is black, a miss
+    sees the sky, so every pixel is either black or a sky colour."""
+    ctx, w, osc = small
+    img, rays = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=1, max_depth=1, seed=3)
+    assert rays == 32 * 24
+    px = img[0].reshape(-1, 3).astype(np.int32)
+    black = (px == 0).all(axis=1)
+    assert black.any() and (~black).any()
+    assert (px[~black, 2] >= px[~black, 0]).all()  # sky: blue >= red
+
+
+def test_path_trace_argument_checks(small):
+    ctx, w, osc = small
+    for kw in (dict(spp=0), dict(max_depth=0), dict(max_depth=65)):
+        with pytest.raises(hr.HoError):
+            ctx.path_trace(w.camera, w.isovalues, 8, 8, **kw)
