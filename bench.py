@@ -218,7 +218,12 @@ def cpu_baseline(workload, seconds, n_iso_sample=None):
 def run_reference(args, rank, world):
     import horender as hr
 
-    w = hr.WORKLOADS[hr.MULTIVIEW[args.workload][0] if args.workload in hr.MULTIVIEW else args.workload]
+    if args.workload in hr.MULTIVIEW:
+        w = hr.WORKLOADS[hr.MULTIVIEW[args.workload][0]]
+    elif args.workload in hr.PATHS:
+        w = hr.WORKLOADS[hr.PATHS[args.workload][0]]
+    else:
+        w = hr.WORKLOADS[args.workload]
     if rank != 0:
         return
     per_step = []
@@ -248,10 +253,14 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     multi = args.workload in hr.MULTIVIEW
+    path = args.workload in hr.PATHS
     if multi:  # many views of one scene in one call
         base, view_kw = hr.MULTIVIEW[args.workload]
         w = hr.WORKLOADS[base]
         cams, vw, vh, visos = hr.sphere_views(**view_kw)
+    elif path:  # path tracing: one sample pass per step, every bounce through the engine
+        base, path_kw = hr.PATHS[args.workload]
+        w = hr.WORKLOADS[base]
     else:
         w = hr.WORKLOADS[args.workload]
     if args.width and args.height:
@@ -272,10 +281,15 @@ def run_gpu(args, rank, world):
     sp = stream.cuda_stream
 
     def step():
+        """One step; returns its ray queries."""
         if multi:
             ctx.render_views_device(cams, vw, vh, visos, rgb.data_ptr(), None, sp)
+        elif path:
+            return ctx.path_trace_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), sp, iso_zero_disables=False,
+                                         **path_kw)
         else:
             ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
+        return nq
 
     tuned = {}
 
@@ -297,6 +311,7 @@ def run_gpu(args, rank, world):
         barrier(world)
         torch.cuda.synchronize()
         evs = []
+        rays = 0
         with ClockSampler(local) as clk:
             with torch.cuda.stream(stream):
                 for _ in range(args.steps):
@@ -304,7 +319,7 @@ def run_gpu(args, rank, world):
                     a = torch.cuda.Event(enable_timing=True)
                     b = torch.cuda.Event(enable_timing=True)
                     a.record(stream)
-                    step()
+                    rays += step()
                     b.record(stream)
                     evs.append((a, b))
                     s_step = ctx.stats()  # the call has synchronised; this reads its host copy
@@ -314,7 +329,7 @@ def run_gpu(args, rank, world):
         barrier(world)
         total = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / 1e3, world)
         st = dict(st, timed=per)
-        return total, st, clk
+        return total, st, clk, rays
 
     train = None
     if args.mode in ("all", "learned"):
@@ -328,14 +343,16 @@ def run_gpu(args, rank, world):
     codes = {"plain": hr.MODE_PLAIN, "batched": hr.MODE_BATCHED, "learned": hr.MODE_LEARNED}
     if args.mode != "all":
         modes = [args.mode]
-    elif multi:  # plain (one thread per ray, padded to the largest order) would take minutes per step here
+    elif multi or path:  # plain (one thread per ray, padded to the largest order) would take minutes per step here
         modes = ["batched", "learned"]
     else:
         modes = ["plain", "batched", "learned"]
     for mode in modes:
         results[mode] = timed(codes[mode])
     head = "learned" if "learned" in results else ("batched" if "batched" in results else "plain")
-    total_s, st, clk = results[head]
+    total_s, st, clk, rays_timed = results[head]
+    if path:
+        nq = rays_timed // args.steps  # ray queries of one sample pass over all bounces
     queries = sum_over_ranks(nq * args.steps, world)
     value = queries / total_s / 1e6
     launch_s = total_s / args.steps
@@ -344,7 +361,7 @@ def run_gpu(args, rank, world):
     def mode_summary(m):
         if m not in results:
             return None
-        t, stt, _ = results[m]
+        t, stt, _, _ = results[m]
         return {"value": queries / t / 1e6, "ms_per_step": t / args.steps * 1e3, "newton_iters": stt["newton_iters"],
                 "face_iters": stt["face_iters"], "geom_evals": stt["geom_evals"]}
 
@@ -369,6 +386,7 @@ def run_gpu(args, rank, world):
 
     # e2e: public API, host image buffer, D2H inside the timed region
     host_rgb = torch.empty((nq, 3) if multi else (n_iso, H, W, 3), dtype=torch.uint8).pin_memory()
+    e2e_rays = 0
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
@@ -376,10 +394,14 @@ def run_gpu(args, rank, world):
     for _ in range(0 if args.no_e2e else args.steps):
         if multi:
             ctx.render_views(cams, vw, vh, visos, rgb_out=host_rgb.numpy())
+        elif path:
+            img, r = ctx.path_trace(w.camera, w.isovalues, W, H, iso_zero_disables=False, **path_kw)
+            host_rgb.numpy()[...] = img
+            e2e_rays += r
         else:
             ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    e2e = None if args.no_e2e else queries / e2e_s / 1e6
+    e2e = None if args.no_e2e else (e2e_rays if path else queries) / e2e_s / 1e6
     del host_rgb
 
     peaks = {}
@@ -400,11 +422,13 @@ def run_gpu(args, rank, world):
         else None,
         "training": train,
         "autotune": tuned,
-        "config": {"workload": args.workload if multi else w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes",
+        "config": {"workload": args.workload if (multi or path) else w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes",
                    "order": w.order_max if w.order_min == w.order_max else f"P in {w.order_min}..{w.order_max}",
                    "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
                    "rays": (f"{len(cams)} views on a radius-2.5 sphere, resolutions "
-                            f"{sorted(set(zip(vw, vh)))}, 1-4 isovalues each") if multi else f"{W}x{H}",
+                            f"{sorted(set(zip(vw, vh)))}, 1-4 isovalues each") if multi else
+                           (f"{W}x{H}, path tracing: {path_kw['spp']} jittered path(s) per pixel per step, up to "
+                            f"{path_kw['max_depth']} intersections per path, Lambertian bounces") if path else f"{W}x{H}",
                    "isovalues": "per view" if multi else w.isovalues, "queries_per_step": nq,
                    "l2": "flushed (256 MiB write) before every timed step",
                    "round_kernel": ("tcgen05 TF32 hi/lo MMAs + FP32 (orders <= 8)" if args.tensor
@@ -418,7 +442,7 @@ def run_gpu(args, rank, world):
                      "ms_per_launch": kernel_s * 1e3,
                      "share_of_step": kernel_s * n_launch / total_s},
         "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4 * n_iso,
-                                         "d2h_bytes_per_step": nq * 3},
+                                         "d2h_bytes_per_step": (W * H * n_iso if path else nq) * 3},
         "gpu_launches": tm["kernel_launches"],
         "clocks": clk.summary(),
         "work": st,

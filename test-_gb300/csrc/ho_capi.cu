@@ -588,14 +588,19 @@ int ho_path_trace_device(ho_context* c, const ho_camera* cam, const float* iso, 
   ca.height = H;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
   int64_t rays = 0;
+  ho_stats totals{};
   for (int k = 0; k < n_iso; ++k) {
     const bool on = !(iso_zero_disables && iso[k] == 0.0f);
     rc = ho::path_trace(c, ca, iso[k], on, spp, max_depth, seed, rgb_dev + static_cast<size_t>(k) * npix * 3, &rays,
-                        s);
+                        &totals, s);
     if (rc < 0) return rc;
     if (rc > 0) return cuda_fail(c, rc, "path tracing");
   }
   if (rays_traced) *rays_traced = rays;
+  // ho_get_stats reports the whole call: the engine's counters summed over
+  // every bounce and isovalue
+  c->last = totals;
+  c->stats_frozen = true;
   return HO_OK;
 }
 
@@ -996,7 +1001,7 @@ int ho_mlp_load(ho_context* c, const char* path) {
 
 int ho_get_stats(ho_context* c, ho_stats* out) {
   if (!c || !out) return HO_ERR_ARG;
-  if (c->stream && c->d_stats) {
+  if (c->stream && c->d_stats && !c->stats_frozen) {
     const int rc = read_stats(c);
     if (rc && rc != HO_ERR_DEVICE) return rc;
   }

@@ -159,6 +159,7 @@ struct ho_context {
   int round_count = 16;      // rounds enqueued before the completion check (at most)
   int tail_after = 4;        // rounds before the warp-per-ray tail finishes every ray (0: no tail)
   int64_t launches = 0;      // kernels enqueued by the last trace call
+  bool stats_frozen = false; // last holds a path-tracing call's totals (not refreshed from the device)
   bool time_rounds = false;  // event pairs around each round's intersection launches
   std::vector<cudaEvent_t> round_events;
   int round_events_used = 0;  // events recorded by the last trace call
@@ -196,7 +197,7 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s);
 // Path tracing of one image at one isovalue (ho_path.cu); returns a
 // cudaError_t, or a negative HO_ status from the engine (message set).
 int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int spp, int max_depth, uint64_t seed,
-               uint8_t* rgb, int64_t* rays_traced, cudaStream_t s);
+               uint8_t* rgb, int64_t* rays_traced, ho_stats* totals, cudaStream_t s);
 // The FP64 check's residuals for caller-given hits (ho_rounds.cu).
 int launch_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out, cudaStream_t s);
 }  // namespace ho

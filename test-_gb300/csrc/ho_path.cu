@@ -157,9 +157,10 @@ __global__ void path_finish_kernel(const float* __restrict__ accum, int64_t npix
 // One image: `spp` passes of one path per pixel, each path traced for up to
 // max_depth intersections by the engine on the context (any solver mode),
 // isovalue `iso`. rgb: H x W x 3 on the device. Returns a cudaError_t or
-// an HO_ status (negative); *rays_traced += the engine's ray queries.
+// an HO_ status (negative); *rays_traced += the engine's ray queries, and
+// *totals += the engine's counters (and the layer's own launches).
 int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int spp, int max_depth, uint64_t seed,
-               uint8_t* rgb, int64_t* rays_traced, cudaStream_t s) {
+               uint8_t* rgb, int64_t* rays_traced, ho_stats* totals, cudaStream_t s) {
   const int64_t npix = static_cast<int64_t>(cam.width) * cam.height;
   const size_t n = static_cast<size_t>(npix);
   char* buf = nullptr;
@@ -184,7 +185,40 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
   if ((e = cudaMalloc(&counter, sizeof(unsigned))) != cudaSuccess) rc = int(e);
   if (rc == 0 && (e = cudaMemsetAsync(accum, 0, n * 12, s)) != cudaSuccess) rc = int(e);
   const unsigned grid = static_cast<unsigned>((npix + 255) / 256);
+  // the engine's counters summed over its calls (each call restarts them),
+  // on top of what *totals holds already
+  ho_stats tot = totals ? *totals : ho_stats{};
+  auto add = [&](const ho_stats& st) {
+    tot.rays += st.rays;
+    tot.candidates += st.candidates;
+    tot.geom_evals += st.geom_evals;
+    tot.map_evals += st.map_evals;
+    tot.field_evals += st.field_evals;
+    tot.newton_iters += st.newton_iters;
+    tot.face_iters += st.face_iters;
+    tot.faces_culled += st.faces_culled;
+    tot.node_visits += st.node_visits;
+    tot.mlp_accepted += st.mlp_accepted;
+    tot.mlp_rejected += st.mlp_rejected;
+    tot.restarts += st.restarts;
+    tot.rounds += st.rounds;
+    tot.round_pairs += st.round_pairs;
+    tot.solve_steps += st.solve_steps;
+    tot.lane_steps += st.lane_steps;
+    tot.fp64_checked += st.fp64_checked;
+    tot.fp64_failed += st.fp64_failed;
+    tot.fp64_failed_after_fallback += st.fp64_failed_after_fallback;
+    tot.round_flops += st.round_flops;
+    tot.kernel_launches += st.kernel_launches + 1;  // + the scatter kernel
+    tot.round_kernel_ns += st.round_kernel_ns;
+    tot.round_launches += st.round_launches;
+    tot.tail_rays += st.tail_rays;
+    tot.graph = st.graph;
+    tot.max_modes = st.max_modes;
+    tot.status |= st.status;
+  };
   for (int sample = 0; sample < spp && rc == 0; ++sample) {
+    ++tot.kernel_launches;  // primary rays
     path_primary_kernel<<<grid, 256, 0, s>>>(cam, npix, static_cast<uint32_t>(sample), seed, rays[0], att[0], pix[0],
                                              keys[0]);
     if ((e = cudaGetLastError()) != cudaSuccess) {
@@ -196,6 +230,13 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
     for (int bounce = 0; bounce < max_depth && live > 0; ++bounce) {
       rc = ho_intersect_device(c, live, rays[cur], iso, iso_on ? 1 : 0, hits, s);
       if (rc) break;
+      {
+        ho_stats st;
+        rc = ho_get_stats(c, &st);  // synchronises the stream
+        if (rc && rc != HO_ERR_DEVICE) break;
+        rc = 0;
+        add(st);
+      }
       if (rays_traced) *rays_traced += live;
       if ((e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s)) != cudaSuccess) {
         rc = int(e);
@@ -219,7 +260,9 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
   if (rc == 0) {
     path_finish_kernel<<<grid, 256, 0, s>>>(accum, npix, spp, rgb);
     if ((e = cudaGetLastError()) != cudaSuccess) rc = int(e);
+    ++tot.kernel_launches;
   }
+  if (rc == 0 && totals) *totals = tot;
   if (rc == 0 && (e = cudaStreamSynchronize(s)) != cudaSuccess) rc = int(e);
   cudaFree(counter);
   cudaFree(buf);

@@ -112,6 +112,7 @@ static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool l
 
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   c->last_graph = false;
+  c->stats_frozen = false;
   c->launches = 0;
   c->round_events_used = 0;
   TraceParams P;

@@ -169,6 +169,7 @@ WORKLOADS = {
     "hex32_p6": Workload("hex32_p6", 32, 6, 6, 0.08, 64, 2, 1920, 1080, [-0.3, 0.0, 0.3]),
     "hex48_mixed": Workload("hex48_mixed", 48, 2, 8, 0.1, 64, 3, 1024, 1024, [-0.2, 0.1, 0.3]),
     "hex64_p5": Workload("hex64_p5", 64, 5, 5, 0.12, 64, 4, 3840, 2160, [0.1]),
+    "hex96_mixed": Workload("hex96_mixed", 96, 3, 8, 0.1, 256, 5, 2048, 2048, [-0.4, 0.1, 0.6]),
 }
 
 
@@ -488,6 +489,8 @@ def sphere_views(n_views: int = 64, radius: float = 2.5, centre=(0.5, 0.5, 0.5),
 
 # multi-view workloads: scene workload + views
 MULTIVIEW = {"views64": ("hex48_mixed", dict(n_views=64, seed=7))}
+# Path-tracing workloads: scene, and the per-step sample pass (ho_path_trace).
+PATHS = {"path96": ("hex96_mixed", dict(spp=1, max_depth=4, seed=1))}
 
 
 def workload_context(name: str, device: int = 0, build: bool = True) -> tuple[Context, Workload]:

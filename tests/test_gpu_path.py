@@ -46,8 +46,10 @@ def test_path_trace_is_reproducible_and_seeded(small):
     ctx.set_mode(hr.MODE_BATCHED)
     a, ra = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=2, max_depth=3, seed=11)
     b, rb = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=2, max_depth=3, seed=11)
+    st = ctx.stats()  # the engine's counters summed over the call's bounces and isovalues
     c, _ = ctx.path_trace(w.camera, w.isovalues, 32, 24, spp=2, max_depth=3, seed=12)
     assert np.array_equal(a, b) and ra == rb
+    assert st["rays"] == rb and st["kernel_launches"] > 3
     assert not np.array_equal(a, c)
 
 
