@@ -264,7 +264,7 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     again by the plain solver (HO_FLAG_FALLBACK), and is
  *                     flagged HO_FLAG_FP64_FAIL if that fails too; 0: off.
  * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
- *                     default: the kernel's pair slots, 16 per warp up to 7
+ *                     default: the kernel's pair slots, 20 per warp up to 7
  *                     modes per direction, 12 at 8, 8 at 9, times 4 warps in
  *                     the tensor-core form); ho_autotune picks it.
  * HO_OPT_TENSOR      0 (default): the FP32 CUDA-core round kernel for every

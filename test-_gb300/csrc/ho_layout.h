@@ -100,7 +100,7 @@ constexpr int kMaxModes = 9;
 // Pair slots per warp of the round kernel: the per-warp shared memory (element
 // record, pair slots, task queue) is sized so that three 4-warp blocks fit on
 // an SM up to N = 8 (two at N = 9, whose record alone is 15.5 KB).
-constexpr int round_slots(int n) { return n <= 7 ? 16 : (n == 8 ? 12 : 8); }
+constexpr int round_slots(int n) { return n <= 7 ? 20 : (n == 8 ? 12 : 8); }
 // The round kernel's tensor-core form takes orders up to this (N*N <= 64
 // accumulator columns per component); one CTA of 4 warps per element batch.
 constexpr int kTcMaxModes = 8;

@@ -28,6 +28,7 @@
 // accepted seed index, faces compared in index order).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "ho_device.cuh"
@@ -49,7 +50,7 @@ constexpr int kSamples = 17;
 template <int N>
 struct RoundCfg {
   static constexpr int B = round_slots(N);  // pair slots
-  static constexpr int Ring = B * 64;         // task queue entries (>= B*54 face seeds)
+  static constexpr int Ring = B * 56;         // task queue entries (>= B*54 face seeds)
 };
 
 // A (ray, candidate) pair of one round, as the gather pass writes it.
@@ -132,7 +133,11 @@ struct PairSm {
   union {
     struct {  // isosurface samples
       float sf[kSamples];
-      float sx[kSamples][3], sg[kSamples][3];
+      float sx[kSamples][3];
+      // world gradient at each sample, in half precision: only the bracket's
+      // left sample's is used, and only as the normal of a hit whose
+      // refinement ran out of iterations
+      __half sg[kSamples][3];
     };
     struct {
       // refinement
@@ -816,7 +821,9 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
           atomicOr(&p.okm, 1u << i);
           p.sf[i] = sf;
           st3(p.sx[i], s.xi);
-          st3(p.sg[i], sg);
+          p.sg[i][0] = __float2half_rn(sg.x);
+          p.sg[i][1] = __float2half_rn(sg.y);
+          p.sg[i][2] = __float2half_rn(sg.z);
         }
       }
       __syncwarp();
@@ -850,7 +857,9 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
             if (found >= 0) {
               // the refinement state overlays the sample store: read first
               const float lf0 = p.sf[prev];
-              const float3 lx0 = ld3(p.sx[prev]), lg0 = ld3(p.sg[prev]), rx0 = ld3(p.sx[found]);
+              const float3 lx0 = ld3(p.sx[prev]), rx0 = ld3(p.sx[found]);
+              const float3 lg0 = make_float3(__half2float(p.sg[prev][0]), __half2float(p.sg[prev][1]),
+                                             __half2float(p.sg[prev][2]));
               p.rlt = p.te + (p.tx - p.te) * (float(prev) / 16.0f);
               p.rrt = p.te + (p.tx - p.te) * (float(found) / 16.0f);
               p.lsf = lf0;

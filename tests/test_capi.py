@@ -104,9 +104,9 @@ def test_engine_options():
     with hr.Context(0) as ctx:
         assert ctx.get_option(hr.OPT_GRAPH) == 1
         assert ctx.get_option(hr.OPT_ROUNDS) == 16
-        assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 16
+        assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 20
         ctx.set_option(hr.OPT_TENSOR, 1)
-        assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 64  # 4 warps x 16 slots (tensor-core form)
+        assert ctx.get_option(hr.OPT_ROUND_CHUNK) == 80  # 4 warps x 20 slots (tensor-core form)
         ctx.set_option(hr.OPT_TENSOR, 0)
         assert ctx.get_option(hr.OPT_FP64_CHECK) == 1
         assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 0
