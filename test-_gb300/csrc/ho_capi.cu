@@ -208,7 +208,6 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->rounds.fail);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
     for (cudaEvent_t ev : c->round_events) cudaEventDestroy(ev);
-    cudaFree(c->d_feat);
     cudaFree(c->d_pred);
     cudaFree(c->d_cand);
     c->mlp.release();

@@ -144,7 +144,6 @@ struct ho_context {
   // learned mode
   ho::Mlp mlp;
   float* d_desc = nullptr;        // n_elem * 48 element descriptors
-  void* d_feat = nullptr;         // network inputs, [queue item][kPredK][64] BF16
   float* d_pred = nullptr;        // network outputs, [queue item][kPredK][8]
   int32_t* d_cand = nullptr;      // elements the predictions belong to
   size_t pred_cap = 0;

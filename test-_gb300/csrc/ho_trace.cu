@@ -3,6 +3,7 @@
 // parallel.
 #include <algorithm>
 
+#include "ho_mlp_infer.cuh"
 #include "ho_trace.cuh"
 
 namespace ho {
@@ -49,38 +50,72 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
   flush_work(P.stats, w, q < n_queries);
 }
 
-// Learned mode, after classify: the first kPredK ordered candidates of each
-// queued ray (the same as the intersect pass's first candidates: nothing is
-// hit yet) and the network input of each (ray, candidate) pair.
-__global__ void __launch_bounds__(128) cand_kernel(TraceParams P, __nv_bfloat16* __restrict__ X,
-                                                   int32_t* __restrict__ cand_e) {
+// Learned mode, after classify: the network's predictions for the first
+// kPredK ordered candidates of each queued ray (the same as the rounds' first
+// candidates: nothing is hit yet). The input row of a (ray, candidate) pair
+// is formed in the kernel that runs the network, two lanes per row, from the
+// candidate list, the element's descriptor and the ray (the same values as
+// write_features); its element goes to cand_e (-1: no candidate, zero row).
+struct CandRows {
+  const TraceParams& P;
+  int32_t* cand_e;
+  __device__ __forceinline__ void fill(int64_t row, int half, __nv_bfloat16* dst) const {
+    const int64_t item = row / kPredK;
+    const int j = static_cast<int>(row % kPredK);
+    const float2 c = P.kbuf[item * kCandK + j];
+    const int ce = __float_as_int(c.y);
+    const int e = ce != INT_MAX ? ce : -1;
+    if (half == 0) cand_e[row] = e;
+    __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(dst);
+    if (e < 0) {
+      const __nv_bfloat162 z = __floats2bfloat162_rn(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < kMlpInPad / 4; ++q) d2[q] = z;
+      return;
+    }
+    const float* desc = P.desc + static_cast<int64_t>(e) * kDescFloats;
+    if (half == 0) {  // columns 0..31: descriptor values
+#pragma unroll
+      for (int q = 0; q < 16; ++q) d2[q] = __floats2bfloat162_rn(__ldg(desc + 2 * q), __ldg(desc + 2 * q + 1));
+      return;
+    }
+    // columns 32..63: descriptor 32..41, entry point, direction, zero pad
+#pragma unroll
+    for (int q = 0; q < 5; ++q) d2[q] = __floats2bfloat162_rn(__ldg(desc + 32 + 2 * q), __ldg(desc + 33 + 2 * q));
+    float3 o, d;
+    float iso;
+    bool iso_on;
+    query_ray(P, P.work[item], o, d, iso, iso_on);
+    float f[6];
+    feature_tail(desc, o, d, c.x, f);
+    d2[5] = __floats2bfloat162_rn(f[0], f[1]);
+    d2[6] = __floats2bfloat162_rn(f[2], f[3]);
+    d2[7] = __floats2bfloat162_rn(f[4], f[5]);
+    const __nv_bfloat162 z = __floats2bfloat162_rn(0.f, 0.f);
+#pragma unroll
+    for (int q = 8; q < 16; ++q) d2[q] = z;
+  }
+};
+
+__global__ void __launch_bounds__(256) pred_kernel(MlpDev M, TraceParams P, int32_t* __restrict__ cand_e,
+                                                   float* __restrict__ Y) {
   // predictions for the first pred_items queued rays (the buffers' size); the
   // rest start cold
   const unsigned n_work = min(*P.qcount, P.pred_items);
   if (blockIdx.x == 0 && threadIdx.x == 0) P.qcount[2] = n_work;
-  Work w;
-  for (int64_t item = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; item < n_work;
-       item += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int64_t q = P.work[item];
-    float3 o, d;
-    float iso;
-    bool iso_on;
-    query_ray(P, q, o, d, iso, iso_on);
-    const float2* kb = P.kbuf + item * kCandK;
-#pragma unroll
-    for (int j = 0; j < kPredK; ++j) {
-      const float2 c = kb[j];
-      const int ce = __float_as_int(c.y);
-      const int e = ce != INT_MAX ? ce : -1;
-      cand_e[item * kPredK + j] = e;
-      __nv_bfloat16* row = X + (item * kPredK + j) * kMlpInPad;
-      if (e >= 0) {
-        write_features(P.desc + static_cast<int64_t>(e) * kDescFloats, o, d, c.x, row);
-      } else {
-        for (int c = 0; c < kMlpInPad; ++c) row[c] = __float2bfloat16(0.f);
-      }
-    }
+  mlp_infer_tiles(M, CandRows{P, cand_e}, static_cast<int64_t>(n_work) * kPredK, Y);
+}
+
+static int launch_pred(ho_context* c, const TraceParams& P, cudaStream_t s, int sms) {
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(pred_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(sizeof(InferSmem)));
+    if (e != cudaSuccess) return int(e);
+    attr = true;
   }
+  pred_kernel<<<sms, 256, sizeof(InferSmem), s>>>(c->mlp.dev(), P, c->d_cand, c->d_pred);
+  return int(cudaGetLastError());
 }
 
 int prepare_rounds(ho_context* c, int64_t n_cap);
@@ -98,11 +133,8 @@ static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool l
   if (e != cudaSuccess) return int(e);
   ++c->launches;
   if (learned) {
-    c->launches += 2;
-    cand_kernel<<<sms * 8, 128, 0, s>>>(P, static_cast<__nv_bfloat16*>(c->d_feat), c->d_cand);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return int(e);
-    const int rc = mlp_infer(c->mlp.dev(), c->d_feat, 0, c->d_qctr + 2, kPredK, c->d_pred, s, sms);
+    ++c->launches;
+    const int rc = launch_pred(c, P, s, sms);
     if (rc) return rc;
   }
   // as many rounds as the previous call needed, plus one, within the option
@@ -202,15 +234,12 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   if (learned) {
     const size_t rows = static_cast<size_t>(P.pred_items) * kPredK;
     if (rows > c->pred_cap) {
-      cudaFree(c->d_feat);
       cudaFree(c->d_pred);
       cudaFree(c->d_cand);
-      c->d_feat = nullptr;
       c->d_pred = nullptr;
       c->d_cand = nullptr;
       c->pred_cap = 0;
-      cudaError_t e = cudaMalloc(&c->d_feat, rows * kMlpInPad * sizeof(__nv_bfloat16));
-      if (e == cudaSuccess) e = cudaMalloc(&c->d_pred, rows * kMlpOut * sizeof(float));
+      cudaError_t e = cudaMalloc(&c->d_pred, rows * kMlpOut * sizeof(float));
       if (e == cudaSuccess) e = cudaMalloc(&c->d_cand, rows * sizeof(int32_t));
       if (e != cudaSuccess) return int(e);
       c->pred_cap = rows;
