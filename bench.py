@@ -112,13 +112,13 @@ def flops_field(n):  # u and grad: (2n^3 + 3n^2 + 4n) FMA + basis (3 x 8n)
     return 2 * (2 * n**3 + 3 * n**2 + 4 * n) + 3 * 8 * n
 
 
-# DRAM bytes (read + write) per round-kernel launch, averaged over the 12
+# DRAM bytes (read + write) per round-kernel launch, averaged over the 4
 # launches of one step, from an ncu capture of the same workload
 # (dram__bytes_read.sum + dram__bytes_write.sum; the capture command is in
 # profiles/launches_hex32_p6.md). Keyed by workload, image size and mode;
 # absent -> null.
 ISECT_TRAFFIC = {
-    ("hex32_p6", 1920, 1080, "learned"): (432.09e6 + 26.47e6) / 12,
+    ("hex32_p6", 1920, 1080, "learned"): (424.06e6 + 26.06e6) / 4,
 }
 
 

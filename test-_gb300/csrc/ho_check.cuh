@@ -174,13 +174,17 @@ cudaError_t launch_residuals_n(const float* rec, const uint32_t* flags, int64_t 
   return cudaGetLastError();
 }
 
-// One thread per queued ray with a hit: FP64 check; failures are listed.
+// One thread per listed ray (the queued rays with a hit): FP64 check;
+// failures are listed.
 template <int N>
 __global__ void __launch_bounds__(128) check_kernel(TraceParams P, RayState* __restrict__ st,
+                                                    const uint32_t* __restrict__ list,
+                                                    const unsigned* __restrict__ n_list,
                                                     uint32_t* __restrict__ fail_list, unsigned* __restrict__ n_fail) {
-  const unsigned item = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
   bool checked = false, failed = false;
-  if (item < *P.qcount) {
+  if (k < *n_list) {
+    const unsigned item = list[k];
     RayState& r = st[item];
     if (r.best.kind != HO_HIT_MISS) {
       float3 o, d;
@@ -235,29 +239,29 @@ __global__ void __launch_bounds__(kTraceBlock) fallback_kernel(TraceParams P, Ra
 }
 
 template <int N>
-cudaError_t launch_check_n(const TraceParams& P, RayState* st, uint32_t* fail_list, unsigned* n_fail, int64_t n_cap,
-                           int sms, cudaStream_t s) {
-  check_kernel<N><<<static_cast<unsigned>((n_cap + 127) / 128), 128, 0, s>>>(P, st, fail_list, n_fail);
+cudaError_t launch_check_n(const TraceParams& P, RayState* st, const uint32_t* list, const unsigned* n_list,
+                           uint32_t* fail_list, unsigned* n_fail, int64_t n_cap, int sms, cudaStream_t s) {
+  check_kernel<N><<<static_cast<unsigned>((n_cap + 127) / 128), 128, 0, s>>>(P, st, list, n_list, fail_list, n_fail);
   fallback_kernel<N><<<sms * 2, kTraceBlock, 0, s>>>(P, st, fail_list, n_fail);
   return cudaGetLastError();
 }
 
-extern template cudaError_t launch_check_n<2>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<3>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<4>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<5>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<6>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<7>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<8>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
-extern template cudaError_t launch_check_n<9>(const TraceParams&, RayState*, uint32_t*, unsigned*, int64_t, int,
-                                              cudaStream_t);
+extern template cudaError_t launch_check_n<2>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<3>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<4>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<5>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<6>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<7>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<8>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+extern template cudaError_t launch_check_n<9>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
+                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
 
 extern template cudaError_t launch_residuals_n<2>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
                                                   double*, cudaStream_t);

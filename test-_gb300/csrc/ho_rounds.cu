@@ -103,19 +103,22 @@ __global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, Ro
   }
 }
 
-// Rays still in flight after the main rounds, listed for the tail kernel
-// (warp-aggregated appends; the count goes to the work counters too).
-__global__ void tail_list_kernel(const unsigned* __restrict__ qcount, const RayState* __restrict__ st,
-                                 uint32_t* __restrict__ list, unsigned* __restrict__ n_list, DevStats* stats) {
+// Queued rays listed by a predicate (warp-aggregated appends): hits = false,
+// the rays still in flight after the main rounds (for the tail kernel; the
+// count goes to the work counters too); hits = true, the rays with a hit
+// (for the FP64 check).
+__global__ void ray_list_kernel(const unsigned* __restrict__ qcount, const RayState* __restrict__ st, bool hits,
+                                uint32_t* __restrict__ list, unsigned* __restrict__ n_list, DevStats* stats) {
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = i < *qcount && !st[i].done;
+  bool live = false;
+  if (i < *qcount) live = hits ? st[i].best.kind != HO_HIT_MISS : !st[i].done;
   const unsigned m = __ballot_sync(kFull, live);
   if (!m) return;
   const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
   unsigned base = 0;
   if (lane == leader) {
     base = atomicAdd(n_list, static_cast<unsigned>(__popc(m)));
-    atomicAdd(&stats->c[ST_TAIL], static_cast<unsigned long long>(__popc(m)));
+    if (!hits) atomicAdd(&stats->c[ST_TAIL], static_cast<unsigned long long>(__popc(m)));
   }
   base = __shfl_sync(kFull, base, leader);
   if (live) list[base + __popc(m & ((1u << lane) - 1u))] = i;
@@ -260,21 +263,29 @@ int launch_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* 
 // FP64 check of the rays' hits, plain fallback of the failures.
 static int enqueue_check(ho_context* c, const TraceParams& P, const RoundParams& R, cudaStream_t s, int64_t n_cap) {
   if (!c->fp64_check) return 0;
+  // the rays with a hit, listed into the (now idle) pair-element buffer, so
+  // that the check's threads are all busy
+  uint32_t* list = reinterpret_cast<uint32_t*>(c->rounds.pelem);
+  unsigned* n_list = c->rounds.ctr + 6;
   RT_TRY(cudaMemsetAsync(c->rounds.ctr + 3, 0, sizeof(unsigned), s));
-  c->launches += 2;
+  RT_TRY(cudaMemsetAsync(n_list, 0, sizeof(unsigned), s));
+  ray_list_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P.qcount, R.state, true, list, n_list,
+                                                                             P.stats);
+  RT_TRY(cudaGetLastError());
+  c->launches += 3;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaError_t e;
   switch (c->N) {
-    case 2: e = launch_check_n<2>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 3: e = launch_check_n<3>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 4: e = launch_check_n<4>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 5: e = launch_check_n<5>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 6: e = launch_check_n<6>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 7: e = launch_check_n<7>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 8: e = launch_check_n<8>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 9: e = launch_check_n<9>(P, R.state, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 2: e = launch_check_n<2>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 3: e = launch_check_n<3>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 4: e = launch_check_n<4>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 5: e = launch_check_n<5>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 6: e = launch_check_n<6>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 7: e = launch_check_n<7>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 8: e = launch_check_n<8>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 9: e = launch_check_n<9>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
     default: e = cudaErrorInvalidValue; break;
   }
   RT_TRY(e);
@@ -397,8 +408,8 @@ static int enqueue_tail(ho_context* c, const TraceParams& P, const RoundParams& 
   unsigned* n_list = rb.ctr + 4;
   unsigned* next = rb.ctr + 5;
   RT_TRY(cudaMemsetAsync(rb.ctr + 4, 0, 2 * sizeof(unsigned), s));
-  tail_list_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P.qcount, R.state, rb.fail, n_list,
-                                                                              P.stats);
+  ray_list_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P.qcount, R.state, false, rb.fail,
+                                                                             n_list, P.stats);
   RT_TRY(cudaGetLastError());
   cudaError_t e;
   switch (c->N) {
