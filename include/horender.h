@@ -281,6 +281,12 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     one warp walking the rest of its candidates (the same
  *                     solves), so the last rays do not wait round by round
  *                     for each round's slowest pair.
+ * HO_OPT_GPU_FIT     the loader's modal fit of the element geometry:
+ *                     -1 (default) on the GPU when the context's device is
+ *                     present, else on the host; 0 host; 1 GPU (an error
+ *                     without a device). Both fit in FP64 in the same order.
+ * HO_OPT_LAST_FIT_GPU (read only) 1 when the last ho_load_xml_fld fitted on
+ *                     the GPU.
  * HO_OPT_TIME_ROUNDS  0 (default); 1: a pair of CUDA events brackets each
  *                     round's intersection launches (event nodes of the graph)
  *                     and ho_stats.round_kernel_ns / round_launches report
@@ -293,6 +299,8 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_TIME_ROUNDS 5
 #define HO_OPT_TENSOR 6
 #define HO_OPT_TAIL 7
+#define HO_OPT_GPU_FIT 8
+#define HO_OPT_LAST_FIT_GPU 9
 int ho_set_option(ho_context* ctx, int option, int64_t value);
 /* Path tracing with Lambertian bounces (replaces: render_kernel at spp
  * samples and depth max_depth, FEM-AABB/raytracer.cu:410-476, with

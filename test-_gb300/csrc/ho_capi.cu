@@ -287,7 +287,15 @@ int ho_load_xml_fld(ho_context* c, const char* xml, const char* fld) {
   if (!c) return HO_ERR_ARG;
   if (!xml || !fld) return fail(c, HO_ERR_ARG, "path is NULL");
   std::string err;
-  const int rc = ho::load_xml_fld(xml, fld, c->hs, err);
+  bool on_gpu = c->gpu_fit == 1;
+  if (c->gpu_fit < 0) {
+    int n_dev = 0;
+    on_gpu = cudaGetDeviceCount(&n_dev) == cudaSuccess && c->device < n_dev;
+    cudaGetLastError();
+  }
+  std::unique_ptr<ho::ModalFitter> fitter = on_gpu ? ho::make_gpu_fitter(c->device) : ho::make_host_fitter();
+  const int rc = ho::load_xml_fld(xml, fld, c->hs, err, fitter.get());
+  c->last_fit_gpu = on_gpu;
   if (rc != HO_OK) return fail(c, rc, err);
   c->built = false;
   return HO_OK;
@@ -676,6 +684,10 @@ int ho_set_option(ho_context* c, int option, int64_t value) {
       if (value < 0 || value > 256) return fail(c, HO_ERR_RANGE, "HO_OPT_TAIL must be in [0, 256]");
       c->tail_after = static_cast<int>(value);
       return HO_OK;
+    case HO_OPT_GPU_FIT:
+      if (value < -1 || value > 1) return fail(c, HO_ERR_RANGE, "HO_OPT_GPU_FIT takes -1, 0 or 1");
+      c->gpu_fit = static_cast<int>(value);
+      return HO_OK;
     default:
       return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
@@ -689,6 +701,8 @@ int ho_get_option(ho_context* c, int option, int64_t* value) {
     case HO_OPT_TIME_ROUNDS: *value = c->time_rounds ? 1 : 0; return HO_OK;
     case HO_OPT_TENSOR: *value = c->use_tc ? 1 : 0; return HO_OK;
     case HO_OPT_TAIL: *value = c->tail_after; return HO_OK;
+    case HO_OPT_GPU_FIT: *value = c->gpu_fit; return HO_OK;
+    case HO_OPT_LAST_FIT_GPU: *value = c->last_fit_gpu ? 1 : 0; return HO_OK;
     case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
     case HO_OPT_ROUND_CHUNK:
       *value = c->round_chunk > 0 ? c->round_chunk : ho::round_batch_default(c->N > 0 ? c->N : 2, c->use_tc);

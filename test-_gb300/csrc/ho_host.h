@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -72,7 +73,28 @@ struct Pcg64 {
   double uniform();  // [0,1), 53 bits
 };
 
-int load_xml_fld(const std::string& xml, const std::string& fld, HostScene& hs, std::string& err);
+// Tensor-product modal fit of elements' nodal geometry (FP64 values on GLL
+// nodes, i fastest, one block of nx*ny*nz values per component) into FP32
+// Modified-A coefficients written to (*dst)[dst_off ...]: the component
+// blocks back to back, coefficient index (k*ny + j)*nx + i. A fitter may
+// hold jobs back and write them in finish(); dst must stay alive (it may be
+// reallocated) until then.
+class ModalFitter {
+ public:
+  virtual ~ModalFitter() = default;
+  virtual bool add(const double* nodal, int comps, int nx, int ny, int nz, std::vector<float>* dst, int64_t dst_off) = 0;
+  virtual bool finish() = 0;
+  virtual const char* error() const { return "modal fit failed"; }
+};
+// The host fitter (FP64, per element, immediately).
+std::unique_ptr<ModalFitter> make_host_fitter();
+// The GPU fitter (ho_fit.cu): jobs gathered in pinned host memory, fitted in
+// batches by one CTA per element (FP64 sum factorisation), on `device`.
+std::unique_ptr<ModalFitter> make_gpu_fitter(int device);
+
+// fitter: the geometry's modal fit (nullptr: the host fitter).
+int load_xml_fld(const std::string& xml, const std::string& fld, HostScene& hs, std::string& err,
+                 ModalFitter* fitter = nullptr);
 
 }  // namespace ho
 
@@ -157,6 +179,8 @@ struct ho_context {
   int round_chunk = 0;       // pairs per element batch (0: the kernel's pair slots)
   int round_count = 16;      // rounds enqueued before the completion check (at most)
   int tail_after = 4;        // rounds before the warp-per-ray tail finishes every ray (0: no tail)
+  int gpu_fit = -1;          // loader's modal fit: -1 on the GPU when one is present, 0 host, 1 GPU
+  bool last_fit_gpu = false; // the last load fitted on the GPU
   int64_t launches = 0;      // kernels enqueued by the last trace call
   bool stats_frozen = false; // last holds a path-tracing call's totals (not refreshed from the device)
   bool time_rounds = false;  // event pairs around each round's intersection launches

@@ -626,7 +626,8 @@ std::vector<V3d> resample_face(const CurvedPts& cf, unsigned du, unsigned dv, co
 
 }  // namespace
 
-int load_xml_fld(const std::string& xml_path, const std::string& fld_path, HostScene& hs, std::string& err) {
+int load_xml_fld(const std::string& xml_path, const std::string& fld_path, HostScene& hs, std::string& err,
+                 ModalFitter* fitter) {
   std::string raw;
   if (!read_file(xml_path, raw) || raw.empty()) {
     err = "cannot read " + xml_path;
@@ -952,6 +953,13 @@ int load_xml_fld(const std::string& xml_path, const std::string& fld_path, HostS
 
   // geometry: trilinear GLL grid, curved edges, curved faces, modal fit
   HostScene out;
+  std::unique_ptr<ModalFitter> host_fit;
+  ModalFitter* fit = fitter;
+  if (!fit) {
+    host_fit = make_host_fitter();
+    fit = host_fit.get();
+  }
+  std::vector<double> soa;
   for (size_t hi = 0; hi < hexes.size(); ++hi) {
     const Hex& h = hexes[hi];
     std::array<unsigned, 3> bm = default_modes;
@@ -1063,40 +1071,19 @@ int load_xml_fld(const std::string& xml_path, const std::string& fld_path, HostS
           }
         }
     }
-    // modal fit, one direction at a time
-    std::vector<double> vr, vs, vt;
-    if (!modal_vandermonde_inverse(rn, vr) || !modal_vandermonde_inverse(sn, vs) ||
-        !modal_vandermonde_inverse(tn, vt)) {
-      err = "modal fit failed";
-      return HO_ERR_PARSE;
-    }
+    // modal fit (the fitter may run it later, in a batch)
     const size_t S = static_cast<size_t>(nx) * ny * nz;
     const int64_t goff = static_cast<int64_t>(out.geom.size());
     out.geom.resize(out.geom.size() + 3 * S);
-    std::vector<double> a(S), b(S), d(S);
-    for (int c = 0; c < 3; ++c) {
-      for (size_t q = 0; q < S; ++q) a[q] = c == 0 ? nodal[q].x : (c == 1 ? nodal[q].y : nodal[q].z);
-      for (int k = 0; k < nz; ++k)
-        for (int j = 0; j < ny; ++j)
-          for (int m = 0; m < nx; ++m) {
-            double s = 0;
-            for (int i = 0; i < nx; ++i) s += vr[m * nx + i] * a[idx(i, j, k)];
-            b[idx(m, j, k)] = s;
-          }
-      for (int k = 0; k < nz; ++k)
-        for (int m = 0; m < ny; ++m)
-          for (int i = 0; i < nx; ++i) {
-            double s = 0;
-            for (int j = 0; j < ny; ++j) s += vs[m * ny + j] * b[idx(i, j, k)];
-            d[idx(i, m, k)] = s;
-          }
-      for (int m = 0; m < nz; ++m)
-        for (int j = 0; j < ny; ++j)
-          for (int i = 0; i < nx; ++i) {
-            double s = 0;
-            for (int k = 0; k < nz; ++k) s += vt[m * nz + k] * d[idx(i, j, k)];
-            out.geom[goff + c * S + idx(i, j, m)] = static_cast<float>(s);
-          }
+    soa.resize(3 * S);
+    for (size_t q = 0; q < S; ++q) {
+      soa[q] = nodal[q].x;
+      soa[S + q] = nodal[q].y;
+      soa[2 * S + q] = nodal[q].z;
+    }
+    if (!fit->add(soa.data(), 3, nx, ny, nz, &out.geom, goff)) {
+      err = fit->error();
+      return HO_ERR_PARSE;
     }
     out.goff.push_back(goff);
     for (int q = 0; q < 3; ++q) out.gmodes.push_back(gm[q]);
@@ -1123,6 +1110,10 @@ int load_xml_fld(const std::string& xml_path, const std::string& fld_path, HostS
     }
   }
 
+  if (!fit->finish()) {
+    err = fit->error();
+    return HO_ERR_PARSE;
+  }
   // append to the caller's scene only when the whole file loaded
   for (size_t e = 0; e < out.goff.size(); ++e) {
     hs.goff.push_back(static_cast<int64_t>(hs.geom.size()) + out.goff[e]);

@@ -193,6 +193,56 @@ void tensor_modal_fit(int n, const std::vector<double>& vinv, const double* noda
       }
 }
 
+// ---- the host modal fitter ----------------------------------------------------
+namespace {
+class HostFitter final : public ModalFitter {
+ public:
+  bool add(const double* nodal, int comps, int nx, int ny, int nz, std::vector<float>* dst, int64_t dst_off) override {
+    for (int n : {nx, ny, nz}) {
+      if (n < 1 || n > kMaxModes) return false;
+      if (vinv_[n].empty() && !modal_vandermonde_inverse(gll_nodes(n), vinv_[n])) return false;
+    }
+    const std::vector<double>&vr = vinv_[nx], &vs = vinv_[ny], &vt = vinv_[nz];
+    const size_t S = static_cast<size_t>(nx) * ny * nz;
+    auto idx = [&](int i, int j, int k) { return (static_cast<size_t>(k) * ny + j) * nx + i; };
+    b_.resize(S);
+    d_.resize(S);
+    for (int c = 0; c < comps; ++c) {
+      const double* a = nodal + c * S;
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int m = 0; m < nx; ++m) {
+            double s = 0;
+            for (int i = 0; i < nx; ++i) s += vr[m * nx + i] * a[idx(i, j, k)];
+            b_[idx(m, j, k)] = s;
+          }
+      for (int k = 0; k < nz; ++k)
+        for (int m = 0; m < ny; ++m)
+          for (int i = 0; i < nx; ++i) {
+            double s = 0;
+            for (int j = 0; j < ny; ++j) s += vs[m * ny + j] * b_[idx(i, j, k)];
+            d_[idx(i, m, k)] = s;
+          }
+      for (int m = 0; m < nz; ++m)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) {
+            double s = 0;
+            for (int k = 0; k < nz; ++k) s += vt[m * nz + k] * d_[idx(i, j, k)];
+            (*dst)[dst_off + c * S + idx(i, j, m)] = static_cast<float>(s);
+          }
+    }
+    return true;
+  }
+  bool finish() override { return true; }
+
+ private:
+  std::vector<double> vinv_[kMaxModes + 1];
+  std::vector<double> b_, d_;
+};
+}  // namespace
+
+std::unique_ptr<ModalFitter> make_host_fitter() { return std::make_unique<HostFitter>(); }
+
 // ---- synthetic scenes -------------------------------------------------------
 template <class F>
 static void parallel_chunks(int64_t n, F&& fn) {
