@@ -112,6 +112,7 @@ def test_engine_options():
         assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 0
         assert ctx.get_option(hr.OPT_TENSOR) == 0
         assert ctx.get_option(hr.OPT_TAIL) == 4
+        assert ctx.get_option(hr.OPT_GPU_FIT) == -1 and ctx.get_option(hr.OPT_LAST_FIT_GPU) == 0
         ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
         assert ctx.get_option(hr.OPT_TIME_ROUNDS) == 1
         ctx.set_option(hr.OPT_GRAPH, 0)
@@ -121,7 +122,7 @@ def test_engine_options():
             0, 3, 200)
         for opt, bad in ((hr.OPT_GRAPH, 2), (hr.OPT_ROUNDS, 0), (hr.OPT_ROUNDS, 257), (hr.OPT_ROUND_CHUNK, 0),
                          (hr.OPT_ROUND_CHUNK, 4097), (hr.OPT_TIME_ROUNDS, 2), (hr.OPT_TENSOR, -1),
-                         (hr.OPT_TAIL, -1), (hr.OPT_TAIL, 257)):
+                         (hr.OPT_TAIL, -1), (hr.OPT_TAIL, 257), (hr.OPT_GPU_FIT, 2)):
             with pytest.raises(hr.HoError) as ei:
                 ctx.set_option(opt, bad)
             assert ei.value.code == -7
