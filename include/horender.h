@@ -158,6 +158,14 @@ const char* ho_last_error(const ho_context* ctx);
  * A missing or empty FLD file loads the geometry without field. */
 int ho_load_xml_fld(ho_context* ctx, const char* xml_path, const char* fld_path);
 
+/* Replaces: bool load_vtu_file(path, Scene&) (FEM-AABB/vtu_loader.h:9,
+ * vtu_loader.cpp:156-343) for hexahedra. ASCII VTK XML unstructured grid:
+ * cells of type 12, 72 or 25 become trilinear hexahedra from their first 8
+ * points; other cells are skipped; no field. Appends to the scene; on error the
+ * scene is unchanged. HO_ERR_IO: file unreadable or empty; HO_ERR_PARSE: no
+ * Points/Cells section, no ASCII points/connectivity/types, or no hexahedron. */
+int ho_load_vtu(ho_context* ctx, const char* path);
+
 /* Replaces: Scene::add_hex (FEM-AABB/raytracer.h:118-166), batched.
  * corners: n*8*3 floats (XML vertex order); geom_modes / field_modes: n*3;
  * geom_offsets[i]: float index of element i's x block in geom (y, z blocks

@@ -23,7 +23,7 @@ mkdir -p "$OUT/obj"
 FLAGS=(-std=c++17 -O2 -fPIC -ffp-contract=off -fpermissive -include cstdint -w -I"$REF" -I"$REF/fem" -I"$CUDA_INC")
 SRCS=(BVH.cu fem/HexElement.cu fem/RayIsosurface.cu fem/PrismElement.cu fem/QuadElement.cu fem/TriElement.cu
       xml_fld_loader.cpp xml_fld_common.cpp xml_fld_math.cpp xml_fld_field_parser.cpp
-      xml_fld_geometry_parser.cpp xml_fld_geometry_builder.cpp)
+      xml_fld_geometry_parser.cpp xml_fld_geometry_builder.cpp vtu_loader.cpp)
 pids=()
 objs=()
 for s in "${SRCS[@]}"; do

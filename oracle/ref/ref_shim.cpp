@@ -20,6 +20,7 @@
 #include "fem/ModalBasis.cuh"
 #include "high_order.h"
 #include "raytracer.h"
+#include "vtu_loader.h"
 #include "xml_fld_loader.h"
 
 namespace {
@@ -85,6 +86,28 @@ void* ref_scene_create(int n, const uint32_t* gm, const int64_t* goff, const flo
 void* ref_scene_load(const char* xml, const char* fld) {
   Scene sc;
   if (!load_xml_fld(xml, fld, sc)) return nullptr;
+  RefScene* s = new RefScene();
+  s->hexes = sc.hexes;
+  s->geom = sc.hex_geom_coefficients;
+  s->field = sc.hex_coefficients;
+  for (size_t i = 0; i < sc.hexes.size(); ++i) {
+    s->goff.push_back(sc.hex_geom_offsets[i]);
+    s->foff.push_back(sc.hex_coeff_offsets[i]);
+  }
+  patch_pointers(*s);
+  return s;
+}
+
+// Scene through the reference's VTU loader (FEM-AABB/vtu_loader.cpp:156);
+// counts3 gets the hexahedra, prisms and quads it added. nullptr when the
+// loader reports failure.
+void* ref_scene_load_vtu(const char* path, int64_t* counts3) {
+  Scene sc;
+  const bool ok = load_vtu_file(path, sc);
+  counts3[0] = int64_t(sc.hexes.size());
+  counts3[1] = int64_t(sc.prisms.size());
+  counts3[2] = int64_t(sc.quads.size());
+  if (!ok) return nullptr;
   RefScene* s = new RefScene();
   s->hexes = sc.hexes;
   s->geom = sc.hex_geom_coefficients;

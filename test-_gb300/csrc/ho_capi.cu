@@ -301,6 +301,16 @@ int ho_load_xml_fld(ho_context* c, const char* xml, const char* fld) {
   return HO_OK;
 }
 
+int ho_load_vtu(ho_context* c, const char* path) {
+  if (!c) return HO_ERR_ARG;
+  if (!path) return fail(c, HO_ERR_ARG, "path is NULL");
+  std::string err;
+  const int rc = ho::load_vtu(path, c->hs, err);
+  if (rc != HO_OK) return fail(c, rc, err);
+  c->built = false;
+  return HO_OK;
+}
+
 int ho_get_scene(ho_context* c, int64_t* n, float* corners, uint32_t* gm, float* geom, int64_t* geom_len,
                  int64_t* goff, uint32_t* fm, float* field, int64_t* field_len, int64_t* foff) {
   if (!c) return HO_ERR_ARG;

@@ -95,6 +95,8 @@ std::unique_ptr<ModalFitter> make_gpu_fitter(int device);
 // fitter: the geometry's modal fit (nullptr: the host fitter).
 int load_xml_fld(const std::string& xml, const std::string& fld, HostScene& hs, std::string& err,
                  ModalFitter* fitter = nullptr);
+// ASCII VTK XML unstructured-grid hexahedra (trilinear, no field), appended.
+int load_vtu(const std::string& path, HostScene& hs, std::string& err);
 
 }  // namespace ho
 

@@ -80,6 +80,7 @@ def _load():
     L.ho_last_error.argtypes = [vp]
     L.ho_last_error.restype = C.c_char_p
     L.ho_load_xml_fld.argtypes = [vp, C.c_char_p, C.c_char_p]
+    L.ho_load_vtu.argtypes = [vp, C.c_char_p]
     L.ho_add_hexes.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, i64, vp]
     L.ho_generate_synthetic.argtypes = [vp, C.POINTER(_Synth)]
     L.ho_get_scene.argtypes = [vp] + [vp] * 10
@@ -219,6 +220,9 @@ class Context:
 
     def load_xml_fld(self, xml: str, fld: str):
         self._ck(lib.ho_load_xml_fld(self.h, str(xml).encode(), str(fld).encode()))
+
+    def load_vtu(self, path: str):
+        self._ck(lib.ho_load_vtu(self.h, str(path).encode()))
 
     def get_scene(self) -> dict:
         n, gl, fl = C.c_int64(), C.c_int64(), C.c_int64()

@@ -228,6 +228,8 @@ def ref():
         L.ref_scene_create.argtypes = [i32, vp, vp, vp, i64, vp, vp, vp, i64, vp]
         L.ref_scene_load.restype = vp
         L.ref_scene_load.argtypes = [C.c_char_p, C.c_char_p]
+        L.ref_scene_load_vtu.restype = vp
+        L.ref_scene_load_vtu.argtypes = [C.c_char_p, vp]
         L.ref_scene_destroy.argtypes = [vp]
         L.ref_scene_count.argtypes = [vp]
         L.ref_scene_elem.argtypes = [vp, i32, vp, vp, vp, vp]
@@ -249,9 +251,16 @@ def ref():
 
 
 class RefScene:
-    def __init__(self, arrs: SceneArrays | None = None, xml: str | None = None, fld: str | None = None):
+    def __init__(self, arrs: SceneArrays | None = None, xml: str | None = None, fld: str | None = None,
+                 vtu: str | None = None):
         L = ref()
-        if xml is not None:
+        if vtu is not None:
+            # hexahedra, prisms and quads the reference loader added
+            self.vtu_counts = np.zeros(3, np.int64)
+            self.h = L.ref_scene_load_vtu(vtu.encode(), _p(self.vtu_counts))
+            if not self.h:
+                raise RuntimeError("reference loader failed")
+        elif xml is not None:
             self.h = L.ref_scene_load(xml.encode(), fld.encode())
             if not self.h:
                 raise RuntimeError("reference loader failed")
