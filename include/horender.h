@@ -42,6 +42,9 @@ extern "C" {
 #define HO_HIT_MISS 0
 #define HO_HIT_FACE 1
 #define HO_HIT_ISO 2
+#define HO_HIT_PRISM 3   /* a prism (elem: index among the scene's prisms)    */
+#define HO_HIT_QUAD 4    /* a quad (elem: index among the quads)             */
+#define HO_HIT_TRI 5     /* a curved triangle (elem: index among the triangles) */
 
 /* ho_hit.flags bits. */
 #define HO_FLAG_FALLBACK 1u      /* learned guess rejected, plain solver answered   */
@@ -100,6 +103,7 @@ typedef struct {
   int32_t bvh_depth;
   int64_t device_bytes;     /* scene + BVH bytes resident on the device         */
   float bounds[6];          /* scene box (lo xyz, hi xyz) over element boxes    */
+  int64_t n_prisms, n_quads, n_tris;  /* other primitives (ho_add_prisms ...) */
 } ho_scene_info;
 
 /* Work counters of the last render/intersect call. */
@@ -159,12 +163,49 @@ const char* ho_last_error(const ho_context* ctx);
 int ho_load_xml_fld(ho_context* ctx, const char* xml_path, const char* fld_path);
 
 /* Replaces: bool load_vtu_file(path, Scene&) (FEM-AABB/vtu_loader.h:9,
- * vtu_loader.cpp:156-343) for hexahedra. ASCII VTK XML unstructured grid:
- * cells of type 12, 72 or 25 become trilinear hexahedra from their first 8
- * points; other cells are skipped; no field. Appends to the scene; on error the
- * scene is unchanged. HO_ERR_IO: file unreadable or empty; HO_ERR_PARSE: no
- * Points/Cells section, no ASCII points/connectivity/types, or no hexahedron. */
+ * vtu_loader.cpp:156-343). ASCII VTK XML unstructured grid: cells of type
+ * 12, 72 or 25 become trilinear hexahedra from their first 8 points, wedges
+ * (13, 73, 26) linear prisms from their first 6 and quads (9, 70, 22) linear
+ * quads from their first 4, in the file's point order; other cells are
+ * skipped; no field. Appends to the scene; on error the scene is unchanged.
+ * HO_ERR_IO: file unreadable or empty; HO_ERR_PARSE: no Points/Cells
+ * section, no ASCII points/connectivity/types, or no cell of those types. */
 int ho_load_vtu(ho_context* ctx, const char* path);
+
+/* Replaces: Scene::add_prism / add_quad / add_curved_tri (FEM-AABB/raytracer.h:
+ * 167-300), batched. verts: n*6*3 (prism: quad base 0-3 at t = -1 in the
+ * order (-,-), (+,-), (+,+), (-,+) of (r, s), top edge 4-5), n*4*3 (quad:
+ * vertex v at r = +-1 by bit 0, s = +-1 by bit 1), n*3*3 (triangle).
+ * geom_modes / field_modes: n*3 for prisms (Modified-A in r and s,
+ * Modified-B in t), n*2 for quads (A x A) and triangles (A x Modified-B);
+ * each in [1, 9]. geom_offsets[i]: float index of primitive i's x block in
+ * geom (y, z follow), -1 = linear from the vertices; field_offsets[i]: -1 =
+ * no field. Block sizes: quad mx*my; triangle sum_{i<mx} max(my-i, 0);
+ * prism my * sum_{i<mx} max(mz-i, 0). Appends; on error nothing is added.
+ * The reference traces these with its prism / quad / triangle routines
+ * (FEM-AABB/fem/PrismElement.cu, QuadElement.cu, TriElement.cu), prisms
+ * without isosurface; so does horender, in a pass after the hexahedra
+ * (hits of kind HO_HIT_PRISM / QUAD / TRI). */
+int ho_add_prisms(ho_context* ctx, int64_t n, const float* verts, const uint32_t* geom_modes, const float* geom,
+                  int64_t geom_len, const int64_t* geom_offsets, const uint32_t* field_modes, const float* field,
+                  int64_t field_len, const int64_t* field_offsets);
+int ho_add_quads(ho_context* ctx, int64_t n, const float* verts, const uint32_t* geom_modes, const float* geom,
+                 int64_t geom_len, const int64_t* geom_offsets, const uint32_t* field_modes, const float* field,
+                 int64_t field_len, const int64_t* field_offsets);
+int ho_add_tris(ho_context* ctx, int64_t n, const float* verts, const uint32_t* geom_modes, const float* geom,
+                int64_t geom_len, const int64_t* geom_offsets, const uint32_t* field_modes, const float* field,
+                int64_t field_len, const int64_t* field_offsets);
+
+/* The scene's prisms, quads and triangles as one list, prisms first, then
+ * quads, then triangles (each kind in the order added; a hit's elem indexes
+ * within its kind): kind (0 prism, 1 quad, 2 triangle), vertices n*18
+ * (unused rows zero), modes n*3, offsets into the returned geom / field
+ * pools. Any output may be NULL; call with NULL arrays first for the sizes. */
+int ho_get_prims(ho_context* ctx, int64_t* n, int32_t* kind, float* verts, uint32_t* geom_modes, float* geom,
+                 int64_t* geom_len, int64_t* geom_offsets, uint32_t* field_modes, float* field, int64_t* field_len,
+                 int64_t* field_offsets);
+/* The primitives' sampled boxes after ho_build_bvh, n*6, in ho_get_prims order. */
+int ho_get_prim_boxes(ho_context* ctx, float* out);
 
 /* Replaces: Scene::add_hex (FEM-AABB/raytracer.h:118-166), batched.
  * corners: n*8*3 floats (XML vertex order); geom_modes / field_modes: n*3;

@@ -18,6 +18,9 @@
 #include <vector>
 
 #include "fem/ModalBasis.cuh"
+#include "fem/PrismElement.cuh"
+#include "fem/QuadElement.cuh"
+#include "fem/TriElement.cuh"
 #include "high_order.h"
 #include "raytracer.h"
 #include "vtu_loader.h"
@@ -118,6 +121,90 @@ void* ref_scene_load_vtu(const char* path, int64_t* counts3) {
   }
   patch_pointers(*s);
   return s;
+}
+
+// One prism (kind 0), quad (1) or curved triangle (2) built the way
+// Scene::add_prism / add_quad / add_curved_tri keep it (FEM-AABB/raytracer.h:
+// 167-300): vertices, and modal geometry when gx is given. box6 gets the
+// reference's sampled box (ComputePrismAabb / ComputeQuadAabb at 4, and
+// ComputeTriAabb at 6 per edge, as raytracer.cu:258-328 calls them); out5 per
+// ray the reference's IntersectRayWith* on [seg0, seg1]: (hit, t, r, s, t-coordinate).
+int ref_prim_intersect(int kind, const float* verts, const uint32_t* gm3, const float* gx, const float* gy,
+                       const float* gz, const float* rays, int64_t n, const double* seg, float* box6,
+                       double* out5) {
+  float3 lo, hi;
+  auto ray_of = [&](int64_t i) {
+    zidingyi::Ray r;
+    r.origin = make_float3(rays[6 * i], rays[6 * i + 1], rays[6 * i + 2]);
+    r.direction = make_float3(rays[6 * i + 3], rays[6 * i + 4], rays[6 * i + 5]);
+    return r;
+  };
+  if (kind == 0) {
+    zidingyi::PrismElementData e{};
+    for (int v = 0; v < 6; ++v) e.vertices[v] = make_float3(verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]);
+    if (gx) {
+      e.geomCoefficients[0] = gx; e.geomCoefficients[1] = gy; e.geomCoefficients[2] = gz;
+      e.geomModes = make_uint3(gm3[0], gm3[1], gm3[2]);
+    }
+    zidingyi::ComputePrismAabb(e, lo, hi, 4);
+    for (int64_t i = 0; i < n; ++i) {
+      float t; float3 x;
+      const bool ok = zidingyi::IntersectRayWithPrism(e, ray_of(i), float(seg[2 * i]), float(seg[2 * i + 1]), t, x);
+      double* o = out5 + 5 * i;
+      o[0] = ok; o[1] = ok ? t : 0; o[2] = ok ? x.x : 0; o[3] = ok ? x.y : 0; o[4] = ok ? x.z : 0;
+    }
+  } else if (kind == 1) {
+    zidingyi::QuadElementData e{};
+    for (int v = 0; v < 4; ++v) e.vertices[v] = make_float3(verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]);
+    if (gx) {
+      e.geomCoefficients[0] = gx; e.geomCoefficients[1] = gy; e.geomCoefficients[2] = gz;
+      e.geomModes = make_uint2(gm3[0], gm3[1]);
+    }
+    zidingyi::ComputeQuadAabb(e, lo, hi, 4);
+    for (int64_t i = 0; i < n; ++i) {
+      float t; float2 x;
+      const bool ok = zidingyi::IntersectRayWithQuad(e, ray_of(i), float(seg[2 * i]), float(seg[2 * i + 1]), t, x);
+      double* o = out5 + 5 * i;
+      o[0] = ok; o[1] = ok ? t : 0; o[2] = ok ? x.x : 0; o[3] = ok ? x.y : 0; o[4] = 0;
+    }
+  } else {
+    zidingyi::TriElementData e{};
+    for (int v = 0; v < 3; ++v) e.vertices[v] = make_float3(verts[3 * v], verts[3 * v + 1], verts[3 * v + 2]);
+    if (gx) {
+      e.geomCoefficients[0] = gx; e.geomCoefficients[1] = gy; e.geomCoefficients[2] = gz;
+      e.geomModes = make_uint2(gm3[0], gm3[1]);
+    }
+    zidingyi::ComputeTriAabb(e, lo, hi, 6);
+    for (int64_t i = 0; i < n; ++i) {
+      float t; float2 x;
+      const bool ok = zidingyi::IntersectRayWithTriangle(e, ray_of(i), float(seg[2 * i]), float(seg[2 * i + 1]), t, x);
+      double* o = out5 + 5 * i;
+      o[0] = ok; o[1] = ok ? t : 0; o[2] = ok ? x.x : 0; o[3] = ok ? x.y : 0; o[4] = 0;
+    }
+  }
+  box6[0] = lo.x; box6[1] = lo.y; box6[2] = lo.z;
+  box6[3] = hi.x; box6[4] = hi.y; box6[5] = hi.z;
+  return 0;
+}
+
+// The prisms' (n x 6 x 3) and quads' (n x 4 x 3) vertices the reference's
+// VTU loader adds; the arrays hold as many as ref_scene_load_vtu counted.
+int ref_vtu_prim_verts(const char* path, float* prism_verts, float* quad_verts) {
+  Scene sc;
+  load_vtu_file(path, sc);
+  for (size_t i = 0; i < sc.prisms.size(); ++i)
+    for (int v = 0; v < 6; ++v) {
+      prism_verts[(6 * i + v) * 3] = sc.prisms[i].vertices[v].x;
+      prism_verts[(6 * i + v) * 3 + 1] = sc.prisms[i].vertices[v].y;
+      prism_verts[(6 * i + v) * 3 + 2] = sc.prisms[i].vertices[v].z;
+    }
+  for (size_t i = 0; i < sc.quads.size(); ++i)
+    for (int v = 0; v < 4; ++v) {
+      quad_verts[(4 * i + v) * 3] = sc.quads[i].vertices[v].x;
+      quad_verts[(4 * i + v) * 3 + 1] = sc.quads[i].vertices[v].y;
+      quad_verts[(4 * i + v) * 3 + 2] = sc.quads[i].vertices[v].z;
+    }
+  return 0;
 }
 
 void ref_scene_destroy(void* p) { delete static_cast<RefScene*>(p); }

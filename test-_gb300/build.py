@@ -24,6 +24,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", str(ROOT / "include"),
           "-I", str(CSRC)]
 CU_FLAGS = ARCH + COMMON + ["--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+# per-file extras: the primitive pass rounds every operation on its own, as
+# the reference's FP32 host code does (its start searches branch on exact values)
+FILE_FLAGS = {"ho_prim.cu": ["--fmad=false"]}
 
 
 def sources() -> list[Path]:
@@ -52,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if not force and not _stale(obj, [src] + hdrs):
             continue
         if src.suffix == ".cu":
-            cmd = [NVCC] + CU_FLAGS + ["-c", str(src), "-o", str(obj)]
+            cmd = [NVCC] + CU_FLAGS + FILE_FLAGS.get(src.name, []) + ["-c", str(src), "-o", str(obj)]
         else:
             cmd = [NVCC] + ARCH + COMMON + ["-x", "c++", "-c", str(src), "-o", str(obj)]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))

@@ -381,7 +381,7 @@ __global__ void karras_kernel(const uint32_t* __restrict__ k, const int32_t* __r
   if (lo == g) {
     const int32_t e = vals[g];
     nd.c[0].idx = ~e;
-    nd.c[0].aux = eflags[e] & kAuxHasField;
+    nd.c[0].aux = eflags ? (eflags[e] & kAuxHasField) : 0u;
     parent_leaf[g] = static_cast<int32_t>(i);
   } else {
     nd.c[0].idx = static_cast<int32_t>(g);
@@ -390,7 +390,7 @@ __global__ void karras_kernel(const uint32_t* __restrict__ k, const int32_t* __r
   if (hi == g + 1) {
     const int32_t e = vals[g + 1];
     nd.c[1].idx = ~e;
-    nd.c[1].aux = eflags[e] & kAuxHasField;
+    nd.c[1].aux = eflags ? (eflags[e] & kAuxHasField) : 0u;
     parent_leaf[g + 1] = static_cast<int32_t>(i);
   } else {
     nd.c[1].idx = static_cast<int32_t>(g + 1);
@@ -432,32 +432,37 @@ __global__ void refit_kernel(const float* __restrict__ box, const int32_t* __res
 }
 
 int build_lbvh(ho_context* c) {
-  const int64_t n = c->n_elem;
-  cudaStream_t s = c->stream;
+  return build_tree(c->d_box, c->d_flags, c->n_elem, c->stream, &c->d_nodes, &c->n_nodes, &c->bvh_depth, c->bounds);
+}
+
+int build_tree(const float* d_box, const uint32_t* d_flags, int64_t n, cudaStream_t s, BNode** nodes_out,
+               int64_t* n_nodes_out, int* depth_out, float bounds[6]) {
   // scene bounds over box centres (host; the boxes are small)
   std::vector<float> hb(static_cast<size_t>(n) * 6);
-  HO_TRY(cudaMemcpyAsync(hb.data(), c->d_box, hb.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+  HO_TRY(cudaMemcpyAsync(hb.data(), d_box, hb.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
   HO_TRY(cudaStreamSynchronize(s));
   float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
   for (int a = 0; a < 3; ++a) {
-    c->bounds[a] = FLT_MAX;
-    c->bounds[3 + a] = -FLT_MAX;
+    bounds[a] = FLT_MAX;
+    bounds[3 + a] = -FLT_MAX;
   }
   for (int64_t i = 0; i < n; ++i)
     for (int a = 0; a < 3; ++a) {
       const float cc = 0.5f * (hb[6 * i + a] + hb[6 * i + 3 + a]);
       clo[a] = std::min(clo[a], cc);
       chi[a] = std::max(chi[a], cc);
-      c->bounds[a] = std::min(c->bounds[a], hb[6 * i + a]);
-      c->bounds[3 + a] = std::max(c->bounds[3 + a], hb[6 * i + 3 + a]);
+      bounds[a] = std::min(bounds[a], hb[6 * i + a]);
+      bounds[3 + a] = std::max(bounds[3 + a], hb[6 * i + 3 + a]);
     }
   const float3 lo = make_float3(clo[0], clo[1], clo[2]);
   const float3 inv = make_float3(chi[0] > clo[0] ? 1.f / (chi[0] - clo[0]) : 0.f,
                                  chi[1] > clo[1] ? 1.f / (chi[1] - clo[1]) : 0.f,
                                  chi[2] > clo[2] ? 1.f / (chi[2] - clo[2]) : 0.f);
 
-  c->n_nodes = std::max<int64_t>(1, n - 1);
-  HO_TRY(cudaMalloc(&c->d_nodes, c->n_nodes * sizeof(BNode)));
+  const int64_t n_nodes = std::max<int64_t>(1, n - 1);
+  *n_nodes_out = n_nodes;
+  HO_TRY(cudaMalloc(nodes_out, n_nodes * sizeof(BNode)));
+  BNode* const d_nodes = *nodes_out;
   if (n == 1) {
     BNode nd;
     std::memset(&nd, 0, sizeof(nd));
@@ -468,12 +473,12 @@ int build_lbvh(ho_context* c) {
       nd.c[1].hi[a] = -FLT_MAX;
     }
     uint32_t fl = 0;
-    HO_TRY(cudaMemcpy(&fl, c->d_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (d_flags) HO_TRY(cudaMemcpy(&fl, d_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     nd.c[0].idx = ~0;
     nd.c[0].aux = fl & kAuxHasField;
     nd.c[1].idx = kEmptyChild;
-    HO_TRY(cudaMemcpy(c->d_nodes, &nd, sizeof(nd), cudaMemcpyHostToDevice));
-    c->bvh_depth = 1;
+    HO_TRY(cudaMemcpy(d_nodes, &nd, sizeof(nd), cudaMemcpyHostToDevice));
+    *depth_out = 1;
     return 0;
   }
 
@@ -489,7 +494,7 @@ int build_lbvh(ho_context* c) {
   HO_TRY(cudaMalloc(&pleaf, n * sizeof(int32_t)));
   HO_TRY(cudaMalloc(&arrive, n * sizeof(uint32_t)));
   const unsigned gb = static_cast<unsigned>((n + 255) / 256);
-  morton_kernel<<<gb, 256, 0, s>>>(c->d_box, n, lo, inv, k0, v0);
+  morton_kernel<<<gb, 256, 0, s>>>(d_box, n, lo, inv, k0, v0);
   HO_TRY(cudaGetLastError());
   for (int pass = 0; pass < 4; ++pass) {
     const int shift = 8 * pass;
@@ -502,14 +507,14 @@ int build_lbvh(ho_context* c) {
   }
   HO_TRY(cudaMemsetAsync(pint, 0xff, n * sizeof(int32_t), s));
   HO_TRY(cudaMemsetAsync(arrive, 0, n * sizeof(uint32_t), s));
-  karras_kernel<<<gb, 256, 0, s>>>(k0, v0, c->d_flags, n, c->d_nodes, pint, pleaf);
+  karras_kernel<<<gb, 256, 0, s>>>(k0, v0, d_flags, n, d_nodes, pint, pleaf);
   HO_TRY(cudaGetLastError());
-  refit_kernel<<<gb, 256, 0, s>>>(c->d_box, v0, n, c->d_nodes, pint, pleaf, arrive);
+  refit_kernel<<<gb, 256, 0, s>>>(d_box, v0, n, d_nodes, pint, pleaf, arrive);
   HO_TRY(cudaGetLastError());
 
   // depth (host walk; also checks every node is reachable exactly once)
-  std::vector<BNode> hn(c->n_nodes);
-  HO_TRY(cudaMemcpyAsync(hn.data(), c->d_nodes, hn.size() * sizeof(BNode), cudaMemcpyDeviceToHost, s));
+  std::vector<BNode> hn(n_nodes);
+  HO_TRY(cudaMemcpyAsync(hn.data(), d_nodes, hn.size() * sizeof(BNode), cudaMemcpyDeviceToHost, s));
   HO_TRY(cudaStreamSynchronize(s));
   int depth = 0;
   int64_t leaves = 0;
@@ -517,10 +522,10 @@ int build_lbvh(ho_context* c) {
   st.push_back({0, 1});
   int64_t visits = 0;
   while (!st.empty()) {
-    if (++visits > c->n_nodes) break;  // a well-formed tree has exactly n_nodes internal nodes
+    if (++visits > n_nodes) break;  // a well-formed tree has exactly n_nodes internal nodes
     auto [id, dd] = st.back();
     st.pop_back();
-    if (id < 0 || id >= c->n_nodes) break;
+    if (id < 0 || id >= n_nodes) break;
     depth = std::max(depth, dd);
     for (int ch = 0; ch < 2; ++ch) {
       const int32_t x = hn[id].c[ch].idx;
@@ -529,7 +534,7 @@ int build_lbvh(ho_context* c) {
       else st.push_back({x, dd + 1});
     }
   }
-  c->bvh_depth = depth;
+  *depth_out = depth;
   cudaFree(k0);
   cudaFree(k1);
   cudaFree(v0);

@@ -64,6 +64,8 @@ void free_scene(ho_context* c) {
   c->d_flags = nullptr;
   c->d_own = nullptr;
   c->d_nodes = nullptr;
+  c->n_elem = 0;
+  ho::prims_free(c);
   c->built = false;
   c->device_bytes = 0;
 }
@@ -190,6 +192,7 @@ void ho_destroy(ho_context* c) {
     free_scene(c);
     cudaFree(c->d_stats);
     cudaFree(c->d_hits);
+    cudaFree(c->d_phits);
     cudaFree(c->d_rgb);
     cudaFree(c->d_rays);
     cudaFree(c->d_views);
@@ -273,6 +276,130 @@ int ho_add_hexes(ho_context* c, int64_t n, const float* corners, const uint32_t*
   return HO_OK;
 }
 
+namespace {
+
+// Coefficients in one component block of a primitive kind (m: its modes).
+int64_t prim_block_len(int kind, const uint32_t m[3]) {
+  if (kind == 1) return static_cast<int64_t>(m[0]) * m[1];
+  const int64_t top = kind == 0 ? m[2] : m[1];
+  int64_t n = 0;
+  for (int64_t i = 0; i < m[0]; ++i) n += std::max<int64_t>(top - i, 0);
+  return kind == 0 ? n * m[1] : n;
+}
+
+// ho_add_prisms / quads / tris: dims modes per primitive (3 or 2), nv vertices.
+int add_prims(ho_context* c, int kind, int nv, int dims, int64_t n, const float* verts, const uint32_t* gm,
+              const float* geom, int64_t geom_len, const int64_t* goff, const uint32_t* fm, const float* field,
+              int64_t field_len, const int64_t* foff) {
+  if (!c) return HO_ERR_ARG;
+  if (n < 0) return fail(c, HO_ERR_ARG, "n must be >= 0");
+  if (n > 0 && (!verts || !gm || !goff || !fm || !foff)) return fail(c, HO_ERR_ARG, "null array");
+  ho::HostPrims& hp = c->hs.prims;
+  if (hp.size() + n > (int64_t(1) << 30)) return fail(c, HO_ERR_RANGE, "at most 2^30 primitives");
+  auto modes = [&](const uint32_t* src, int64_t i, uint32_t out[3]) {
+    out[0] = src[dims * i];
+    out[1] = src[dims * i + 1];
+    out[2] = dims == 3 ? src[dims * i + 2] : 0u;
+  };
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t m[3];
+    if (goff[i] >= 0) {
+      modes(gm, i, m);
+      for (int a = 0; a < dims; ++a)
+        if (m[a] < 1 || m[a] > ho::kMaxModes)
+          return fail(c, HO_ERR_RANGE, "primitive " + std::to_string(i) + ": geometry modes must be in [1, 9]");
+      if (!geom || goff[i] + 3 * prim_block_len(kind, m) > geom_len)
+        return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": geometry coefficients out of range");
+    }
+    if (foff[i] >= 0) {
+      modes(fm, i, m);
+      for (int a = 0; a < dims; ++a)
+        if (m[a] < 1 || m[a] > ho::kMaxModes)
+          return fail(c, HO_ERR_RANGE, "primitive " + std::to_string(i) + ": field modes must be in [1, 9]");
+      if (!field || foff[i] + prim_block_len(kind, m) > field_len)
+        return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": field coefficients out of range");
+    }
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    hp.kind.push_back(kind);
+    const size_t at = hp.verts.size();
+    hp.verts.resize(at + 18, 0.0f);
+    std::copy(verts + 3 * nv * i, verts + 3 * nv * (i + 1), hp.verts.begin() + at);
+    uint32_t m[3];
+    if (goff[i] >= 0) {
+      modes(gm, i, m);
+      const int64_t cnt = 3 * prim_block_len(kind, m);
+      hp.goff.push_back(static_cast<int64_t>(hp.geom.size()));
+      hp.geom.insert(hp.geom.end(), geom + goff[i], geom + goff[i] + cnt);
+    } else {
+      m[0] = m[1] = m[2] = 0;
+      hp.goff.push_back(-1);
+    }
+    hp.gmodes.insert(hp.gmodes.end(), m, m + 3);
+    modes(fm, i, m);
+    if (foff[i] >= 0) {
+      const int64_t cnt = prim_block_len(kind, m);
+      hp.foff.push_back(static_cast<int64_t>(hp.field.size()));
+      hp.field.insert(hp.field.end(), field + foff[i], field + foff[i] + cnt);
+    } else {
+      hp.foff.push_back(-1);
+    }
+    hp.fmodes.insert(hp.fmodes.end(), m, m + 3);
+  }
+  c->built = false;
+  return HO_OK;
+}
+
+}  // namespace
+
+int ho_add_prisms(ho_context* c, int64_t n, const float* verts, const uint32_t* gm, const float* geom, int64_t geom_len,
+                  const int64_t* goff, const uint32_t* fm, const float* field, int64_t field_len, const int64_t* foff) {
+  return add_prims(c, 0, 6, 3, n, verts, gm, geom, geom_len, goff, fm, field, field_len, foff);
+}
+
+int ho_add_quads(ho_context* c, int64_t n, const float* verts, const uint32_t* gm, const float* geom, int64_t geom_len,
+                 const int64_t* goff, const uint32_t* fm, const float* field, int64_t field_len, const int64_t* foff) {
+  return add_prims(c, 1, 4, 2, n, verts, gm, geom, geom_len, goff, fm, field, field_len, foff);
+}
+
+int ho_add_tris(ho_context* c, int64_t n, const float* verts, const uint32_t* gm, const float* geom, int64_t geom_len,
+                const int64_t* goff, const uint32_t* fm, const float* field, int64_t field_len, const int64_t* foff) {
+  return add_prims(c, 2, 3, 2, n, verts, gm, geom, geom_len, goff, fm, field, field_len, foff);
+}
+
+int ho_get_prims(ho_context* c, int64_t* n, int32_t* kind, float* verts, uint32_t* gm, float* geom, int64_t* geom_len,
+                 int64_t* goff, uint32_t* fm, float* field, int64_t* field_len, int64_t* foff) {
+  if (!c) return HO_ERR_ARG;
+  const ho::HostPrims& hp = c->hs.prims;
+  if (n) *n = hp.size();
+  if (geom_len) *geom_len = static_cast<int64_t>(hp.geom.size());
+  if (field_len) *field_len = static_cast<int64_t>(hp.field.size());
+  if (geom) std::memcpy(geom, hp.geom.data(), hp.geom.size() * sizeof(float));
+  if (field) std::memcpy(field, hp.field.data(), hp.field.size() * sizeof(float));
+  int64_t j = 0;
+  for (int k = 0; k < 3; ++k)
+    for (int64_t i = 0; i < hp.size(); ++i) {
+      if (hp.kind[i] != k) continue;
+      if (kind) kind[j] = k;
+      if (verts) std::memcpy(verts + 18 * j, hp.verts.data() + 18 * i, 18 * sizeof(float));
+      if (gm) std::memcpy(gm + 3 * j, hp.gmodes.data() + 3 * i, 3 * sizeof(uint32_t));
+      if (fm) std::memcpy(fm + 3 * j, hp.fmodes.data() + 3 * i, 3 * sizeof(uint32_t));
+      if (goff) goff[j] = hp.goff[i];
+      if (foff) foff[j] = hp.foff[i];
+      ++j;
+    }
+  return HO_OK;
+}
+
+int ho_get_prim_boxes(ho_context* c, float* out) {
+  if (!c || !out) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (c->n_prims == 0) return HO_OK;
+  CK(cudaMemcpyAsync(out, c->d_pbox, c->n_prims * 6 * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "read boxes");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return HO_OK;
+}
+
 int ho_generate_synthetic(ho_context* c, const ho_synth_params* p) {
   if (!c) return HO_ERR_ARG;
   if (!p) return fail(c, HO_ERR_ARG, "params is NULL");
@@ -331,12 +458,22 @@ int ho_get_scene(ho_context* c, int64_t* n, float* corners, uint32_t* gm, float*
 int ho_build_bvh(ho_context* c) {
   if (!c) return HO_ERR_ARG;
   const HostScene& hs = c->hs;
-  if (hs.size() == 0) return fail(c, HO_ERR_STATE, "scene is empty");
+  if (hs.size() == 0 && hs.prims.size() == 0) return fail(c, HO_ERR_STATE, "scene is empty");
   if (hs.size() > (int64_t(1) << 30)) return fail(c, HO_ERR_RANGE, "at most 2^30 elements");
   int rc = ensure_device(c);
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream), "sync");
   free_scene(c);
+  rc = ho::prims_build(c);
+  if (rc) return cuda_fail(c, rc, "primitive setup");
+  if (c->pbvh_depth + 2 > 64) return fail(c, HO_ERR_RANGE, "primitive BVH deeper than the traversal stack");
+  if (hs.size() == 0) {  // primitives only
+    c->N = 0;
+    c->n_elem = 0;
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    c->built = true;
+    return HO_OK;
+  }
   const int N = ho::scene_max_modes(hs);
   if (N > ho::kMaxModes) return fail(c, HO_ERR_RANGE, "modes per direction must be <= 9");
   c->N = N;
@@ -401,6 +538,11 @@ int ho_scene_info_get(ho_context* c, ho_scene_info* out) {
   out->bvh_depth = c->built ? c->bvh_depth : 0;
   out->device_bytes = c->built ? c->device_bytes : 0;
   for (int i = 0; i < 6; ++i) out->bounds[i] = c->bounds[i];
+  int64_t cnt[3] = {0, 0, 0};
+  for (int32_t k : c->hs.prims.kind) ++cnt[k];
+  out->n_prisms = cnt[0];
+  out->n_quads = cnt[1];
+  out->n_tris = cnt[2];
   return HO_OK;
 }
 
@@ -645,8 +787,12 @@ int ho_hit_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* 
   if (n == 0) return HO_OK;
   if (!rays || !hits || !out) return fail(c, HO_ERR_ARG, "null buffer");
   for (int64_t i = 0; i < n; ++i)
-    if (hits[i].kind != HO_HIT_MISS && (hits[i].elem < 0 || hits[i].elem >= c->n_elem))
+    if ((hits[i].kind == HO_HIT_FACE || hits[i].kind == HO_HIT_ISO) && (hits[i].elem < 0 || hits[i].elem >= c->n_elem))
       return fail(c, HO_ERR_RANGE, "hit " + std::to_string(i) + " names no element of the scene");
+  if (c->n_elem == 0) {  // no hexahedron hits: every residual is 0
+    std::memset(out, 0, static_cast<size_t>(n) * 2 * sizeof(double));
+    return HO_OK;
+  }
   int rc;
   if ((rc = ensure_buf(c, c->d_rays, c->rays_cap, static_cast<size_t>(n) * 6, "cudaMalloc(rays)"))) return rc;
   if ((rc = ensure_buf(c, c->d_hits, c->hits_cap, static_cast<size_t>(n), "cudaMalloc(hits)"))) return rc;
@@ -933,6 +1079,7 @@ int ho_mlp_grad(ho_context* c, const float* X, const float* T, const uint8_t* va
 int ho_learn_samples(ho_context* c, int64_t n, uint64_t seed, float* X, float* T, uint8_t* valid) {
   if (!c || n <= 0 || !X || !T || !valid) return HO_ERR_ARG;
   if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (c->n_elem == 0) return fail(c, HO_ERR_STATE, "the network learns hexahedra; the scene has none");
   void* dx = nullptr;
   float* dt = nullptr;
   uint8_t* dv = nullptr;
@@ -961,6 +1108,7 @@ int ho_learn_samples(ho_context* c, int64_t n, uint64_t seed, float* X, float* T
 int ho_train_mlp(ho_context* c, int64_t n_samples, int steps, int batch, float lr, uint64_t seed, float* losses) {
   if (!c || n_samples <= 0 || steps <= 0 || batch <= 0 || batch > 65536) return HO_ERR_ARG;
   if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (c->n_elem == 0) return fail(c, HO_ERR_STATE, "the network learns hexahedra; the scene has none");
   if (!c->mlp.ready) {
     const int rc = ho_mlp_init(c, seed);
     if (rc) return rc;

@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(128) residual_kernel(const float* __restrict__
   if (i >= n) return;
   const ho_hit h = hits[i];
   double r = 0.0, u = 0.0;
-  if (h.kind != HO_HIT_MISS && h.elem >= 0) {
+  if ((h.kind == HO_HIT_FACE || h.kind == HO_HIT_ISO) && h.elem >= 0) {
     const float* ray = rays + 6 * i;
     fp64_residuals<N>(rec, h.elem, make_float3(ray[0], ray[1], ray[2]), make_float3(ray[3], ray[4], ray[5]), h.t,
                       make_float3(h.xi[0], h.xi[1], h.xi[2]), (flags[h.elem] & 1u) != 0, r, u);

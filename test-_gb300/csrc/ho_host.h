@@ -18,7 +18,23 @@ namespace ho {
 // Scene as supplied (ho_add_hexes / loader / generator): same layout as the
 // reference's Scene hex buffers (FEM-AABB/raytracer.h:65-96), one entry per
 // element, coefficients FP32.
+// Prisms, quads and curved triangles, in the order they were added; the
+// device keeps them kind by kind (prisms, quads, triangles), each kind in
+// this order.
+struct HostPrims {
+  std::vector<int32_t> kind;      // 0 prism, 1 quad, 2 triangle
+  std::vector<float> verts;       // n*18 (6 / 4 / 3 vertices used)
+  std::vector<uint32_t> gmodes;   // n*3 (prism x, y, z; quad / triangle x, y, 0)
+  std::vector<uint32_t> fmodes;   // n*3
+  std::vector<int64_t> goff;      // n, -1 = linear geometry
+  std::vector<int64_t> foff;      // n, -1 = no field
+  std::vector<float> geom;        // x, y, z blocks per curved primitive
+  std::vector<float> field;
+  int64_t size() const { return static_cast<int64_t>(kind.size()); }
+};
+
 struct HostScene {
+  HostPrims prims;
   std::vector<float> corners;     // n*24, XML vertex order
   std::vector<uint32_t> gmodes;   // n*3 (0,0,0 = trilinear from corners)
   std::vector<uint32_t> fmodes;   // n*3
@@ -153,6 +169,19 @@ struct ho_context {
   float bounds[6] = {0, 0, 0, 0, 0, 0};
   int64_t device_bytes = 0;
 
+  // prisms, quads and curved triangles (ho_prim.cu)
+  int64_t n_prims = 0;
+  void* d_prims = nullptr;        // n_prims PrimRec, kind-major
+  float* d_pgeom = nullptr;
+  float* d_pfield = nullptr;
+  float* d_pbox = nullptr;        // n_prims * 6
+  ho::BNode* d_pnodes = nullptr;  // max(1, n_prims - 1)
+  int64_t n_pnodes = 0;
+  int pbvh_depth = 0;
+  int64_t prim_counts[3] = {0, 0, 0};
+  ho_hit* d_phits = nullptr;      // hits of calls that asked for none (the primitive pass needs them)
+  size_t phits_cap = 0;
+
   ho::DevStats* d_stats = nullptr;
   ho_stats last{};
 
@@ -203,6 +232,10 @@ namespace ho {
 // Kernel launchers (ho_build.cu / ho_trace.cu). Return cudaError_t as int.
 int launch_setup(ho_context* c);
 int build_lbvh(ho_context* c);
+// LBVH over n device boxes (lo xyz, hi xyz); leaf aux bits from d_flags
+// (nullable). Allocates *nodes_out (max(1, n - 1) nodes).
+int build_tree(const float* d_box, const uint32_t* d_flags, int64_t n, cudaStream_t s, BNode** nodes_out,
+               int64_t* n_nodes_out, int* depth_out, float bounds[6]);
 struct TraceArgs {
   // camera mode (rays == nullptr): pixel-centre rays of a pinhole camera
   float origin[3], llc[3], horiz[3], vert[3];
@@ -223,6 +256,14 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s);
 // cudaError_t, or a negative HO_ status from the engine (message set).
 int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int spp, int max_depth, uint64_t seed,
                uint8_t* rgb, int64_t* rays_traced, ho_stats* totals, cudaStream_t s);
+// Primitive scene upload, boxes and tree (ho_prim.cu); frees the old one.
+int prims_build(ho_context* c);
+void prims_free(ho_context* c);
+// The primitive pass over the queries of a trace call: each query's hit is
+// replaced by a nearer primitive hit. fresh: the hexahedra were not traced
+// (a scene without them); every query is written.
+// stats: device counters for the traversal status (nullptr: the context's).
+int launch_prims(ho_context* c, const TraceArgs& a, ho_hit* hits, bool fresh, DevStats* stats, cudaStream_t s);
 // The FP64 check's residuals for caller-given hits (ho_rounds.cu).
 int launch_residuals(ho_context* c, int64_t n, const float* rays, const ho_hit* hits, double* out, cudaStream_t s);
 }  // namespace ho

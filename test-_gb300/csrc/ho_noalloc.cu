@@ -133,6 +133,20 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
   P.cand_e = nullptr;
   P.pred = nullptr;
   P.pred_items = 0;
+  if (c->n_elem == 0) {  // primitives only
+    TraceArgs a;
+    a.rays = rays_dev;
+    a.n_rays = n;
+    a.n_iso = 1;
+    a.iso[0] = iso;
+    a.iso_on_mask = P.iso_on_mask;
+    e = static_cast<cudaError_t>(launch_prims(c, a, out_dev, true, P.stats, s));
+    if (e != cudaSuccess) {
+      c->err = std::string("primitive kernel: ") + cudaGetErrorString(e);
+      return HO_ERR_CUDA;
+    }
+    return HO_OK;
+  }
   classify_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(P, n);
   e = cudaGetLastError();
   if (e == cudaSuccess) {
@@ -147,6 +161,15 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
       case 9: e = launch_n<9>(P, n, n, s, HO_MODE_BATCHED); break;
       default: e = cudaErrorInvalidValue; break;
     }
+  }
+  if (e == cudaSuccess && c->n_prims > 0) {
+    TraceArgs a;
+    a.rays = rays_dev;
+    a.n_rays = n;
+    a.n_iso = 1;
+    a.iso[0] = iso;
+    a.iso_on_mask = P.iso_on_mask;
+    e = static_cast<cudaError_t>(launch_prims(c, a, out_dev, false, P.stats, s));
   }
   if (e != cudaSuccess) {
     c->err = std::string("trace kernels: ") + cudaGetErrorString(e);

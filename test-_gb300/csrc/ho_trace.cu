@@ -142,7 +142,7 @@ static int enqueue_batched(ho_context* c, TraceParams& P, cudaStream_t s, bool l
   return enqueue_rounds(c, P, s, learned, n_queries, rounds);
 }
 
-int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
+static int trace_hexes(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   c->last_graph = false;
   c->stats_frozen = false;
   c->launches = 0;
@@ -295,6 +295,40 @@ int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   if (rc) return rc;
   c->graph_warm = true;
   return finish_rounds(c, P, s, learned, n_queries);
+}
+
+// A call's queries: the hexahedra's engine, then the primitive pass when the
+// scene has prisms, quads or triangles. The primitive pass reads each
+// query's hexahedron hit, so a call that asked for no hits gets a scratch
+// array; a scene without hexahedra runs the primitive pass alone.
+int launch_trace(ho_context* c, const TraceArgs& a_in, cudaStream_t s) {
+  if (c->n_prims == 0) return trace_hexes(c, a_in, s);
+  TraceArgs a = a_in;
+  const int64_t nq = a.rays ? a.n_rays * a.n_iso
+                            : (a.views ? a.n_queries_views : static_cast<int64_t>(a.width) * a.height * a.n_iso);
+  if (nq == 0) return 0;
+  if (!a.hits) {
+    if (static_cast<size_t>(nq) > c->phits_cap || !c->d_phits) {
+      cudaFree(c->d_phits);
+      c->d_phits = nullptr;
+      c->phits_cap = 0;
+      const cudaError_t e = cudaMalloc(&c->d_phits, static_cast<size_t>(nq) * sizeof(ho_hit));
+      if (e != cudaSuccess) return int(e);
+      c->phits_cap = static_cast<size_t>(nq);
+    }
+    a.hits = c->d_phits;
+  }
+  if (c->n_elem == 0) {
+    c->last_graph = false;
+    c->stats_frozen = false;
+    c->round_events_used = 0;
+    c->launches = 1;
+    return launch_prims(c, a, a.hits, true, nullptr, s);
+  }
+  const int rc = trace_hexes(c, a, s);
+  if (rc) return rc;
+  ++c->launches;
+  return launch_prims(c, a, a.hits, false, nullptr, s);
 }
 
 }  // namespace ho

@@ -87,10 +87,11 @@ __device__ __forceinline__ void load_child(const BNode* __restrict__ nodes, int 
   aux = __float_as_uint(b.w);
 }
 
-// Collect the K smallest candidate keys > (kt, ke) with entry <= tmax.
-// Returns false on traversal-stack overflow (status set by the caller).
-static __device__ bool collect(const TraceParams& P, float3 o, float3 d, float tmax, float kt, int ke, float (&bt)[kCandK],
-                        int (&be)[kCandK], bool& overflow, Work& w) {
+// Collect the K smallest candidate keys > (kt, ke) with entry <= tmax from
+// the tree `nodes`. Returns false on traversal-stack overflow (status set by
+// the caller).
+static __device__ bool collect_in(const BNode* __restrict__ nodes, float3 o, float3 d, float tmax, float kt, int ke,
+                                  float (&bt)[kCandK], int (&be)[kCandK], bool& overflow, Work& w) {
 #pragma unroll
   for (int j = 0; j < kCandK; ++j) {
     bt[j] = FLT_MAX;
@@ -110,7 +111,7 @@ static __device__ bool collect(const TraceParams& P, float3 o, float3 d, float t
     for (int c = 0; c < 2; ++c) {
       float lo[3], hi[3];
       uint32_t aux;
-      load_child(P.nodes, node, c, lo, hi, id[c], aux);
+      load_child(nodes, node, c, lo, hi, id[c], aux);
       hit[c] = false;
       te[c] = FLT_MAX;
       if (id[c] == kEmptyChild) continue;
@@ -145,6 +146,11 @@ static __device__ bool collect(const TraceParams& P, float3 o, float3 d, float t
     }
   }
   return true;
+}
+
+static __device__ __forceinline__ bool collect(const TraceParams& P, float3 o, float3 d, float tmax, float kt, int ke,
+                                               float (&bt)[kCandK], int (&be)[kCandK], bool& overflow, Work& w) {
+  return collect_in(P.nodes, o, d, tmax, kt, ke, bt, be, overflow, w);
 }
 
 __device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool active) {

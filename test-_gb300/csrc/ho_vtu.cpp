@@ -11,11 +11,13 @@
 // ends the cell list. Hexahedra (VTK cell types 12, and 72 and 25 as the
 // reference numbers its Lagrange and Bezier hexahedra) become trilinear
 // elements whose 8 corners are the cell's first 8 points in the file's order
-// (a higher-order VTK cell lists its corners first); a point index outside the
-// point list reads as the origin. No field. Wedges, quads and other cells are
-// skipped (the reference keeps wedges and quads as other primitive kinds).
+// (a higher-order VTK cell lists its corners first); wedges (13, 73, 26) become
+// linear prisms from their first 6 points and quads (9, 70, 22) linear quads
+// from their first 4, each taken in the file's order as the reference takes
+// them; a point index outside the point list reads as the origin. No field.
+// Other cells are skipped.
 //
-// The reference leaves these hexes' loader boxes zero-initialised, a point at
+// The reference leaves the hexes' loader boxes zero-initialised, a point at
 // the origin, which its BVH build takes as the element's box; here, as for
 // every element, the box is computed from the geometry at BVH build time.
 #include <algorithm>
@@ -100,6 +102,7 @@ bool int_array(const std::string& sec, const std::string& name, std::vector<int>
 
 constexpr int kVtkHex = 12, kVtkWedge = 13, kVtkQuad = 9;
 constexpr int kRefLagrangeHex = 72, kRefBezierHex = 25;
+constexpr int kLagrangeWedge = 73, kBezierWedge = 26, kLagrangeQuad = 70, kBezierQuad = 22;
 
 }  // namespace
 
@@ -140,6 +143,8 @@ int load_vtu(const std::string& path, HostScene& hs, std::string& err) {
   }
   const int n_points = static_cast<int>(xyz.size() / 3);
   HostScene out;
+  HostPrims& prims = out.prims;
+  auto point = [&](int p, int a) { return p >= 0 && p < n_points ? xyz[3 * size_t(p) + a] : 0.0f; };
   size_t cursor = 0;
   for (size_t c = 0; c < types.size(); ++c) {
     const int type = types[c];
@@ -153,8 +158,7 @@ int load_vtu(const std::string& path, HostScene& hs, std::string& err) {
     const bool hex = type == kVtkHex || type == kRefLagrangeHex || type == kRefBezierHex;
     if (hex && count >= 8) {
       for (int v = 0; v < 8; ++v) {
-        const int p = conn[cursor + v];
-        for (int a = 0; a < 3; ++a) out.corners.push_back(p >= 0 && p < n_points ? xyz[3 * size_t(p) + a] : 0.0f);
+        for (int a = 0; a < 3; ++a) out.corners.push_back(point(conn[cursor + v], a));
       }
       for (int a = 0; a < 3; ++a) {
         out.gmodes.push_back(0);
@@ -163,10 +167,24 @@ int load_vtu(const std::string& path, HostScene& hs, std::string& err) {
       out.goff.push_back(-1);
       out.foff.push_back(-1);
     }
+    const bool wedge = type == kVtkWedge || type == kLagrangeWedge || type == kBezierWedge;
+    const bool quad = type == kVtkQuad || type == kLagrangeQuad || type == kBezierQuad;
+    if ((wedge && count >= 6) || (quad && count >= 4)) {
+      const int nv = wedge ? 6 : 4;
+      prims.kind.push_back(wedge ? 0 : 1);
+      for (int v = 0; v < 6; ++v)
+        for (int a = 0; a < 3; ++a) prims.verts.push_back(v < nv ? point(conn[cursor + v], a) : 0.0f);
+      for (int a = 0; a < 3; ++a) {
+        prims.gmodes.push_back(0);
+        prims.fmodes.push_back(0);
+      }
+      prims.goff.push_back(-1);
+      prims.foff.push_back(-1);
+    }
     cursor += static_cast<size_t>(count);
   }
-  if (out.goff.empty()) {
-    err = "no hexahedral cells in " + path;
+  if (out.goff.empty() && prims.size() == 0) {
+    err = "no hexahedron, wedge or quad cells in " + path;
     return HO_ERR_PARSE;
   }
   // append only when the whole file loaded
@@ -175,6 +193,13 @@ int load_vtu(const std::string& path, HostScene& hs, std::string& err) {
   hs.fmodes.insert(hs.fmodes.end(), out.fmodes.begin(), out.fmodes.end());
   hs.goff.insert(hs.goff.end(), out.goff.begin(), out.goff.end());
   hs.foff.insert(hs.foff.end(), out.foff.begin(), out.foff.end());
+  HostPrims& hp = hs.prims;
+  hp.kind.insert(hp.kind.end(), prims.kind.begin(), prims.kind.end());
+  hp.verts.insert(hp.verts.end(), prims.verts.begin(), prims.verts.end());
+  hp.gmodes.insert(hp.gmodes.end(), prims.gmodes.begin(), prims.gmodes.end());
+  hp.fmodes.insert(hp.fmodes.end(), prims.fmodes.begin(), prims.fmodes.end());
+  hp.goff.insert(hp.goff.end(), prims.goff.begin(), prims.goff.end());
+  hp.foff.insert(hp.foff.end(), prims.foff.begin(), prims.foff.end());
   return HO_OK;
 }
 

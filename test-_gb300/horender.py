@@ -28,6 +28,7 @@ OPT_GPU_FIT, OPT_LAST_FIT_GPU = 8, 9
 MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
+HIT_PRISM, HIT_QUAD, HIT_TRI = 3, 4, 5
 FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW = 1, 2, 4
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("elem", "<i4"), ("face", "<i2"), ("kind", "<i2"), ("xi", "<f4", 3),
@@ -54,7 +55,8 @@ class _Synth(C.Structure):
 
 class _Info(C.Structure):
     _fields_ = [("n_elem", C.c_int64), ("n_nodes", C.c_int64), ("max_modes", C.c_int32),
-                ("bvh_depth", C.c_int32), ("device_bytes", C.c_int64), ("bounds", C.c_float * 6)]
+                ("bvh_depth", C.c_int32), ("device_bytes", C.c_int64), ("bounds", C.c_float * 6),
+                ("n_prisms", C.c_int64), ("n_quads", C.c_int64), ("n_tris", C.c_int64)]
 
 
 class _Stats(C.Structure):
@@ -82,6 +84,10 @@ def _load():
     L.ho_load_xml_fld.argtypes = [vp, C.c_char_p, C.c_char_p]
     L.ho_load_vtu.argtypes = [vp, C.c_char_p]
     L.ho_add_hexes.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, i64, vp]
+    for f in (L.ho_add_prisms, L.ho_add_quads, L.ho_add_tris):
+        f.argtypes = [vp, i64, vp, vp, vp, i64, vp, vp, vp, i64, vp]
+    L.ho_get_prims.argtypes = [vp] + [vp] * 11
+    L.ho_get_prim_boxes.argtypes = [vp, vp]
     L.ho_generate_synthetic.argtypes = [vp, C.POINTER(_Synth)]
     L.ho_get_scene.argtypes = [vp] + [vp] * 10
     L.ho_build_bvh.argtypes = [vp]
@@ -214,6 +220,61 @@ class Context:
         self._ck(lib.ho_add_hexes(self.h, n, _p(corners), _p(gm), _p(geom), geom.size, _p(go), _p(fm), _p(field),
                                   field.size, _p(fo)))
 
+    def _add_prims(self, fn, dims, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets):
+        verts = np.ascontiguousarray(verts, np.float32)
+        go = np.ascontiguousarray(geom_offsets, np.int64).reshape(-1)
+        n = go.shape[0]
+        gm = np.ascontiguousarray(geom_modes, np.uint32).reshape(n, dims)
+        fm = np.ascontiguousarray(field_modes, np.uint32).reshape(n, dims)
+        geom = np.ascontiguousarray(geom, np.float32)
+        field = np.ascontiguousarray(field, np.float32)
+        fo = np.ascontiguousarray(field_offsets, np.int64).reshape(-1)
+        self._ck(fn(self.h, n, _p(verts), _p(gm), _p(geom), geom.size, _p(go), _p(fm), _p(field), field.size, _p(fo)))
+
+    def add_prisms(self, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets):
+        """verts n x 6 x 3; modes n x 3 (see ho_add_prisms)."""
+        self._add_prims(lib.ho_add_prisms, 3, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets)
+
+    def add_quads(self, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets):
+        """verts n x 4 x 3; modes n x 2."""
+        self._add_prims(lib.ho_add_quads, 2, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets)
+
+    def add_tris(self, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets):
+        """verts n x 3 x 3; modes n x 2."""
+        self._add_prims(lib.ho_add_tris, 2, verts, geom_modes, geom, geom_offsets, field_modes, field, field_offsets)
+
+    def add_prim_arrays(self, arrs):
+        """Add every primitive of a kind-major list (kind, verts n x 6 x 3, modes
+        n x 3, offsets into one geometry and one field pool)."""
+        fns = {0: (self.add_prisms, 6, 3), 1: (self.add_quads, 4, 2), 2: (self.add_tris, 3, 2)}
+        for k, (fn, nv, dims) in fns.items():
+            m = np.asarray(arrs.kind) == k
+            if m.any():
+                fn(np.asarray(arrs.verts)[m][:, :nv], np.asarray(arrs.geom_modes)[m][:, :dims], arrs.geom,
+                   np.asarray(arrs.geom_offset)[m], np.asarray(arrs.field_modes)[m][:, :dims], arrs.field,
+                   np.asarray(arrs.field_offset)[m])
+
+    def get_prims(self) -> dict:
+        """The scene's prisms, quads and triangles, kind-major (ho_get_prims)."""
+        n, gl, fl = C.c_int64(), C.c_int64(), C.c_int64()
+        self._ck(lib.ho_get_prims(self.h, C.byref(n), None, None, None, None, C.byref(gl), None, None, None,
+                                  C.byref(fl), None))
+        n = n.value
+        out = dict(kind=np.zeros(n, np.int32), verts=np.zeros((n, 6, 3), np.float32),
+                   geom_modes=np.zeros((n, 3), np.uint32), geom=np.zeros(gl.value, np.float32),
+                   geom_offsets=np.zeros(n, np.int64), field_modes=np.zeros((n, 3), np.uint32),
+                   field=np.zeros(fl.value, np.float32), field_offsets=np.zeros(n, np.int64))
+        self._ck(lib.ho_get_prims(self.h, None, _p(out["kind"]), _p(out["verts"]), _p(out["geom_modes"]),
+                                  _p(out["geom"]), None, _p(out["geom_offsets"]), _p(out["field_modes"]),
+                                  _p(out["field"]), None, _p(out["field_offsets"])))
+        return out
+
+    def prim_boxes(self) -> np.ndarray:
+        i = self.info()
+        out = np.zeros((i["n_prisms"] + i["n_quads"] + i["n_tris"], 6), np.float32)
+        self._ck(lib.ho_get_prim_boxes(self.h, _p(out)))
+        return out
+
     def generate_synthetic(self, nx, ny, nz, order_min, order_max, curve_amp, n_gauss, seed):
         s = _Synth(nx, ny, nz, order_min, order_max, curve_amp, n_gauss, seed)
         self._ck(lib.ho_generate_synthetic(self.h, C.byref(s)))
@@ -245,7 +306,8 @@ class Context:
         i = _Info()
         self._ck(lib.ho_scene_info_get(self.h, C.byref(i)))
         return dict(n_elem=i.n_elem, n_nodes=i.n_nodes, max_modes=i.max_modes, bvh_depth=i.bvh_depth,
-                    device_bytes=i.device_bytes, bounds=list(i.bounds))
+                    device_bytes=i.device_bytes, bounds=list(i.bounds), n_prisms=i.n_prisms, n_quads=i.n_quads,
+                    n_tris=i.n_tris)
 
     def boxes(self) -> np.ndarray:
         n = self.info()["n_elem"]

@@ -3,7 +3,7 @@ XML unstructured grids (seeded, made here, not taken from any data set) and
 vtu_ref.npz, what the reference's own loader (load_vtu_file,
 FEM-AABB/vtu_loader.cpp:156-343, compiled into oracle/_ref/libref.so by
 oracle/build_ref.sh) made of each: whether it succeeded, how many hexahedra,
-prisms and quads it added, and the hexahedra's corner vertices.
+prisms and quads it added, and their vertices.
 
 Cases:
   grid      3x2x2 jittered linear hexes (type 12), Int32 arrays, a binary
@@ -16,7 +16,7 @@ Cases:
   badindex  point indices -1 and beyond the point list (read as the origin)
   wide      a connectivity value beyond int's range: the int parse stops
             there, the long long retry is not taken, later cells fall off
-  nohex     wedges and quads only (the reference succeeds, horender fails)
+  nohex     wedges and quads only
 
 Run: python tests/golden/make_vtu.py (needs oracle/_ref/libref.so).
 """
@@ -168,11 +168,15 @@ def main():
         try:
             rs = ob.RefScene(vtu=str(path))
             ok, counts, verts = True, rs.vtu_counts.copy(), rs.arrays().verts
+            prisms, quads = rs.vtu_prisms, rs.vtu_quads
         except RuntimeError:
             ok, counts, verts = False, np.zeros(3, np.int64), np.zeros((0, 8, 3), np.float32)
+            prisms, quads = np.zeros((0, 6, 3), np.float32), np.zeros((0, 4, 3), np.float32)
         ref[f"{name}_ok"] = np.array(ok)
         ref[f"{name}_counts"] = counts
         ref[f"{name}_verts"] = verts
+        ref[f"{name}_prisms"] = prisms
+        ref[f"{name}_quads"] = quads
         print(name, "ok" if ok else "failed", "hex/prism/quad", counts.tolist())
     np.savez_compressed(OUT / "vtu_ref.npz", **ref)
 

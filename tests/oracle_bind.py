@@ -38,6 +38,22 @@ class _SceneDesc(C.Structure):
     ]
 
 
+class _PrimsDesc(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("kind", C.c_void_p),
+        ("verts", C.c_void_p),
+        ("geom_modes", C.c_void_p),
+        ("geom_offset", C.c_void_p),
+        ("geom", C.c_void_p),
+        ("geom_len", C.c_int64),
+        ("field_modes", C.c_void_p),
+        ("field_offset", C.c_void_p),
+        ("field", C.c_void_p),
+        ("field_len", C.c_int64),
+    ]
+
+
 class _Counters(C.Structure):
     _fields_ = [("newton_iters", C.c_uint64), ("face_iters", C.c_uint64),
                 ("newton_solves", C.c_uint64), ("candidates", C.c_uint64)]
@@ -73,6 +89,13 @@ def lib():
         L.hor_camera_rays.argtypes = [vp, vp, vp, f32, i32, i32, vp]
         L.hor_shade.argtypes = [vp, vp, i64, vp]
         L.hor_trace_replay.argtypes = [vp, i32, vp, i64, f32, i32, vp, i32, vp, vp]
+        L.hor_prims_create.restype = vp
+        L.hor_prims_create.argtypes = [C.POINTER(_PrimsDesc)]
+        L.hor_prims_destroy.argtypes = [vp]
+        L.hor_prims_boxes.argtypes = [vp, i32, vp]
+        L.hor_prims_intersect.argtypes = [vp, i32, i32, vp, i64, vp, vp]
+        L.hor_prims_map.argtypes = [vp, i32, i32, vp, i64, vp]
+        L.hor_prims_trace.argtypes = [vp, i32, vp, i64, vp, i32]
         _lib = L
     return _lib
 
@@ -186,6 +209,84 @@ class OracleScene:
         return out
 
 
+PRIM_PRISM, PRIM_QUAD, PRIM_TRI = 0, 1, 2
+NVERTS = {PRIM_PRISM: 6, PRIM_QUAD: 4, PRIM_TRI: 3}
+
+
+class PrimArrays:
+    """Prisms, quads and curved triangles as one list (kind-major: all prisms,
+    then quads, then triangles, as the product stores them): kind (n), vertices
+    (n x 6 x 3, unused rows zero), geometry/field modes (n x 3), offsets
+    (-1 = linear geometry / no field) into flat fp32 pools; a geometry entry
+    is the x, y and z blocks back to back."""
+
+    def __init__(self, kind, verts, geom_modes, geom_offset, geom, field_modes, field_offset, field):
+        self.kind = np.ascontiguousarray(kind, np.int32)
+        self.verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 6, 3)
+        self.geom_modes = np.ascontiguousarray(geom_modes, np.uint32).reshape(-1, 3)
+        self.geom_offset = np.ascontiguousarray(geom_offset, np.int64)
+        self.geom = np.ascontiguousarray(geom, np.float32)
+        self.field_modes = np.ascontiguousarray(field_modes, np.uint32).reshape(-1, 3)
+        self.field_offset = np.ascontiguousarray(field_offset, np.int64)
+        self.field = np.ascontiguousarray(field, np.float32)
+
+    @property
+    def n(self) -> int:
+        return int(self.kind.shape[0])
+
+    def of_kind(self, k):
+        """(vertices n_k x nv x 3, geometry modes, offsets, field modes, offsets) of one kind."""
+        m = self.kind == k
+        return (self.verts[m][:, :NVERTS[k]], self.geom_modes[m], self.geom_offset[m], self.field_modes[m],
+                self.field_offset[m])
+
+
+class OraclePrims:
+    def __init__(self, arrs: PrimArrays):
+        self.arrs = arrs
+        g = arrs.geom if arrs.geom.size else np.zeros(1, np.float32)
+        f = arrs.field if arrs.field.size else np.zeros(1, np.float32)
+        self._keep = (g, f)
+        d = _PrimsDesc(arrs.n, _p(arrs.kind).value, _p(arrs.verts).value, _p(arrs.geom_modes).value,
+                       _p(arrs.geom_offset).value, _p(g).value, arrs.geom.size, _p(arrs.field_modes).value,
+                       _p(arrs.field_offset).value, _p(f).value, arrs.field.size)
+        self.h = lib().hor_prims_create(C.byref(d))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().hor_prims_destroy(self.h)
+            self.h = None
+
+    def boxes(self, precision=32) -> np.ndarray:
+        out = np.zeros((self.arrs.n, 6))
+        lib().hor_prims_boxes(self.h, precision, _p(out))
+        return out
+
+    def intersect(self, prim, rays, seg, precision=32):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        seg = np.ascontiguousarray(seg, np.float64).reshape(-1, 2)
+        out = np.zeros((rays.shape[0], 5))
+        assert lib().hor_prims_intersect(self.h, precision, prim, _p(rays), rays.shape[0], _p(seg), _p(out)) == 0
+        return out
+
+    def map(self, prim, xi, precision=64):
+        xi = np.ascontiguousarray(xi, np.float64).reshape(-1, 3)
+        out = np.zeros_like(xi)
+        lib().hor_prims_map(self.h, precision, prim, _p(xi), xi.shape[0], _p(out))
+        return out
+
+    def trace(self, rays, hex_hits=None, precision=32, threads=None):
+        """The primitive pass after the hexahedra: hex_hits (HIT_DTYPE, or
+        None = all miss) is each ray's hexahedron answer; returns the merged hits."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        io = np.zeros(rays.shape[0], HIT_DTYPE) if hex_hits is None else np.array(hex_hits, HIT_DTYPE, copy=True)
+        if hex_hits is None:
+            io["elem"] = -1
+            io["face"] = -1
+        lib().hor_prims_trace(self.h, precision, _p(rays), rays.shape[0], _p(io), threads or os.cpu_count() or 1)
+        return io
+
+
 def basis(nmodes: int, x: float, precision=64) -> np.ndarray:
     out = np.zeros((nmodes, 2))
     lib().hor_basis(precision, nmodes, float(x), _p(out))
@@ -228,6 +329,8 @@ def ref():
         L.ref_scene_create.argtypes = [i32, vp, vp, vp, i64, vp, vp, vp, i64, vp]
         L.ref_scene_load.restype = vp
         L.ref_scene_load.argtypes = [C.c_char_p, C.c_char_p]
+        L.ref_prim_intersect.argtypes = [i32, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
+        L.ref_vtu_prim_verts.argtypes = [C.c_char_p, vp, vp]
         L.ref_scene_load_vtu.restype = vp
         L.ref_scene_load_vtu.argtypes = [C.c_char_p, vp]
         L.ref_scene_destroy.argtypes = [vp]
@@ -260,6 +363,9 @@ class RefScene:
             self.h = L.ref_scene_load_vtu(vtu.encode(), _p(self.vtu_counts))
             if not self.h:
                 raise RuntimeError("reference loader failed")
+            self.vtu_prisms = np.zeros((int(self.vtu_counts[1]), 6, 3), np.float32)
+            self.vtu_quads = np.zeros((int(self.vtu_counts[2]), 4, 3), np.float32)
+            L.ref_vtu_prim_verts(vtu.encode(), _p(self.vtu_prisms), _p(self.vtu_quads))
         elif xml is not None:
             self.h = L.ref_scene_load(xml.encode(), fld.encode())
             if not self.h:
@@ -350,6 +456,35 @@ class RefScene:
         cnt = np.zeros(rays.shape[0], np.int32)
         ref().ref_trace_order(self.h, _p(rays), rays.shape[0], float(iso), _p(out), _p(order), order_cap, _p(cnt))
         return out, order, cnt
+
+
+def ref_prim_intersect(arrs: PrimArrays, prim: int, rays, seg):
+    """The reference's own box and IntersectRayWith* for primitive `prim` of
+    arrs: (box (6,), results n x 5 = hit, t, r, s, t-coordinate)."""
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    seg = np.ascontiguousarray(seg, np.float64).reshape(-1, 2)
+    k = int(arrs.kind[prim])
+    verts = np.ascontiguousarray(arrs.verts[prim], np.float32)
+    gm = np.ascontiguousarray(arrs.geom_modes[prim], np.uint32)
+    ptrs = [None, None, None]
+    keep = []
+    if arrs.geom_offset[prim] >= 0:
+        from_ = int(arrs.geom_offset[prim])
+        m = [int(v) for v in gm]
+        if k == PRIM_QUAD:
+            blk = m[0] * m[1]
+        else:
+            top = m[2] if k == PRIM_PRISM else m[1]
+            blk = sum(max(top - i, 0) for i in range(m[0])) * (m[1] if k == PRIM_PRISM else 1)
+        for a in range(3):
+            b = np.ascontiguousarray(arrs.geom[from_ + a * blk: from_ + (a + 1) * blk], np.float32)
+            keep.append(b)
+            ptrs[a] = _p(b)
+    box = np.zeros(6, np.float32)
+    out = np.zeros((rays.shape[0], 5))
+    ref().ref_prim_intersect(k, _p(verts), _p(gm), ptrs[0], ptrs[1], ptrs[2], _p(rays), rays.shape[0], _p(seg),
+                             _p(box), _p(out))
+    return box, out
 
 
 def ref_basis(nmodes: int, x: float) -> np.ndarray:

@@ -2,10 +2,9 @@
 loader (load_vtu_file, FEM-AABB/vtu_loader.cpp:156-343).
 
 The fixtures under golden/vtu and what the reference loader made of them
-(vtu_ref.npz) come from make_vtu.py. Criteria: the same hexahedra, in the same
-order, with bit-identical corner vertices (both sides parse the text as
-float); a file whose cells hold no hexahedron fails here (the reference
-succeeds when it found prisms or quads, which are other primitive kinds);
+(vtu_ref.npz) come from make_vtu.py. Criteria: the same hexahedra, prisms
+and quads, in the same order, with bit-identical vertices (both sides parse
+the text as float); a file without any of those cells fails on both sides;
 every failure leaves the scene unchanged."""
 from __future__ import annotations
 
@@ -17,7 +16,7 @@ from conftest import GOLDEN
 
 VTU = GOLDEN / "vtu"
 REF = np.load(VTU / "vtu_ref.npz")
-CASES = ["grid", "mixed", "nooffsets", "badrange", "badindex", "wide"]
+CASES = ["grid", "mixed", "nooffsets", "badrange", "badindex", "wide", "nohex"]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -26,6 +25,12 @@ def test_matches_reference_loader(name):
     with hr.Context(0) as ctx:
         ctx.load_vtu(str(VTU / f"{name}.vtu"))
         s = ctx.get_scene()
+        p = ctx.get_prims()
+    counts = REF[f"{name}_counts"]
+    assert np.array_equal(np.bincount(p["kind"], minlength=3), [counts[1], counts[2], 0])
+    assert np.array_equal(p["verts"][p["kind"] == 0], REF[f"{name}_prisms"])
+    assert np.array_equal(p["verts"][p["kind"] == 1][:, :4], REF[f"{name}_quads"])
+    assert (p["geom_offsets"] == -1).all() and (p["field_offsets"] == -1).all()
     ref_verts = REF[f"{name}_verts"]
     assert len(s["corners"]) == int(REF[f"{name}_counts"][0]) == len(ref_verts)
     assert np.array_equal(s["corners"], ref_verts)
@@ -45,16 +50,27 @@ def test_edge_cases_read_as_the_reference_reads_them():
     assert len(REF["wide_verts"]) == 1
 
 
-def test_no_hexahedra_fails_and_leaves_scene_unchanged():
-    assert bool(REF["nohex_ok"]) and list(REF["nohex_counts"]) == [0, 2, 1]
+def test_no_supported_cell_fails_and_leaves_scene_unchanged(tmp_path):
+    pts = " ".join("%d %d %d" % (i & 1, (i >> 1) & 1, i >> 2) for i in range(8))
+    text = (f"<Points><DataArray>{pts}</DataArray></Points><Cells>"
+            "<DataArray Name=\"connectivity\">0 1 2 4 1 3 2 7</DataArray>"
+            "<DataArray Name=\"offsets\">4 8</DataArray>"
+            "<DataArray Name=\"types\">10 10</DataArray></Cells>")
+    path = broken(tmp_path, text)
     with hr.Context(0) as ctx:
         ctx.load_vtu(str(VTU / "grid.vtu"))
         before = ctx.get_scene()["corners"].copy()
         with pytest.raises(hr.HoError) as ei:
-            ctx.load_vtu(str(VTU / "nohex.vtu"))
+            ctx.load_vtu(path)
         assert ei.value.code == -5
-        assert "no hexahedral cells" in str(ei.value)
+        assert "no hexahedron, wedge or quad cells" in str(ei.value)
         assert np.array_equal(ctx.get_scene()["corners"], before)
+        assert ctx.get_prims()["kind"].size == 0
+    import oracle_bind as ob
+
+    if ob.ref_available():
+        with pytest.raises(RuntimeError):
+            ob.RefScene(vtu=path)
 
 
 def test_appends_to_the_scene(tmp_path):
