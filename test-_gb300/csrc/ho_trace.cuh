@@ -116,20 +116,22 @@ static __device__ bool collect_in(const BNode* __restrict__ nodes, float3 o, flo
       te[c] = FLT_MAX;
       if (id[c] == kEmptyChild) continue;
       float a0, a1;
-      // the current bound: the closest hit so far, tightened by the K-th key
-      const float bound = fminf(tmax, bt[kCandK - 1]);
-      if (!ray_box(o, d, lo, hi, 0.001f, bound, a0, a1)) continue;
+      if (!ray_box(o, d, lo, hi, 0.001f, tmax, a0, a1)) continue;
       if (a1 < kt) continue;  // everything inside enters before the last visited key
+      // with the buffer full, a box entered after the K-th key holds only
+      // candidates for a later walk: note that one is needed
+      const bool full = be[kCandK - 1] != INT_MAX;
       if (id[c] < 0) {
         const int e = ~id[c];
         if (!key_less(kt, ke, a0, e)) continue;  // already visited
-        if (a0 > tmax) continue;
         if (!key_less(a0, e, bt[kCandK - 1], be[kCandK - 1])) {
           overflow = true;
           continue;
         }
-        if (be[kCandK - 1] != INT_MAX) overflow = true;  // the largest falls out
+        if (full) overflow = true;  // the largest falls out
         kbuf_insert(bt, be, a0, e);
+      } else if (full && a0 > bt[kCandK - 1]) {
+        overflow = true;
       } else {
         hit[c] = true;
         te[c] = a0;
