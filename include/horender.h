@@ -144,6 +144,11 @@ typedef struct {
                                 kernels' launches (CUDA events), else 0      */
   uint64_t round_launches;   /* HO_OPT_TIME_ROUNDS: round kernel launches     */
   uint64_t tail_rays;        /* rays finished by the tail (HO_OPT_TAIL)       */
+  uint64_t prim_candidates;  /* (query, prism/quad/triangle) pairs visited    */
+  uint64_t prim_iters;       /* their Newton / projection iterations          */
+  uint64_t prim_flops;       /* algorithmic FP32 flops of the primitive pass  */
+  uint64_t prim_kernel_ns;   /* HO_OPT_TIME_ROUNDS: device time of the
+                                primitive pass (CUDA events), else 0          */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

@@ -144,6 +144,18 @@ int read_stats(ho_context* c) {
   s.solve_steps = ds.c[ho::ST_STEPS];
   s.lane_steps = ds.c[ho::ST_LANES];
   s.tail_rays = ds.c[ho::ST_TAIL];
+  s.prim_candidates = ds.c[ho::ST_PRIM_CAND];
+  s.prim_iters = ds.c[ho::ST_PRIM_ITERS];
+  s.prim_flops = ds.c[ho::ST_PRIM_FLOPS];
+  s.prim_kernel_ns = 0;
+  if (c->prim_timed) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->prim_events[0], c->prim_events[1]) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, HO_ERR_CUDA, "primitive timing events could not be read");
+    }
+    s.prim_kernel_ns = static_cast<uint64_t>(static_cast<double>(ms) * 1e6 + 0.5);
+  }
   s.kernel_launches = static_cast<uint64_t>(c->launches);
   s.round_kernel_ns = 0;
   s.round_launches = 0;
@@ -193,6 +205,8 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_stats);
     cudaFree(c->d_hits);
     cudaFree(c->d_phits);
+    if (c->prim_events[0]) cudaEventDestroy(c->prim_events[0]);
+    if (c->prim_events[1]) cudaEventDestroy(c->prim_events[1]);
     cudaFree(c->d_rgb);
     cudaFree(c->d_rays);
     cudaFree(c->d_views);

@@ -181,6 +181,8 @@ struct ho_context {
   int64_t prim_counts[3] = {0, 0, 0};
   ho_hit* d_phits = nullptr;      // hits of calls that asked for none (the primitive pass needs them)
   size_t phits_cap = 0;
+  cudaEvent_t prim_events[2] = {nullptr, nullptr};  // HO_OPT_TIME_ROUNDS: around the primitive pass
+  bool prim_timed = false;        // the last trace call recorded them
 
   ho::DevStats* d_stats = nullptr;
   ho_stats last{};

@@ -79,6 +79,10 @@ enum StatSlot {
   ST_CHECK_FINAL,
   ST_FLOPS,
   ST_TAIL,
+  ST_FLUSH,  // the slots before this one are summed by the hexahedron kernels' flush
+  ST_PRIM_CAND = ST_FLUSH,
+  ST_PRIM_ITERS,
+  ST_PRIM_FLOPS,
   ST_COUNT
 };
 

@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
   float best = h.kind != HO_HIT_MISS ? h.t : FLT_MAX;
   int win = -1;
   float3 xw = make_float3(0.f, 0.f, 0.f);
-  uint32_t iters = 0;
+  PrimWork pw;
+  unsigned cand = 0;
   Work w;
   float kt = -FLT_MAX;
   int ke = -1;
@@ -119,7 +120,8 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
       const PrimRec p = P.prims[ce];
       float te, tx, th;
       float3 xh;
-      if (pr_slab(o, d, p.lo, p.hi, 0.001f, best, te, tx) && pr_hit(p, P.geom, o, d, 0.001f, best, th, xh, iters) &&
+      ++cand;
+      if (pr_slab(o, d, p.lo, p.hi, 0.001f, best, te, tx) && pr_hit(p, P.geom, o, d, 0.001f, best, th, xh, pw) &&
           th > 0.001f && th < best) {
         best = th;
         win = ce;
@@ -146,7 +148,21 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
     h.u = pr_field(p, P.field, xw);
     h.flags = 0;
   }
-  h.iters += iters;
+  h.iters += pw.iters;
+  // counters: summed over the warp when all its lanes are here together
+  // (the last block's tail warp is partial), else added one by one
+  const unsigned long long v[3] = {cand, pw.iters, pw.flops};
+  const bool whole = __activemask() == 0xffffffffu;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    unsigned long long x = v[k];
+    if (whole) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) != 0) x = 0;
+    }
+    if (x) atomicAdd(&P.stats->c[ST_PRIM_CAND + k], x);
+  }
   if (P.hits && (P.fresh || win >= 0)) P.hits[q] = h;
   if (P.rgb && P.rays == nullptr && (P.fresh || win >= 0)) {
     HitState s;

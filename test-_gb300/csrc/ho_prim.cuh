@@ -272,6 +272,25 @@ __device__ inline float3 pr_point(const PrimRec& p, const float* __restrict__ po
   return X;
 }
 
+// Work of one query's primitive visits: solver iterations and algorithmic
+// FP32 flops. A curved evaluation costs (6 + b) flops per coefficient and
+// output (b = 2 basis products in 3-D, 1 in 2-D; outputs: the point plus 3 or
+// 2 tangents when asked for); a linear one a fixed count per kind.
+struct PrimWork {
+  uint32_t iters = 0;
+  unsigned long long flops = 0;
+};
+
+__device__ inline unsigned pr_geom_flops(const PrimRec& p, bool tan) {
+  if (pr_curved(p)) {
+    const unsigned outs = 1u + (tan ? (p.kind == kPrimPrism ? 3u : 2u) : 0u);
+    return static_cast<unsigned>(prim_block(p.kind, p.gm)) * (p.kind == kPrimPrism ? 8u : 7u) * outs;
+  }
+  if (p.kind == kPrimPrism) return tan ? 170u : 60u;
+  if (p.kind == kPrimQuad) return tan ? 100u : 40u;
+  return tan ? 47u : 35u;
+}
+
 // Field value (0 without a field).
 __device__ float pr_field(const PrimRec& p, const float* __restrict__ pool, float3 x) {
   if (p.foff < 0) return 0.f;
@@ -398,7 +417,7 @@ __device__ inline bool pr_solve3(const float A[9], float3 b, float3& x) {
 // inside [-1.05, 1.05]^3; a start ends when the closest ray point leaves
 // the box segment or J is singular.
 __device__ bool pr_hit_prism(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
-                             float tmax, float& th, float3& xh, uint32_t& iters) {
+                             float tmax, float& th, float3& xh, PrimWork& w) {
   float enter, exit;
   if (!pr_slab(o, d, p.lo, p.hi, tmin, tmax, enter, exit)) return false;
   const float seeds[7][3] = {{0.f, 0.f, 0.f},     {-0.5f, -0.5f, -0.5f}, {0.5f, -0.5f, -0.5f}, {0.f, 0.5f, -0.5f},
@@ -406,7 +425,8 @@ __device__ bool pr_hit_prism(const PrimRec& p, const float* __restrict__ pool, f
   for (int sd = 0; sd < 7; ++sd) {
     float3 x = make_float3(seeds[sd][0], seeds[sd][1], seeds[sd][2]);
     for (int it = 0; it < 60; ++it) {
-      ++iters;
+      ++w.iters;
+      w.flops += pr_geom_flops(p, true) + 81u;  // + closest point, residual, 3x3 solve
       float3 X, tan[3];
       pr_geom(p, pool, x, X, tan);
       const float tau = pr_param(o, d, X);
@@ -429,11 +449,12 @@ __device__ bool pr_hit_prism(const PrimRec& p, const float* __restrict__ pool, f
 
 // Gauss-Newton projection of q onto a surface primitive from (r0, s0).
 __device__ bool pr_project(const PrimRec& p, const float* __restrict__ pool, float3 q, float r0, float s0, float& r,
-                           float& s, int max_it, float tol, uint32_t& iters) {
+                           float& s, int max_it, float tol, PrimWork& w) {
   r = r0;
   s = s0;
   for (int it = 0; it < max_it; ++it) {
-    ++iters;
+    ++w.iters;
+    w.flops += pr_geom_flops(p, true) + 39u;  // + metric tensor, 2x2 solve
     float3 X, tan[3];
     pr_geom(p, pool, make_float3(r, s, 0.f), X, tan);
     const float3 diff = pr_sub(X, q);
@@ -455,14 +476,15 @@ __device__ bool pr_project(const PrimRec& p, const float* __restrict__ pool, flo
 // steps at 1e-4, inside [-1.05, 1.05]^2, maps back within 5e-4); triangle
 // (4 starts of 30 steps at 1e-4, then the clamped-barycentric inside test).
 __device__ bool pr_contains(const PrimRec& p, const float* __restrict__ pool, float3 q, float& r_out, float& s_out,
-                            uint32_t& iters) {
+                            PrimWork& w) {
   if (p.kind == kPrimQuad) {
     const float seeds[9][2] = {{0.f, 0.f},     {-0.5f, -0.5f}, {0.5f, -0.5f}, {-0.5f, 0.5f}, {0.5f, 0.5f},
                                {-0.9f, -0.9f}, {0.9f, -0.9f},  {-0.9f, 0.9f}, {0.9f, 0.9f}};
     for (int sd = 0; sd < 9; ++sd) {
       float r, s;
-      if (!pr_project(p, pool, q, seeds[sd][0], seeds[sd][1], r, s, 40, 1e-4f, iters)) continue;
+      if (!pr_project(p, pool, q, seeds[sd][0], seeds[sd][1], r, s, 40, 1e-4f, w)) continue;
       if (r < -1.05f || r > 1.05f || s < -1.05f || s > 1.05f) continue;
+      w.flops += pr_geom_flops(p, false);
       const float3 X = pr_point(p, pool, make_float3(r, s, 0.f));
       if (fabsf(X.x - q.x) > 5e-4f || fabsf(X.y - q.y) > 5e-4f || fabsf(X.z - q.z) > 5e-4f) continue;
       r_out = r;
@@ -474,12 +496,12 @@ __device__ bool pr_contains(const PrimRec& p, const float* __restrict__ pool, fl
   const float seeds[4][2] = {{0.f, 0.f}, {-0.5f, -0.5f}, {0.5f, -0.5f}, {0.f, 0.5f}};
   float r = 0.f, s = 0.f;
   bool ok = false;
-  for (int sd = 0; sd < 4 && !ok; ++sd) ok = pr_project(p, pool, q, seeds[sd][0], seeds[sd][1], r, s, 30, 1e-4f, iters);
+  for (int sd = 0; sd < 4 && !ok; ++sd) ok = pr_project(p, pool, q, seeds[sd][0], seeds[sd][1], r, s, 30, 1e-4f, w);
   if (!ok) return false;
   float u, v;
   pr_bary(r, s, u, v);
-  const float w = 1.0f - u - v;
-  if (!(u >= -1e-3f && v >= -1e-3f && w >= -1e-3f)) return false;
+  const float w0 = 1.0f - u - v;
+  if (!(u >= -1e-3f && v >= -1e-3f && w0 >= -1e-3f)) return false;
   r_out = r;
   s_out = s;
   return true;
@@ -490,7 +512,7 @@ __device__ bool pr_contains(const PrimRec& p, const float* __restrict__ pool, fl
 // surface, else the vertex plane, else the segment middle; then Newton on
 // (r, s, t) for x(r, s) = o + t d, at most 40 steps at 1e-5.
 __device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
-                               float tmax, float& th, float3& xh, uint32_t& iters) {
+                               float tmax, float& th, float3& xh, PrimWork& w) {
   float enter, exit;
   if (!pr_slab(o, d, p.lo, p.hi, tmin, tmax, enter, exit)) return false;
   const bool quad = p.kind == kPrimQuad;
@@ -500,7 +522,7 @@ __device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool,
   for (int i = 0; i <= n && !started; ++i) {
     const float u = static_cast<float>(i) / static_cast<float>(n);
     float rr, ss;
-    if (pr_contains(p, pool, pr_at(o, d, enter + (exit - enter) * u), rr, ss, iters)) {
+    if (pr_contains(p, pool, pr_at(o, d, enter + (exit - enter) * u), rr, ss, w)) {
       r = rr;
       s = ss;
       t = pr_param(o, d, pr_point(p, pool, make_float3(r, s, 0.f)));
@@ -518,7 +540,7 @@ __device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool,
         float tp = pr_dot(nrm, pr_sub(a, o)) / den;
         if (tp < enter || tp > exit) tp = mid;
         float rr, ss;
-        if (pr_contains(p, pool, pr_at(o, d, tp), rr, ss, iters)) {
+        if (pr_contains(p, pool, pr_at(o, d, tp), rr, ss, w)) {
           r = rr;
           s = ss;
           t = pr_param(o, d, pr_point(p, pool, make_float3(r, s, 0.f)));
@@ -531,7 +553,7 @@ __device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool,
         if (q >= enter && q <= exit) tp = q;
       }
       float rr, ss;
-      if (pr_contains(p, pool, pr_at(o, d, tp), rr, ss, iters)) {
+      if (pr_contains(p, pool, pr_at(o, d, tp), rr, ss, w)) {
         r = rr;
         s = ss;
       }
@@ -539,7 +561,8 @@ __device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool,
     }
   }
   for (int it = 0; it < 40; ++it) {
-    ++iters;
+    ++w.iters;
+    w.flops += pr_geom_flops(p, true) + 69u;  // + ray point, residual, 3x3 solve
     float3 X, tan[3];
     pr_geom(p, pool, make_float3(r, s, 0.f), X, tan);
     const float3 res = pr_sub(pr_at(o, d, t), X);
@@ -561,9 +584,9 @@ __device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool,
 }
 
 __device__ inline bool pr_hit(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
-                              float tmax, float& th, float3& xh, uint32_t& iters) {
-  return p.kind == kPrimPrism ? pr_hit_prism(p, pool, o, d, tmin, tmax, th, xh, iters)
-                              : pr_hit_surface(p, pool, o, d, tmin, tmax, th, xh, iters);
+                              float tmax, float& th, float3& xh, PrimWork& w) {
+  return p.kind == kPrimPrism ? pr_hit_prism(p, pool, o, d, tmin, tmax, th, xh, w)
+                              : pr_hit_surface(p, pool, o, d, tmin, tmax, th, xh, w);
 }
 
 // Normal at a hit: unit cross product of the r and s tangents turned against

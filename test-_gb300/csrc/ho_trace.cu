@@ -301,7 +301,25 @@ static int trace_hexes(ho_context* c, const TraceArgs& a, cudaStream_t s) {
 // scene has prisms, quads or triangles. The primitive pass reads each
 // query's hexahedron hit, so a call that asked for no hits gets a scratch
 // array; a scene without hexahedra runs the primitive pass alone.
+// The primitive pass, between two timing events when HO_OPT_TIME_ROUNDS is on.
+static int timed_prims(ho_context* c, const TraceArgs& a, bool fresh, cudaStream_t s) {
+  c->prim_timed = false;
+  if (c->time_rounds) {
+    for (cudaEvent_t& e : c->prim_events)
+      if (!e && cudaEventCreate(&e) != cudaSuccess) return int(cudaGetLastError());
+    const cudaError_t e = cudaEventRecord(c->prim_events[0], s);
+    if (e != cudaSuccess) return int(e);
+  }
+  const int rc = launch_prims(c, a, a.hits, fresh, nullptr, s);
+  if (rc || !c->time_rounds) return rc;
+  const cudaError_t e = cudaEventRecord(c->prim_events[1], s);
+  if (e != cudaSuccess) return int(e);
+  c->prim_timed = true;
+  return 0;
+}
+
 int launch_trace(ho_context* c, const TraceArgs& a_in, cudaStream_t s) {
+  c->prim_timed = false;
   if (c->n_prims == 0) return trace_hexes(c, a_in, s);
   TraceArgs a = a_in;
   const int64_t nq = a.rays ? a.n_rays * a.n_iso
@@ -323,12 +341,12 @@ int launch_trace(ho_context* c, const TraceArgs& a_in, cudaStream_t s) {
     c->stats_frozen = false;
     c->round_events_used = 0;
     c->launches = 1;
-    return launch_prims(c, a, a.hits, true, nullptr, s);
+    return timed_prims(c, a, true, s);
   }
   const int rc = trace_hexes(c, a, s);
   if (rc) return rc;
   ++c->launches;
-  return launch_prims(c, a, a.hits, false, nullptr, s);
+  return timed_prims(c, a, false, s);
 }
 
 }  // namespace ho

@@ -157,11 +157,11 @@ static __device__ __forceinline__ bool collect(const TraceParams& P, float3 o, f
 
 __device__ __forceinline__ void flush_work(DevStats* st, const Work& w, bool active) {
   // warp-aggregated counters
-  unsigned long long v[ST_COUNT] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled,
+  unsigned long long v[ST_FLUSH] = {active ? 1u : 0u, w.cand, w.geom, w.map, w.field, w.newton, w.face, w.culled,
                                     w.nodes, w.accepted, w.rejected, w.restarts, w.cyc[0], w.cyc[1], w.cyc[2],
                                     w.cyc[3], w.steps, w.lanes, 0ull, 0ull, 0ull, 0ull, 0ull, w.flops, 0ull};
 #pragma unroll
-  for (int s = 0; s < ST_COUNT; ++s) {
+  for (int s = 0; s < ST_FLUSH; ++s) {
     unsigned long long x = v[s];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
