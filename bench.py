@@ -218,6 +218,24 @@ def cpu_baseline(workload, seconds, n_iso_sample=None):
 def run_reference(args, rank, world):
     import horender as hr
 
+    if args.workload in PRIMS:
+        if rank != 0:
+            return
+        vals, cb = [], None
+        for i in range(args.warmup + args.steps):
+            cb = prims_cpu_baseline(args.workload, max(2.0, args.cpu_seconds / 2))
+            if i >= args.warmup:
+                vals.append(cb["value"])
+        v = float(np.mean(vals))
+        cfg = PRIMS[args.workload]
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                          "config": {"workload": args.workload, "rays": f"{cfg['width']}x{cfg['height']} primary"},
+                          "cpu_baseline": dict(cb, value=v),
+                          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
     if args.workload in hr.MULTIVIEW:
         w = hr.WORKLOADS[hr.MULTIVIEW[args.workload][0]]
     elif args.workload in hr.PATHS:
@@ -455,6 +473,141 @@ def run_gpu(args, rank, world):
     ctx.close()
 
 
+# ---- prisms, quads and curved triangles --------------------------------------
+# One scene of the three non-hexahedral primitive kinds (tents on a floor of
+# quads before a wall of triangles, half of them curved), rendered primary
+# rays only: every query goes through the primitive pass (the scene has no
+# hexahedra). Seeded, generated on the host (prim_synth).
+PRIMS = {"prims_sheet": dict(seed=11, n_side=64, width=1920, height=1080,
+                             camera=((1.6, 1.1, 1.9), (0.5, 0.2, 0.3), 50.0))}
+
+
+def prims_scene(name):
+    import prim_synth
+
+    cfg = PRIMS[name]
+    return prim_synth.mixed_scene(seed=cfg["seed"], n_side=cfg["n_side"]), cfg
+
+
+def prims_cpu_baseline(name, seconds):
+    """The FP32 oracle's primitive pass on a bounded random sample of the
+    workload's rays, all host threads."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_bind as ob
+
+    ps, cfg = prims_scene(name)
+    arrs = ob.PrimArrays(ps.kind, ps.verts, ps.geom_modes, ps.geom_offset, ps.geom, ps.field_modes, ps.field_offset,
+                         ps.field)
+    op = ob.OraclePrims(arrs)
+    frm, at, fov = cfg["camera"]
+    rays = ob.camera_rays(frm, at, (0, 1, 0), fov, cfg["width"], cfg["height"])
+    rng = np.random.default_rng(0)
+    threads = os.cpu_count() or 1
+    done = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        idx = rng.integers(0, rays.shape[0], 4096)
+        op.trace(rays[idx], None, 32, threads)
+        done += idx.size
+    dt = time.perf_counter() - t0
+    return {"value": done / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{done} primary rays drawn uniformly from the {cfg['width']}x{cfg['height']} image, "
+                      f"FP32 oracle port of the reference's primitive routines, {threads} threads, {dt:.1f} s"}
+
+
+def run_prims(args, rank, world):
+    import torch
+
+    import horender as hr
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ps, cfg = prims_scene(args.workload)
+    W, H = (args.width, args.height) if args.width and args.height else (cfg["width"], cfg["height"])
+    frm, at, fov = cfg["camera"]
+    cam = hr.Camera(frm, at, vfov_deg=fov)
+    ctx = hr.Context(local)
+    ctx.add_prim_arrays(ps)
+    ctx.build_bvh()
+    ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
+    info = ctx.info()
+    nq = W * H
+    rgb = torch.empty(nq * 3, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    keys = ("prim_kernel_ns", "prim_flops", "prim_candidates", "prim_iters", "kernel_launches")
+    per = dict.fromkeys(keys, 0)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            ctx.render_device(cam, [0.0], W, H, rgb.data_ptr(), None, sp)
+    torch.cuda.synchronize()
+    barrier(world)
+    evs = []
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.render_device(cam, [0.0], W, H, rgb.data_ptr(), None, sp)
+                b.record(stream)
+                evs.append((a, b))
+                s_step = ctx.stats()
+                for k in keys:
+                    per[k] += s_step[k]
+        torch.cuda.synchronize()
+    barrier(world)
+    total_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs) / 1e3, world)
+    queries = sum_over_ranks(nq * args.steps, world)
+    value = queries / total_s / 1e6
+    kernel_s = per["prim_kernel_ns"] * 1e-9 / args.steps
+    flops = per["prim_flops"] / args.steps
+    achieved = flops / kernel_s / 1e12
+    # e2e: public API, host image buffer, D2H inside the timed region
+    host_rgb = torch.empty((1, H, W, 3), dtype=torch.uint8).pin_memory()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(0 if args.no_e2e else args.steps):
+        ctx.render(cam, [0.0], W, H, rgb_out=host_rgb.numpy())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = None if args.no_e2e else queries / e2e_s / 1e6
+    fp32_peak = fp32_peak_tflops(torch, dev)
+    st = ctx.stats()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "gb300",
+        "mode": "primitive pass (prisms, quads, curved triangles; thread per query)",
+        "config": {"workload": args.workload, "primitives": {"prisms": info["n_prisms"], "quads": info["n_quads"],
+                                                             "triangles": info["n_tris"]},
+                   "curved": int((ps.geom_offset >= 0).sum()), "rays": f"{W}x{H} primary",
+                   "queries_per_step": nq, "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": (achieved / fp32_peak) if fp32_peak else None, "traffic": None,
+                     "peak_source": "FP32 FMA loop measured in this run (peaks file has HBM and bf16 only)",
+                     "kernel": "prim_trace_kernel", "flops_per_launch": flops, "launches": args.steps,
+                     "ms_per_launch": kernel_s * 1e3, "share_of_step": kernel_s * args.steps / total_s},
+        "e2e": None if e2e is None else {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 44 + 4,
+                                         "d2h_bytes_per_step": nq * 3},
+        "gpu_launches": per["kernel_launches"],
+        "clocks": clk.summary(),
+        "work": {"candidates_per_query": per["prim_candidates"] / queries,
+                 "iterations_per_query": per["prim_iters"] / queries, "last_call": st},
+        "scene": info,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = prims_cpu_baseline(args.workload, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def fp32_peak_tflops(torch, dev):
     """Measured FP32 FMA rate of this GPU in TFLOP/s (ho_measure_fp32_peak)."""
     import horender as hr
@@ -467,6 +620,8 @@ def main():
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload in PRIMS:
+        run_prims(args, rank, world)
     else:
         run_gpu(args, rank, world)
     if world > 1:

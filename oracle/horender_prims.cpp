@@ -13,6 +13,7 @@
 // hit. The reference visits hexes and primitives together in BVH stack
 // order instead.
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstring>
 #include <thread>
@@ -53,12 +54,95 @@ namespace {
 
 constexpr int kHitPrism = 3;  // hit kinds of the three primitive kinds: 3 + kind
 
+struct GNode {
+  double lo[3], hi[3];
+  int left, right;  // leaf: left = first in `order`, right = -count - 1
+};
+
 struct PScene {
   std::vector<float> geom, field;
   std::vector<Prim> prims;
   std::vector<int> local;  // index among the primitives of the same kind
   std::vector<double> box32, box64;
+  // candidate gathering: a median-split tree over boxes holding both
+  // precisions' boxes, slightly inflated; the exact test decides afterwards
+  std::vector<double> gbox;
+  std::vector<int> order;
+  std::vector<GNode> nodes;
 };
+
+int build_gather(PScene& s, int first, int count) {
+  GNode nd;
+  for (int a = 0; a < 3; ++a) {
+    nd.lo[a] = 1e300;
+    nd.hi[a] = -1e300;
+  }
+  for (int i = 0; i < count; ++i) {
+    const double* b = &s.gbox[6 * s.order[first + i]];
+    for (int a = 0; a < 3; ++a) {
+      nd.lo[a] = std::min(nd.lo[a], b[a]);
+      nd.hi[a] = std::max(nd.hi[a], b[3 + a]);
+    }
+  }
+  const int me = static_cast<int>(s.nodes.size());
+  s.nodes.push_back(nd);
+  if (count <= 4) {
+    s.nodes[me].left = first;
+    s.nodes[me].right = -count - 1;
+    return me;
+  }
+  int axis = 0;
+  for (int a = 1; a < 3; ++a)
+    if (nd.hi[a] - nd.lo[a] > nd.hi[axis] - nd.lo[axis]) axis = a;
+  const int mid = first + count / 2;
+  std::nth_element(s.order.begin() + first, s.order.begin() + mid, s.order.begin() + first + count,
+                   [&](int x, int y) {
+                     const double cx = s.gbox[6 * x + axis] + s.gbox[6 * x + 3 + axis];
+                     const double cy = s.gbox[6 * y + axis] + s.gbox[6 * y + 3 + axis];
+                     return cx < cy || (cx == cy && x < y);
+                   });
+  const int l = build_gather(s, first, mid - first);
+  const int r = build_gather(s, mid, first + count - mid);
+  s.nodes[me].left = l;
+  s.nodes[me].right = r;
+  return me;
+}
+
+bool slab_line(const double* lo, const double* hi, const double o[3], const double d[3]) {
+  double te = 0.0, tx = 1e300;
+  for (int a = 0; a < 3; ++a) {
+    if (std::fabs(d[a]) < 1e-12) {
+      if (o[a] < lo[a] || o[a] > hi[a]) return false;
+      continue;
+    }
+    double t0 = (lo[a] - o[a]) / d[a], t1 = (hi[a] - o[a]) / d[a];
+    if (t0 > t1) std::swap(t0, t1);
+    te = std::max(te, t0);
+    tx = std::min(tx, t1);
+    if (te > tx) return false;
+  }
+  return true;
+}
+
+// Every primitive whose inflated box the ray's half-line meets.
+void gather(const PScene& s, const float* rf, std::vector<int>& out) {
+  out.clear();
+  if (s.nodes.empty()) return;
+  const double o[3] = {rf[0], rf[1], rf[2]}, d[3] = {rf[3], rf[4], rf[5]};
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const GNode& n = s.nodes[stack[--sp]];
+    if (!slab_line(n.lo, n.hi, o, d)) continue;
+    if (n.right < 0) {
+      for (int i = 0; i < -n.right - 1; ++i) out.push_back(s.order[n.left + i]);
+    } else {
+      stack[sp++] = n.left;
+      stack[sp++] = n.right;
+    }
+  }
+}
 
 template <class R> void boxes(const PScene& s, std::vector<double>& out) {
   out.assign(s.prims.size() * 6, 0.0);
@@ -81,14 +165,15 @@ template <class R> void box_of(const PScene& s, int i, R lo[3], R hi[3]) {
 }
 
 template <class R> void trace_one(const PScene& s, const float* rf, hor_prim_hit& io,
-                                  std::vector<std::pair<R, int>>& cands) {
+                                  std::vector<std::pair<R, int>>& cands, std::vector<int>& near) {
   Ray<R> ray;
   ray.o = mk<R>(rf[0], rf[1], rf[2]);
   ray.d = mk<R>(rf[3], rf[4], rf[5]);
   const R eps = static_cast<R>(0.001f);
   R best = io.kind != 0 ? static_cast<R>(io.t) : static_cast<R>(FLT_MAX);
   cands.clear();
-  for (int i = 0; i < static_cast<int>(s.prims.size()); ++i) {
+  gather(s, rf, near);
+  for (int i : near) {
     R lo[3], hi[3], te, tx;
     box_of<R>(s, i, lo, hi);
     if (ray_box<R>(ray, mk<R>(lo[0], lo[1], lo[2]), mk<R>(hi[0], hi[1], hi[2]), eps, best, te, tx))
@@ -167,6 +252,18 @@ void* hor_prims_create(const hor_prims_desc* d) {
   }
   boxes<float>(*s, s->box32);
   boxes<double>(*s, s->box64);
+  const int n = static_cast<int>(s->prims.size());
+  s->gbox.resize(6 * static_cast<size_t>(n));
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      const double lo = std::min(s->box32[6 * i + a], s->box64[6 * i + a]);
+      const double hi = std::max(s->box32[6 * i + 3 + a], s->box64[6 * i + 3 + a]);
+      s->gbox[6 * i + a] = lo - 1e-6 * (1.0 + std::fabs(lo));
+      s->gbox[6 * i + 3 + a] = hi + 1e-6 * (1.0 + std::fabs(hi));
+    }
+  s->order.resize(n);
+  for (int i = 0; i < n; ++i) s->order[i] = i;
+  if (n > 0) build_gather(*s, 0, n);
   return s;
 }
 
@@ -235,12 +332,13 @@ int hor_prims_map(void* sp, int precision, int prim, const double* xi, int64_t n
 int hor_prims_trace(void* sp, int precision, const float* rays, int64_t n, hor_prim_hit* io, int nthreads) {
   PScene* s = static_cast<PScene*>(sp);
   parallel_for(n, nthreads, [&](int64_t b, int64_t e) {
+    std::vector<int> near;
     if (precision == 32) {
       std::vector<std::pair<float, int>> c;
-      for (int64_t i = b; i < e; ++i) trace_one<float>(*s, rays + 6 * i, io[i], c);
+      for (int64_t i = b; i < e; ++i) trace_one<float>(*s, rays + 6 * i, io[i], c, near);
     } else {
       std::vector<std::pair<double, int>> c;
-      for (int64_t i = b; i < e; ++i) trace_one<double>(*s, rays + 6 * i, io[i], c);
+      for (int64_t i = b; i < e; ++i) trace_one<double>(*s, rays + 6 * i, io[i], c, near);
     }
   });
   return 0;
