@@ -149,6 +149,7 @@ typedef struct {
   uint64_t prim_flops;       /* algorithmic FP32 flops of the primitive pass  */
   uint64_t prim_kernel_ns;   /* HO_OPT_TIME_ROUNDS: device time of the
                                 primitive pass (CUDA events), else 0          */
+  uint64_t prim_node_visits; /* primitive-tree nodes visited by that pass     */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

@@ -114,8 +114,23 @@ void camera_basis(const ho_camera& cam, int W, int H, ho::TraceArgs& a) {
   a.height = H;
 }
 
+// End of a *_device call on stream s: later stats reads wait for it. A
+// stream the caller is capturing gets no event (nothing has run yet).
+int mark_call_done(ho_context* c, cudaStream_t s) {
+  c->call_done_pending = false;
+  if (s == c->stream) return HO_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(s, &cs), "cudaStreamIsCapturing");
+  if (cs != cudaStreamCaptureStatusNone) return HO_OK;
+  if (!c->call_done) CK(cudaEventCreateWithFlags(&c->call_done, cudaEventDisableTiming), "cudaEventCreate");
+  CK(cudaEventRecord(c->call_done, s), "cudaEventRecord");
+  c->call_done_pending = true;
+  return HO_OK;
+}
+
 int read_stats(ho_context* c) {
   ho::DevStats ds;
+  if (c->call_done_pending) CK(cudaStreamWaitEvent(c->stream, c->call_done, 0), "cudaStreamWaitEvent");
   CK(cudaMemcpyAsync(&ds, c->d_stats, sizeof(ds), cudaMemcpyDeviceToHost, c->stream), "read stats");
   CK(cudaStreamSynchronize(c->stream), "sync");
   ho_stats& s = c->last;
@@ -147,6 +162,7 @@ int read_stats(ho_context* c) {
   s.prim_candidates = ds.c[ho::ST_PRIM_CAND];
   s.prim_iters = ds.c[ho::ST_PRIM_ITERS];
   s.prim_flops = ds.c[ho::ST_PRIM_FLOPS];
+  s.prim_node_visits = ds.c[ho::ST_PRIM_NODES];
   s.prim_kernel_ns = 0;
   if (c->prim_timed) {
     float ms = 0.f;
@@ -207,6 +223,7 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->d_phits);
     if (c->prim_events[0]) cudaEventDestroy(c->prim_events[0]);
     if (c->prim_events[1]) cudaEventDestroy(c->prim_events[1]);
+    if (c->call_done) cudaEventDestroy(c->call_done);
     cudaFree(c->d_rgb);
     cudaFree(c->d_rays);
     cudaFree(c->d_views);
@@ -603,7 +620,7 @@ int ho_render_device(ho_context* c, const ho_camera* cam, const float* iso, int 
   CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
   rc = ho::launch_trace(c, a, s);
   if (rc) return cuda_fail(c, rc, "trace kernel");
-  return HO_OK;
+  return mark_call_done(c, s);
 }
 
 int ho_render_views_device(ho_context* c, int n_views, const ho_camera* cams, const int32_t* widths,
@@ -655,7 +672,7 @@ int ho_render_views_device(ho_context* c, int n_views, const ho_camera* cams, co
   CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
   rc = ho::launch_trace(c, a, s);
   if (rc) return cuda_fail(c, rc, "trace kernel");
-  return HO_OK;
+  return mark_call_done(c, s);
 }
 
 int ho_render_views(ho_context* c, int n_views, const ho_camera* cams, const int32_t* widths, const int32_t* heights,
@@ -714,10 +731,10 @@ int ho_intersect_device(ho_context* c, int64_t n, const float* rays_dev, float i
   a.hits = out_dev;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
   CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
-  if (n == 0) return HO_OK;
+  if (n == 0) return mark_call_done(c, s);
   const int rc = ho::launch_trace(c, a, s);
   if (rc) return cuda_fail(c, rc, "trace kernel");
-  return HO_OK;
+  return mark_call_done(c, s);
 }
 
 int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso_enabled, ho_hit* out) {

@@ -186,6 +186,11 @@ struct ho_context {
 
   ho::DevStats* d_stats = nullptr;
   ho_stats last{};
+  // Recorded on the caller's stream at the end of a *_device call, so that
+  // reading the counters and timing events over the context's own stream
+  // waits for that call's kernels.
+  cudaEvent_t call_done = nullptr;
+  bool call_done_pending = false;
 
   // render scratch
   ho_hit* d_hits = nullptr;

@@ -83,6 +83,7 @@ enum StatSlot {
   ST_PRIM_CAND = ST_FLUSH,
   ST_PRIM_ITERS,
   ST_PRIM_FLOPS,
+  ST_PRIM_NODES,
   ST_COUNT
 };
 

@@ -213,6 +213,11 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
     tot.round_kernel_ns += st.round_kernel_ns;
     tot.round_launches += st.round_launches;
     tot.tail_rays += st.tail_rays;
+    tot.prim_candidates += st.prim_candidates;
+    tot.prim_iters += st.prim_iters;
+    tot.prim_flops += st.prim_flops;
+    tot.prim_kernel_ns += st.prim_kernel_ns;
+    tot.prim_node_visits += st.prim_node_visits;
     tot.graph = st.graph;
     tot.max_modes = st.max_modes;
     tot.status |= st.status;

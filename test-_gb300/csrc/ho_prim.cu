@@ -31,6 +31,17 @@ namespace {
   } while (0)
 
 constexpr int kPrimThreads = 128;
+// Resident blocks per SM the register budget is sized for (80 registers a
+// thread; measured faster than 64, 128 or an unbounded 208 despite spills),
+// and candidates collected per walk of the primitive tree (a ray with more
+// walks again; 16 halves the node visits but measured no faster).
+#ifndef HO_PRIM_MIN_BLOCKS
+#define HO_PRIM_MIN_BLOCKS 6
+#endif
+#ifndef HO_PRIM_CAND_K
+#define HO_PRIM_CAND_K 8
+#endif
+constexpr int kPrimCandK = HO_PRIM_CAND_K;
 
 __global__ void prim_setup_kernel(PrimRec* __restrict__ recs, const float* __restrict__ pool, int64_t n,
                                   float* __restrict__ box) {
@@ -66,9 +77,9 @@ struct PrimParams {
   DevStats* stats;
 };
 
-__global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) {
-  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (q >= P.n_queries) return;
+// One query's primitive pass: the candidates in (box entry, index) order on
+// [0.001, closest hit so far], then the hit record and the pixel.
+__device__ __forceinline__ void prim_query(const PrimParams& P, int64_t q, PrimWork& pw, unsigned& cand, Work& w) {
   float3 o, d;
   float iso;
   bool iso_on;
@@ -89,26 +100,24 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
   float best = h.kind != HO_HIT_MISS ? h.t : FLT_MAX;
   int win = -1;
   float3 xw = make_float3(0.f, 0.f, 0.f);
-  PrimWork pw;
-  unsigned cand = 0;
-  Work w;
+  const uint32_t iters0 = pw.iters;
   float kt = -FLT_MAX;
   int ke = -1;
   for (;;) {
-    float bt[kCandK];
-    int be[kCandK];
+    float bt[kPrimCandK];
+    int be[kPrimCandK];
     bool overflow;
-    if (!collect_in(P.nodes, o, d, best, kt, ke, bt, be, overflow, w)) {
+    if (!collect_in<kPrimCandK>(P.nodes, o, d, best, kt, ke, bt, be, overflow, w)) {
       atomicOr(&P.stats->status, kStatusStackOverflow);
       break;
     }
     bool done = false;
 #pragma unroll 1
-    for (int j = 0; j < kCandK; ++j) {
+    for (int j = 0; j < kPrimCandK; ++j) {
       float ct = bt[0];
       int ce = be[0];
 #pragma unroll
-      for (int m = 1; m < kCandK; ++m)
+      for (int m = 1; m < kPrimCandK; ++m)
         if (j == m) {
           ct = bt[m];
           ce = be[m];
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
         done = true;
         break;
       }
-      const PrimRec p = P.prims[ce];
+      const PrimRec& p = P.prims[ce];  // read in place: the solvers take it by reference
       float te, tx, th;
       float3 xh;
       ++cand;
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
     if (done || !overflow) break;
   }
   if (win >= 0) {
-    const PrimRec p = P.prims[win];
+    const PrimRec& p = P.prims[win];
     const float3 n = pr_normal(p, P.geom, xw, d);
     h.t = best;
     h.elem = p.local;
@@ -148,21 +157,7 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
     h.u = pr_field(p, P.field, xw);
     h.flags = 0;
   }
-  h.iters += pw.iters;
-  // counters: summed over the warp when all its lanes are here together
-  // (the last block's tail warp is partial), else added one by one
-  const unsigned long long v[3] = {cand, pw.iters, pw.flops};
-  const bool whole = __activemask() == 0xffffffffu;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    unsigned long long x = v[k];
-    if (whole) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-      if ((threadIdx.x & 31) != 0) x = 0;
-    }
-    if (x) atomicAdd(&P.stats->c[ST_PRIM_CAND + k], x);
-  }
+  h.iters += pw.iters - iters0;
   if (P.hits && (P.fresh || win >= 0)) P.hits[q] = h;
   if (P.rgb && P.rays == nullptr && (P.fresh || win >= 0)) {
     HitState s;
@@ -172,6 +167,28 @@ __global__ void __launch_bounds__(kPrimThreads) prim_trace_kernel(PrimParams P) 
     s.kind = h.kind;
     s.n = make_float3(h.n[0], h.n[1], h.n[2]);
     shade(s, d, P.rgb + 3 * q);
+  }
+}
+
+__global__ void __launch_bounds__(kPrimThreads, HO_PRIM_MIN_BLOCKS) prim_trace_kernel(PrimParams P) {
+  PrimWork pw;
+  unsigned cand = 0;
+  Work w;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q < P.n_queries) prim_query(P, q, pw, cand, w);
+  // counters: summed over the warp when all its lanes are here together
+  // (the last block's tail warp is partial), else added one by one
+  const unsigned long long v[4] = {cand, pw.iters, pw.flops, w.nodes};
+  const bool whole = __activemask() == 0xffffffffu;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    unsigned long long x = v[k];
+    if (whole) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) != 0) x = 0;
+    }
+    if (x) atomicAdd(&P.stats->c[ST_PRIM_CAND + k], x);
   }
 }
 
@@ -271,8 +288,8 @@ int launch_prims(ho_context* c, const TraceArgs& a, ho_hit* hits, bool fresh, De
   P.fresh = fresh;
   P.stats = stats ? stats : c->d_stats;
   if (P.n_queries == 0) return 0;
-  prim_trace_kernel<<<static_cast<unsigned>((P.n_queries + kPrimThreads - 1) / kPrimThreads), kPrimThreads, 0, s>>>(
-      P);
+  const int64_t blocks = (P.n_queries + kPrimThreads - 1) / kPrimThreads;
+  prim_trace_kernel<<<static_cast<unsigned>(blocks), kPrimThreads, 0, s>>>(P);
   return static_cast<int>(cudaGetLastError());
 }
 

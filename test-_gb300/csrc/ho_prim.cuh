@@ -16,6 +16,7 @@
 namespace ho {
 
 constexpr int kPrimPrism = 0, kPrimQuad = 1, kPrimTri = 2;
+constexpr int kPrimMaxModes = 9;  // modes per direction, geometry and field
 
 // One primitive in device memory (128 bytes). Vertices: prism 6 (quad base
 // 0-3 at t = -1, top edge 4-5), quad 4 (vertex v at r = +-1 by bit 0 and
@@ -130,22 +131,41 @@ __device__ inline float3 pr_vert(const PrimRec& p, int v) { return make_float3(p
 __device__ inline bool pr_curved(const PrimRec& p) { return p.goff >= 0 && p.gm != 0; }
 
 // Modal point (and, when tan != nullptr, the r, s, t tangents) of a curved
-// primitive. Sum orders: prism i, j, k; quad j, i; triangle i, j.
-__device__ void pr_modal_geom(const PrimRec& p, const float* __restrict__ pool, float3 x, float3& X, float3* tan) {
+// primitive. Sum orders: prism i, j, k; quad j, i; triangle i, j. Each 1-D
+// basis value is computed once per evaluation and reused across the other
+// indices; the values and the order of the sums are those of evaluating
+// every term afresh. Out of line, like the other solver routines below: one
+// copy of each in the kernel keeps its code within the instruction cache.
+__device__ __noinline__ void pr_modal_geom(const PrimRec& p, const float* __restrict__ pool, float3 x, float3& X,
+                                           float3* tan) {
   const float* c = pool + p.goff;
   const int blk = prim_block(p.kind, p.gm);
   const unsigned mx = pmode(p.gm, 0), my = pmode(p.gm, 1), mz = pmode(p.gm, 2);
   float v[3] = {0.f, 0.f, 0.f}, dr[3] = {0.f, 0.f, 0.f}, ds[3] = {0.f, 0.f, 0.f}, dt[3] = {0.f, 0.f, 0.f};
+  float ar[kPrimMaxModes], dar[kPrimMaxModes], bs[kPrimMaxModes], dbs[kPrimMaxModes];
+  for (unsigned i = 0; i < mx; ++i) {
+    ar[i] = pr_a(i, x.x);
+    dar[i] = tan ? pr_a_d(i, x.x) : 0.f;
+  }
   int idx = 0;
   if (p.kind == kPrimPrism) {
+    for (unsigned j = 0; j < my; ++j) {
+      bs[j] = pr_a(j, x.y);
+      dbs[j] = tan ? pr_a_d(j, x.y) : 0.f;
+    }
+    float bt[kPrimMaxModes], dbt[kPrimMaxModes];
     for (unsigned i = 0; i < mx; ++i) {
-      const float ri = pr_a(i, x.x), dri = pr_a_d(i, x.x);
+      const float ri = ar[i], dri = dar[i];
+      const unsigned top = mz > i ? mz - i : 0;
+      for (unsigned k = 0; k < top; ++k) {
+        bt[k] = pr_b(i, k, x.z);
+        dbt[k] = tan ? pr_b_d(i, k, x.z) : 0.f;
+      }
       for (unsigned j = 0; j < my; ++j) {
-        const float sj = pr_a(j, x.y), dsj = pr_a_d(j, x.y);
-        const unsigned top = mz > i ? mz - i : 0;
+        const float sj = bs[j], dsj = dbs[j];
         for (unsigned k = 0; k < top; ++k, ++idx) {
-          const float tk = pr_b(i, k, x.z);
-          const float dtk = tan ? pr_b_d(i, k, x.z) : 0.f;
+          const float tk = bt[k];
+          const float dtk = dbt[k];
           for (int a = 0; a < 3; ++a) {
             const float cf = __ldg(c + a * blk + idx);
             v[a] += cf * ri * sj * tk;
@@ -160,9 +180,9 @@ __device__ void pr_modal_geom(const PrimRec& p, const float* __restrict__ pool, 
     }
   } else if (p.kind == kPrimQuad) {
     for (unsigned j = 0; j < my; ++j) {
-      const float sj = pr_a(j, x.y), dsj = pr_a_d(j, x.y);
+      const float sj = pr_a(j, x.y), dsj = tan ? pr_a_d(j, x.y) : 0.f;
       for (unsigned i = 0; i < mx; ++i, ++idx) {
-        const float ri = pr_a(i, x.x), dri = pr_a_d(i, x.x);
+        const float ri = ar[i], dri = dar[i];
         for (int a = 0; a < 3; ++a) {
           const float cf = __ldg(c + a * blk + idx);
           v[a] += cf * ri * sj;
@@ -175,7 +195,7 @@ __device__ void pr_modal_geom(const PrimRec& p, const float* __restrict__ pool, 
     }
   } else {
     for (unsigned i = 0; i < mx; ++i) {
-      const float ai = pr_a(i, x.x), dai = pr_a_d(i, x.x);
+      const float ai = ar[i], dai = dar[i];
       const unsigned top = my > i ? my - i : 0;
       for (unsigned j = 0; j < top; ++j, ++idx) {
         const float bj = pr_b(i, j, x.y);
@@ -212,7 +232,7 @@ __device__ inline void pr_bary(float r, float s, float& u, float& v) {
 
 // Linear point and tangents. The prism's t tangent carries the reference's
 // extra 0.5 (1 + r) dr term (PrismElement.cu:264-270).
-__device__ void pr_linear_geom(const PrimRec& p, float3 x, float3& X, float3* tan) {
+__device__ __noinline__ void pr_linear_geom(const PrimRec& p, float3 x, float3& X, float3* tan) {
   float acc[3] = {0.f, 0.f, 0.f}, dr[3] = {0.f, 0.f, 0.f}, ds[3] = {0.f, 0.f, 0.f}, dt[3] = {0.f, 0.f, 0.f};
   if (p.kind == kPrimPrism) {
     const float rm = 1.0f - x.x, rp = 1.0f + x.x, sm = 1.0f - x.y, sp = 1.0f + x.y, tm = 1.0f - x.z, tp = 1.0f + x.z;
@@ -292,7 +312,7 @@ __device__ inline unsigned pr_geom_flops(const PrimRec& p, bool tan) {
 }
 
 // Field value (0 without a field).
-__device__ float pr_field(const PrimRec& p, const float* __restrict__ pool, float3 x) {
+__device__ __noinline__ float pr_field(const PrimRec& p, const float* __restrict__ pool, float3 x) {
   if (p.foff < 0) return 0.f;
   const float* c = pool + p.foff;
   const unsigned mx = pmode(p.fm, 0), my = pmode(p.fm, 1), mz = pmode(p.fm, 2);
@@ -416,7 +436,7 @@ __device__ inline bool pr_solve3(const float A[9], float3 b, float3& x) {
 // J dx = x(rst) - (closest ray point), at most 60; accepted within 1e-5 and
 // inside [-1.05, 1.05]^3; a start ends when the closest ray point leaves
 // the box segment or J is singular.
-__device__ bool pr_hit_prism(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
+__device__ __noinline__ bool pr_hit_prism(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
                              float tmax, float& th, float3& xh, PrimWork& w) {
   float enter, exit;
   if (!pr_slab(o, d, p.lo, p.hi, tmin, tmax, enter, exit)) return false;
@@ -448,7 +468,7 @@ __device__ bool pr_hit_prism(const PrimRec& p, const float* __restrict__ pool, f
 }
 
 // Gauss-Newton projection of q onto a surface primitive from (r0, s0).
-__device__ bool pr_project(const PrimRec& p, const float* __restrict__ pool, float3 q, float r0, float s0, float& r,
+__device__ __noinline__ bool pr_project(const PrimRec& p, const float* __restrict__ pool, float3 q, float r0, float s0, float& r,
                            float& s, int max_it, float tol, PrimWork& w) {
   r = r0;
   s = s0;
@@ -475,7 +495,7 @@ __device__ bool pr_project(const PrimRec& p, const float* __restrict__ pool, flo
 // Does q lie on the surface? Quad (QuadElementContainsPoint, 9 starts, 40
 // steps at 1e-4, inside [-1.05, 1.05]^2, maps back within 5e-4); triangle
 // (4 starts of 30 steps at 1e-4, then the clamped-barycentric inside test).
-__device__ bool pr_contains(const PrimRec& p, const float* __restrict__ pool, float3 q, float& r_out, float& s_out,
+__device__ __noinline__ bool pr_contains(const PrimRec& p, const float* __restrict__ pool, float3 q, float& r_out, float& s_out,
                             PrimWork& w) {
   if (p.kind == kPrimQuad) {
     const float seeds[9][2] = {{0.f, 0.f},     {-0.5f, -0.5f}, {0.5f, -0.5f}, {-0.5f, 0.5f}, {0.5f, 0.5f},
@@ -511,7 +531,7 @@ __device__ bool pr_contains(const PrimRec& p, const float* __restrict__ pool, fl
 // from the first of 11 (quad) / 9 (triangle) box-segment points on the
 // surface, else the vertex plane, else the segment middle; then Newton on
 // (r, s, t) for x(r, s) = o + t d, at most 40 steps at 1e-5.
-__device__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
+__device__ __noinline__ bool pr_hit_surface(const PrimRec& p, const float* __restrict__ pool, float3 o, float3 d, float tmin,
                                float tmax, float& th, float3& xh, PrimWork& w) {
   float enter, exit;
   if (!pr_slab(o, d, p.lo, p.hi, tmin, tmax, enter, exit)) return false;
@@ -592,7 +612,7 @@ __device__ inline bool pr_hit(const PrimRec& p, const float* __restrict__ pool, 
 // Normal at a hit: unit cross product of the r and s tangents turned against
 // the ray, then negated once more unless strictly against it (the
 // reference's HitRecord::set_face_normal).
-__device__ inline float3 pr_normal(const PrimRec& p, const float* __restrict__ pool, float3 x, float3 d) {
+__device__ __noinline__ float3 pr_normal(const PrimRec& p, const float* __restrict__ pool, float3 x, float3 d) {
   float3 X, tan[3];
   pr_geom(p, pool, x, X, tan);
   float3 n = pr_unit(pr_cross(tan[0], tan[1]));

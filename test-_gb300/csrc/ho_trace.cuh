@@ -64,9 +64,10 @@ __device__ __forceinline__ bool key_less(float ta, int ea, float tb, int eb) {
 }
 
 // Insert (t, e) into the ascending register buffer; the largest falls out.
-__device__ __forceinline__ void kbuf_insert(float (&bt)[kCandK], int (&be)[kCandK], float t, int e) {
+template <int K>
+__device__ __forceinline__ void kbuf_insert(float (&bt)[K], int (&be)[K], float t, int e) {
 #pragma unroll
-  for (int j = 0; j < kCandK; ++j) {
+  for (int j = 0; j < K; ++j) {
     const bool sw = key_less(t, e, bt[j], be[j]);
     const float tt = sw ? bt[j] : t;
     const int ee = sw ? be[j] : e;
@@ -90,10 +91,11 @@ __device__ __forceinline__ void load_child(const BNode* __restrict__ nodes, int 
 // Collect the K smallest candidate keys > (kt, ke) with entry <= tmax from
 // the tree `nodes`. Returns false on traversal-stack overflow (status set by
 // the caller).
+template <int K>
 static __device__ bool collect_in(const BNode* __restrict__ nodes, float3 o, float3 d, float tmax, float kt, int ke,
-                                  float (&bt)[kCandK], int (&be)[kCandK], bool& overflow, Work& w) {
+                                  float (&bt)[K], int (&be)[K], bool& overflow, Work& w) {
 #pragma unroll
-  for (int j = 0; j < kCandK; ++j) {
+  for (int j = 0; j < K; ++j) {
     bt[j] = FLT_MAX;
     be[j] = INT_MAX;
   }
@@ -120,17 +122,17 @@ static __device__ bool collect_in(const BNode* __restrict__ nodes, float3 o, flo
       if (a1 < kt) continue;  // everything inside enters before the last visited key
       // with the buffer full, a box entered after the K-th key holds only
       // candidates for a later walk: note that one is needed
-      const bool full = be[kCandK - 1] != INT_MAX;
+      const bool full = be[K - 1] != INT_MAX;
       if (id[c] < 0) {
         const int e = ~id[c];
         if (!key_less(kt, ke, a0, e)) continue;  // already visited
-        if (!key_less(a0, e, bt[kCandK - 1], be[kCandK - 1])) {
+        if (!key_less(a0, e, bt[K - 1], be[K - 1])) {
           overflow = true;
           continue;
         }
         if (full) overflow = true;  // the largest falls out
         kbuf_insert(bt, be, a0, e);
-      } else if (full && a0 > bt[kCandK - 1]) {
+      } else if (full && a0 > bt[K - 1]) {
         overflow = true;
       } else {
         hit[c] = true;

@@ -166,6 +166,33 @@ def test_vtu_wedges_and_quads_render(oracle):
     compare(h, oracle.OraclePrims(arrs).trace(rays, None, 32), "VTU wedges and quads")
 
 
+def test_stats_after_device_call_on_caller_stream(prim_scene):
+    """A primitive-only scene rendered on a caller's stream: ho_get_stats,
+    read straight after the call returns, waits for that stream and reports
+    the finished call (counters equal to a synchronous render's, the
+    primitive pass's event time present)."""
+    torch = pytest.importorskip("torch")
+    ctx, arrs, z, op = prim_scene
+    W, H = 320, 240
+    ctx.render(CAM, [0.0], W, H, iso_zero_disables=True, want_rgb=False, want_hits=True)
+    want = ctx.stats()
+    rgb = torch.empty(W * H * 3, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
+    try:
+        for _ in range(3):
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                ctx.render_device(CAM, [0.0], W, H, rgb.data_ptr(), None, stream.cuda_stream)
+            got = ctx.stats()
+            for k in ("rays", "prim_candidates", "prim_iters", "prim_flops"):
+                assert got[k] == want[k], (k, got[k], want[k])
+            assert got["prim_kernel_ns"] > 0
+    finally:
+        ctx.set_option(hr.OPT_TIME_ROUNDS, 0)
+        torch.cuda.synchronize()
+
+
 def test_noalloc_path_with_primitives(prim_scene, oracle):
     torch = pytest.importorskip("torch")
     ctx, arrs, z, op = prim_scene
