@@ -436,6 +436,12 @@ int ho_measure_fp32_peak(int device, double* tflops);
 /* Replaces: save_image_ppm (FEM-AABB/raytracer.cu:480-494). P6, rows in
  * buffer order. */
 int ho_save_ppm(const uint8_t* rgb, int width, int height, const char* path);
+/* Beside save_image_ppm (FEM-AABB/raytracer.cu:480-494), which is the
+ * reference's only image writer: the same image as an 8-bit RGB PNG, rows in
+ * buffer order, uncompressed (stored deflate blocks). HO_ERR_ARG on a NULL
+ * argument or a size <= 0; HO_ERR_RANGE when the image data would exceed
+ * 2^31 bytes; HO_ERR_IO when the file cannot be written. */
+int ho_save_png(const uint8_t* rgb, int width, int height, const char* path);
 
 #ifdef __cplusplus
 }

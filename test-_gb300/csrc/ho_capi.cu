@@ -1222,4 +1222,83 @@ int ho_save_ppm(const uint8_t* rgb, int W, int H, const char* path) {
   return ok ? HO_OK : HO_ERR_IO;
 }
 
+// PNG (ISO/IEC 15948): 8-bit RGB, no interlace, every row with filter type
+// 0, the image data a zlib stream (RFC 1950) of stored deflate blocks
+// (RFC 1951, uncompressed), chunk CRC-32 over type and data.
+namespace {
+uint32_t png_crc(const uint8_t* p, size_t n, uint32_t c = 0xffffffffu) {
+  static uint32_t table[256];
+  static bool ready = false;
+  if (!ready) {
+    for (uint32_t i = 0; i < 256; ++i) {
+      uint32_t v = i;
+      for (int k = 0; k < 8; ++k) v = (v & 1u) ? 0xedb88320u ^ (v >> 1) : v >> 1;
+      table[i] = v;
+    }
+    ready = true;
+  }
+  for (size_t i = 0; i < n; ++i) c = table[(c ^ p[i]) & 0xffu] ^ (c >> 8);
+  return c;
+}
+
+void put_be32(std::vector<uint8_t>& out, uint32_t v) {
+  for (int s = 24; s >= 0; s -= 8) out.push_back(static_cast<uint8_t>(v >> s));
+}
+
+void put_chunk(std::vector<uint8_t>& out, const char* type, const std::vector<uint8_t>& data) {
+  put_be32(out, static_cast<uint32_t>(data.size()));
+  const size_t at = out.size();
+  out.insert(out.end(), type, type + 4);
+  out.insert(out.end(), data.begin(), data.end());
+  put_be32(out, png_crc(out.data() + at, out.size() - at) ^ 0xffffffffu);
+}
+}  // namespace
+
+int ho_save_png(const uint8_t* rgb, int W, int H, const char* path) {
+  if (!rgb || !path || W <= 0 || H <= 0) return HO_ERR_ARG;
+  const size_t row = static_cast<size_t>(W) * 3;
+  if (row + 1 > 0x7fffffffu / static_cast<size_t>(H)) return HO_ERR_RANGE;
+  // raw scanlines: filter byte 0, then the row
+  std::vector<uint8_t> raw;
+  raw.reserve((row + 1) * H);
+  for (int y = 0; y < H; ++y) {
+    raw.push_back(0);
+    raw.insert(raw.end(), rgb + y * row, rgb + (y + 1) * row);
+  }
+  std::vector<uint8_t> z;
+  z.reserve(raw.size() + raw.size() / 65535 * 5 + 16);
+  z.push_back(0x78);  // deflate, 32 KB window
+  z.push_back(0x01);  // no dictionary, fastest; (0x78 << 8 | 0x01) % 31 == 0
+  uint32_t a = 1, b = 0;  // Adler-32
+  for (size_t at = 0; at < raw.size() || at == 0;) {
+    const size_t n = std::min<size_t>(65535, raw.size() - at);
+    const bool last = at + n == raw.size();
+    z.push_back(last ? 1 : 0);  // BFINAL, BTYPE 00 (stored)
+    z.push_back(static_cast<uint8_t>(n));
+    z.push_back(static_cast<uint8_t>(n >> 8));
+    z.push_back(static_cast<uint8_t>(~n));
+    z.push_back(static_cast<uint8_t>(~n >> 8));
+    z.insert(z.end(), raw.begin() + at, raw.begin() + at + n);
+    for (size_t i = at; i < at + n; ++i) {
+      a = (a + raw[i]) % 65521u;
+      b = (b + a) % 65521u;
+    }
+    at += n;
+    if (last) break;
+  }
+  put_be32(z, b << 16 | a);
+  std::vector<uint8_t> out = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
+  std::vector<uint8_t> ihdr;
+  put_be32(ihdr, static_cast<uint32_t>(W));
+  put_be32(ihdr, static_cast<uint32_t>(H));
+  ihdr.insert(ihdr.end(), {8, 2, 0, 0, 0});  // 8 bits, RGB, deflate, filter set 0, no interlace
+  put_chunk(out, "IHDR", ihdr);
+  put_chunk(out, "IDAT", z);
+  put_chunk(out, "IEND", {});
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return HO_ERR_IO;
+  const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
+  return (std::fclose(f) == 0 && ok) ? HO_OK : HO_ERR_IO;
+}
+
 }  // extern "C"

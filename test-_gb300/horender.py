@@ -112,6 +112,7 @@ def _load():
     L.ho_autotune.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, C.POINTER(C.c_int64), vp, vp]
     L.ho_get_stats.argtypes = [vp, C.POINTER(_Stats)]
     L.ho_save_ppm.argtypes = [vp, i32, i32, C.c_char_p]
+    L.ho_save_png.argtypes = [vp, i32, i32, C.c_char_p]
     L.ho_measure_fp32_peak.argtypes = [i32, C.POINTER(C.c_double)]
     L.ho_intersect_device_noalloc.argtypes = [vp, i64, vp, f32, i32, vp, vp]
     L.ho_mlp_init.argtypes = [vp, C.c_uint64]
@@ -523,6 +524,14 @@ def save_ppm(rgb: np.ndarray, path: str):
     rgb = np.ascontiguousarray(rgb, np.uint8)
     h, w = rgb.shape[:2]
     rc = lib.ho_save_ppm(_p(rgb), w, h, str(path).encode())
+    if rc != HO_OK:
+        raise HoError(rc, f"cannot write {path}")
+
+
+def save_png(rgb: np.ndarray, path: str):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    h, w = rgb.shape[:2]
+    rc = lib.ho_save_png(_p(rgb), w, h, str(path).encode())
     if rc != HO_OK:
         raise HoError(rc, f"cannot write {path}")
 

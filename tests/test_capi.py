@@ -100,6 +100,42 @@ def test_save_ppm(tmp_path):
         hr.save_ppm(rgb, str(tmp_path / "no" / "such" / "dir.ppm"))
 
 
+def read_png(path):
+    """Chunks checked (CRC-32), IDAT inflated by zlib, filter bytes 0."""
+    import struct
+    import zlib
+
+    data = path.read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    at, chunks = 8, []
+    while at < len(data):
+        (n,) = struct.unpack(">I", data[at:at + 4])
+        kind, body = data[at + 4:at + 8], data[at + 8:at + 8 + n]
+        (crc,) = struct.unpack(">I", data[at + 8 + n:at + 12 + n])
+        assert crc == zlib.crc32(kind + body)
+        chunks.append((kind, body))
+        at += 12 + n
+    assert [k for k, _ in chunks] == [b"IHDR", b"IDAT", b"IEND"]
+    w, h, depth, ctype, comp, filt, lace = struct.unpack(">IIBBBBB", chunks[0][1])
+    assert (depth, ctype, comp, filt, lace) == (8, 2, 0, 0, 0)
+    raw = np.frombuffer(zlib.decompress(chunks[1][1]), np.uint8).reshape(h, 1 + 3 * w)
+    assert (raw[:, 0] == 0).all()
+    return raw[:, 1:].reshape(h, w, 3)
+
+
+@pytest.mark.parametrize("shape", [(4, 3), (1, 1), (200, 151)])
+def test_save_png(tmp_path, shape):
+    """The PNG holds the same pixels as the PPM, in the same row order; the
+    200 x 151 image spans two stored deflate blocks."""
+    h, w = shape
+    rgb = np.random.default_rng(h * w).integers(0, 256, (h, w, 3), dtype=np.uint8)
+    p = tmp_path / "a.png"
+    hr.save_png(rgb, str(p))
+    assert np.array_equal(read_png(p), rgb)
+    with pytest.raises(hr.HoError):
+        hr.save_png(rgb, str(tmp_path / "no" / "such" / "dir.png"))
+
+
 def test_engine_options():
     with hr.Context(0) as ctx:
         assert ctx.get_option(hr.OPT_GRAPH) == 1
