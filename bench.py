@@ -120,6 +120,12 @@ def flops_field(n):  # u and grad: (2n^3 + 3n^2 + 4n) FMA + basis (3 x 8n)
 ISECT_TRAFFIC = {
     ("hex32_p6", 1920, 1080, "learned"): (424.06e6 + 26.06e6) / 4,
 }
+# The same for the primitive pass (prim_trace_kernel), per launch, averaged
+# over 5 launches (profiles/launches_prims_sheet.md). Nearly all of it is the
+# write-back of the threads' spilled stack frames, not algorithmic traffic.
+PRIM_TRAFFIC = {
+    ("prims_sheet", 1920, 1080): 176.53e6 + 4569.10e6,
+}
 
 
 def algorithmic_flops(st, n):
@@ -589,7 +595,8 @@ def run_prims(args, rank, world):
                    "queries_per_step": nq, "l2": "flushed (256 MiB write) before every timed step",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": (achieved / fp32_peak) if fp32_peak else None, "traffic": None,
+                     "frac": (achieved / fp32_peak) if fp32_peak else None,
+                     "traffic": PRIM_TRAFFIC.get((args.workload, W, H)),
                      "peak_source": "FP32 FMA loop measured in this run (peaks file has HBM and bf16 only)",
                      "kernel": "prim_trace_kernel", "flops_per_launch": flops, "launches": args.steps,
                      "ms_per_launch": kernel_s * 1e3, "share_of_step": kernel_s * args.steps / total_s},
