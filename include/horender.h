@@ -426,6 +426,11 @@ int ho_train_mlp(ho_context* ctx, int64_t n_samples, int steps, int batch, float
 /* Checkpoint: FP32 master parameters + their BF16 copy. */
 int ho_mlp_save(ho_context* ctx, const char* path);
 int ho_mlp_load(ho_context* ctx, const char* path);
+/* Counters of the last trace call. After a *_device call on a caller's stream
+ * it waits for that call's work on that stream first (an event recorded at
+ * the end of the call); a call enqueued while its stream was being captured
+ * records no event, and its counters appear once the graph has run and a
+ * later call or read finds them. */
 int ho_get_stats(ho_context* ctx, ho_stats* out);
 
 /* FP32 FMA throughput of the device in TFLOP/s (register-resident FMA loop):
