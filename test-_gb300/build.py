@@ -19,6 +19,8 @@ ROOT = HERE.parent
 CSRC = HERE / "csrc"
 OBJ = HERE / "_build"
 LIB = HERE / "libhorender.so"
+CLI_SRC = HERE / "cli" / "horender_cli.cpp"
+CLI = HERE / "horender_cli"
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", str(ROOT / "include"),
@@ -74,6 +76,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}")
+    # the command-line renderer, linked against the library beside it
+    if force or _stale(CLI, [CLI_SRC, LIB, ROOT / "include" / "horender.hpp", ROOT / "include" / "horender.h"]):
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(CLI_SRC),
+               "-L", str(HERE), "-lhorender", "-Wl,-rpath,$ORIGIN", "-o", str(CLI)]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed:\n{r.stdout}")
     return LIB
 
 
