@@ -35,8 +35,10 @@ extern "C" {
  * is mapped to the GPU and where Newton starts. */
 #define HO_MODE_PLAIN 0      /* one thread per ray, sequential cold-start Newton (the reference's structure) */
 #define HO_MODE_LEARNED 1    /* BATCHED + network-predicted Newton starts; plain cold start as fallback     */
-#define HO_MODE_BATCHED 2    /* default: miss-culling pass + device queue + persistent warp per ray, the
-                                independent Newton solves of a candidate spread over the lanes               */
+#define HO_MODE_BATCHED 2    /* default: miss-culling pass + device queue, then element-major rounds: each
+                                round's (ray, element) pairs are bucketed by element and one warp per
+                                element batch runs every Newton solve of its pairs from a task queue; a
+                                warp per ray finishes the last rays; FP64 residual check + plain fallback */
 
 /* Hit kinds. */
 #define HO_HIT_MISS 0
@@ -50,6 +52,8 @@ extern "C" {
 #define HO_FLAG_FALLBACK 1u      /* learned guess rejected, plain solver answered   */
 #define HO_FLAG_FP64_FAIL 2u     /* FP64 residual check above tolerance             */
 #define HO_FLAG_OVERFLOW 4u      /* candidate list restarted (more than K boxes)     */
+#define HO_FLAG_INCOMPLETE 8u    /* the tree walk met its stack limit: candidates may
+                                    be missing from this ray's answer                */
 
 typedef struct ho_context ho_context;
 
@@ -294,7 +298,16 @@ int ho_intersect_device(ho_context* ctx, int64_t n, const float* rays_dev, float
  * HO_NOALLOC_MAX_RAYS rays per call; larger n fails with HO_ERR_RANGE. Needs ho_build_bvh first; the
  * caller owns rays_dev (n*6 floats) and out_dev (n hits). The first call on a
  * device looks the array's address up; make it before any stream capture.
- * All calls share the array: calls whose GPU work overlaps race. */
+ * All calls share the array: calls whose GPU work overlaps race.
+ * What it runs differs from ho_intersect_device: the miss-culling pass, then
+ * the warp-per-ray batched kernel with cold-start Newton whatever the
+ * ho_set_mode choice, then the primitive pass. It has no FP64 residual check,
+ * no plain-solver fallback and no tail, so its hits meet the FP32 solvers'
+ * own stopping rules (|u - iso| < 1e-5 at an isosurface root, face residual
+ * < 1e-4) without FP64 confirmation; on the test scenes they equal
+ * ho_intersect_device's on at least 99.9% of rays. ho_get_stats does not
+ * report this call (its counters sit in the fixed array); a ray whose tree
+ * walk met the stack limit carries HO_FLAG_INCOMPLETE in its hit. */
 #define HO_NOALLOC_MAX_RAYS 32768
 int ho_intersect_device_noalloc(ho_context* ctx, int64_t n, const float* rays_dev, float iso, int iso_enabled,
                                 ho_hit* out_dev, void* stream);

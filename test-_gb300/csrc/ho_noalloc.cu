@@ -25,6 +25,17 @@
 // the counters are cleared at the start of every call, and calls whose GPU
 // work overlaps (two streams, or two host threads) race on the array and
 // corrupt each other's results — serialise them.
+//
+// What it runs: the miss-culling classify pass, then the warp-per-ray
+// intersection kernel (isect_kernel) in batched form with cold-start Newton,
+// whatever ho_set_mode chose; then the primitive pass when the scene has
+// prisms, quads or triangles. It skips the round engine's FP64 residual check
+// and plain-solver fallback (their ray lists would need more scratch), so its
+// hits carry the FP32 solvers' own stopping rules (|u - iso| < 1e-5 at an
+// isosurface root, face residual < 1e-4) without the FP64 confirmation.
+// Its counters live in the scratch array, so ho_get_stats does not report
+// this call; a ray whose tree walk met the stack limit is flagged
+// HO_FLAG_INCOMPLETE in its own hit.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -97,6 +108,9 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
     c->err = std::string("scratch set-up: ") + cudaGetErrorString(e);
     return HO_ERR_CUDA;
   }
+  // an empty call touches nothing on the device, so it cannot clear the
+  // counters under another call still in flight
+  if (n == 0) return HO_OK;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
   // the counters and work totals must start at zero; the lists are written
   // before they are read
@@ -105,7 +119,6 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
     c->err = std::string("cudaMemsetAsync: ") + cudaGetErrorString(e);
     return HO_ERR_CUDA;
   }
-  if (n == 0) return HO_OK;
   TraceParams P;
   P.nodes = c->d_nodes;
   P.rec = c->d_rec;

@@ -103,12 +103,14 @@ __device__ __forceinline__ void prim_query(const PrimParams& P, int64_t q, PrimW
   const uint32_t iters0 = pw.iters;
   float kt = -FLT_MAX;
   int ke = -1;
+  bool incomplete = false;
   for (;;) {
     float bt[kPrimCandK];
     int be[kPrimCandK];
     bool overflow;
     if (!collect_in<kPrimCandK>(P.nodes, o, d, best, kt, ke, bt, be, overflow, w)) {
       atomicOr(&P.stats->status, kStatusStackOverflow);
+      incomplete = true;
       break;
     }
     bool done = false;
@@ -158,7 +160,8 @@ __device__ __forceinline__ void prim_query(const PrimParams& P, int64_t q, PrimW
     h.flags = 0;
   }
   h.iters += pw.iters - iters0;
-  if (P.hits && (P.fresh || win >= 0)) P.hits[q] = h;
+  if (incomplete) h.flags |= HO_FLAG_INCOMPLETE;
+  if (P.hits && (P.fresh || win >= 0 || incomplete)) P.hits[q] = h;
   if (P.rgb && P.rays == nullptr && (P.fresh || win >= 0)) {
     HitState s;
     s.t = h.t;

@@ -60,6 +60,7 @@ __global__ void round_gather_kernel(TraceParams P, RayState* __restrict__ st, Ro
       bool overflow;
       if (!collect(P, o, d, r.best.t, r.kt, r.ke, bt, be, overflow, w)) {
         atomicOr(&P.stats->status, kStatusStackOverflow);
+        r.best.flags |= HO_FLAG_INCOMPLETE;
         r.done = 1;
         break;
       }

@@ -1083,6 +1083,7 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
       // the list was cut at kCandK: walk the tree again after the last visited key
       if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, wu)) {
         if (lane == 0) atomicOr(&P.stats->status, kStatusStackOverflow);
+        best.flags |= HO_FLAG_INCOMPLETE;
         break;
       }
       first = 0;

@@ -15,7 +15,7 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
   const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   Work w;
-  bool need = false, overflow = false;
+  bool need = false, overflow = false, incomplete = false;
   float bt[kCandK];
   int be[kCandK];
   float3 o = make_float3(0.f, 0.f, 0.f), d = make_float3(0.f, 0.f, 1.f);
@@ -28,9 +28,14 @@ __global__ void __launch_bounds__(256) classify_kernel(TraceParams P, int64_t n_
     if (!collect(P, o, d, FLT_MAX, -FLT_MAX, -1, bt, be, overflow, w)) {
       atomicOr(&P.stats->status, kStatusStackOverflow);
       be[0] = INT_MAX;
+      incomplete = true;
     }
     need = be[0] != INT_MAX;
-    if (!need) write_result(P, q, d, miss_state(), 0);
+    if (!need) {
+      HitState m = miss_state();
+      if (incomplete) m.flags |= HO_FLAG_INCOMPLETE;
+      write_result(P, q, d, m, 0);
+    }
   }
   const unsigned m = __ballot_sync(kFull, need);
   if (m) {

@@ -16,6 +16,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "ho_device.cuh"
 #include "ho_host.h"
 #include "ho_learn.h"
@@ -27,6 +29,7 @@ constexpr int kCandK = 8;
 constexpr int64_t kPredItemsCap = int64_t(8) << 20;
 constexpr int kStack = 64;
 constexpr int kTraceBlock = 128;  // intersect pass: 4 warps, one query each
+constexpr int kGridCacheDevices = 64;  // devices whose persistent grid size launch_n caches
 
 
 
@@ -327,6 +330,7 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
       wu.cyc[0] += clock64() - c0;
       if (!walked) {
         if (lane == 0) atomicOr(&P.stats->status, kStatusStackOverflow);
+        best.flags |= HO_FLAG_INCOMPLETE;
         break;
       }
       bool done = false;
@@ -407,6 +411,7 @@ __device__ HitState plain_trace(const TraceParams& P, float3 o, float3 d, float 
     bool overflow;
     if (!collect(P, o, d, best.t, kt, ke, bt, be, overflow, w)) {
       atomicOr(&P.stats->status, kStatusStackOverflow);
+      best.flags |= HO_FLAG_INCOMPLETE;
       break;
     }
     bool done = false;
@@ -486,12 +491,17 @@ cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads,
     return cudaGetLastError();
   }
   const bool learned = mode == HO_MODE_LEARNED;
-  static int grid[2] = {0, 0};  // persistent grid: resident blocks per SM x SMs
-  int& g = grid[learned ? 1 : 0];
+  // persistent grid (resident blocks per SM x SMs), per device and form; two
+  // host threads that fill the same entry at once store the same value
+  static std::atomic<int> grid[kGridCacheDevices][2];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kGridCacheDevices) return cudaErrorInvalidDevice;
+  int g = grid[dev][learned ? 1 : 0].load(std::memory_order_relaxed);
   if (g == 0) {
     const int smem_i = static_cast<int>((kTraceBlock / 32) * record_floats(N) * sizeof(float));
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
+    int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (learned) {
       cudaFuncSetAttribute(isect_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_i);
@@ -501,6 +511,7 @@ cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads,
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, false>, kTraceBlock, smem_i);
     }
     g = sms * (per > 0 ? per : 1);
+    grid[dev][learned ? 1 : 0].store(g, std::memory_order_relaxed);
   }
   const size_t smem = static_cast<size_t>(kTraceBlock / 32) * record_floats(N) * sizeof(float);
   if (learned) isect_kernel<N, true><<<g, kTraceBlock, smem, s>>>(P);

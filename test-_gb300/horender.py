@@ -11,10 +11,12 @@ module raises.
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass, field
 from pathlib import Path
 
 import numpy as np
+
+from workloads import (ISO_POOL, MULTIVIEW, PATHS, RESOLUTIONS, WORKLOADS, Camera, Workload,  # noqa: F401
+                       sphere_views)
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "libhorender.so"
@@ -29,7 +31,7 @@ MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
 HIT_PRISM, HIT_QUAD, HIT_TRI = 3, 4, 5
-FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW = 1, 2, 4
+FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW, FLAG_INCOMPLETE = 1, 2, 4, 8
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("elem", "<i4"), ("face", "<i2"), ("kind", "<i2"), ("xi", "<f4", 3),
                       ("n", "<f4", 3), ("u", "<f4"), ("flags", "<u4"), ("iters", "<u4")])
@@ -134,53 +136,16 @@ def _p(a: np.ndarray) -> int:
     return a.ctypes.data
 
 
-@dataclass
-class Camera:
-    """Pinhole camera (FEM-AABB/raytracer.h:31-48 with aperture 0)."""
-    lookfrom: tuple
-    lookat: tuple
-    vup: tuple = (0.0, 1.0, 0.0)
-    vfov_deg: float = 60.0
-    focus_dist: float = 0.0
-
-    def _c(self) -> _Camera:
-        c = _Camera()
-        c.lookfrom[:] = [float(x) for x in self.lookfrom]
-        c.lookat[:] = [float(x) for x in self.lookat]
-        c.vup[:] = [float(x) for x in self.vup]
-        c.vfov_deg = float(self.vfov_deg)
-        c.focus_dist = float(self.focus_dist)
-        return c
+def _cam(cam: Camera) -> _Camera:
+    c = _Camera()
+    c.lookfrom[:] = [float(x) for x in cam.lookfrom]
+    c.lookat[:] = [float(x) for x in cam.lookat]
+    c.vup[:] = [float(x) for x in cam.vup]
+    c.vfov_deg = float(cam.vfov_deg)
+    c.focus_dist = float(cam.focus_dist)
+    return c
 
 
-@dataclass
-class Workload:
-    """A named synthetic workload: scene + view + isovalues."""
-    name: str
-    nx: int
-    order_min: int
-    order_max: int
-    curve_amp: float
-    n_gauss: int
-    seed: int
-    width: int
-    height: int
-    isovalues: list = field(default_factory=list)
-    camera: Camera = field(default_factory=lambda: Camera((2.5, 2.0, 1.8), (0.5, 0.5, 0.5), (0, 1, 0), 60.0))
-
-    def synth(self) -> dict:
-        return dict(nx=self.nx, ny=self.nx, nz=self.nx, order_min=self.order_min, order_max=self.order_max,
-                    curve_amp=self.curve_amp, n_gauss=self.n_gauss, seed=self.seed)
-
-
-# Benchmark workloads (seeded synthetic stand-ins for the reference's meshes).
-WORKLOADS = {
-    "hex4_p4": Workload("hex4_p4", 4, 4, 4, 0.05, 8, 1, 256, 256, [0.2]),
-    "hex32_p6": Workload("hex32_p6", 32, 6, 6, 0.08, 64, 2, 1920, 1080, [-0.3, 0.0, 0.3]),
-    "hex48_mixed": Workload("hex48_mixed", 48, 2, 8, 0.1, 64, 3, 1024, 1024, [-0.2, 0.1, 0.3]),
-    "hex64_p5": Workload("hex64_p5", 64, 5, 5, 0.12, 64, 4, 3840, 2160, [0.1]),
-    "hex96_mixed": Workload("hex96_mixed", 96, 3, 8, 0.1, 256, 5, 2048, 2048, [-0.4, 0.1, 0.6]),
-}
 
 
 class Context:
@@ -337,7 +302,7 @@ class Context:
         chunk = C.c_int64()
         cand = np.zeros(5, np.int64)
         ms = np.zeros(5, np.float32)
-        self._ck(lib.ho_autotune(self.h, C.byref(cam._c()), _p(iso), iso.size, int(width), int(height),
+        self._ck(lib.ho_autotune(self.h, C.byref(_cam(cam)), _p(iso), iso.size, int(width), int(height),
                                  int(bool(iso_zero_disables)), C.byref(chunk), _p(cand), _p(ms)))
         return {"chunk": chunk.value, "candidates": cand.tolist(), "ms": ms.tolist()}
 
@@ -357,7 +322,7 @@ class Context:
         else:
             rgb = np.zeros((n, height, width, 3), np.uint8) if want_rgb else None
         hits = np.zeros((n, height, width), HIT_DTYPE) if want_hits else None
-        cam = camera._c()
+        cam = _cam(camera)
         self._ck(lib.ho_render(self.h, C.byref(cam), _p(iso), n, width, height, int(iso_zero_disables),
                                _p(rgb) if rgb is not None else None, _p(hits) if hits is not None else None))
         return rgb, hits
@@ -365,7 +330,7 @@ class Context:
     @staticmethod
     def _views(cameras, widths, heights, isovalues):
         n = len(cameras)
-        cams = (_Camera * n)(*[c._c() for c in cameras])
+        cams = (_Camera * n)(*[_cam(c) for c in cameras])
         w = np.ascontiguousarray(widths, np.int32)
         h = np.ascontiguousarray(heights, np.int32)
         iso = np.zeros((n, 8), np.float32)
@@ -406,7 +371,7 @@ class Context:
     def render_device(self, camera: Camera, isovalues, width, height, rgb_ptr, hits_ptr, stream_ptr,
                       iso_zero_disables: bool = True):
         iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
-        cam = camera._c()
+        cam = _cam(camera)
         self._ck(lib.ho_render_device(self.h, C.byref(cam), _p(iso), iso.size, width, height,
                                       int(iso_zero_disables), rgb_ptr, hits_ptr, stream_ptr))
 
@@ -416,7 +381,7 @@ class Context:
         iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
         out = np.zeros((iso.size, height, width, 3), np.uint8)
         rays = C.c_int64(0)
-        cam = camera._c()
+        cam = _cam(camera)
         self._ck(lib.ho_path_trace(self.h, C.byref(cam), _p(iso), iso.size, width, height, int(spp), int(max_depth),
                                    int(seed), int(iso_zero_disables), _p(out), C.byref(rays)))
         return out, int(rays.value)
@@ -425,7 +390,7 @@ class Context:
                           seed=1, iso_zero_disables: bool = True) -> int:
         iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
         rays = C.c_int64(0)
-        cam = camera._c()
+        cam = _cam(camera)
         self._ck(lib.ho_path_trace_device(self.h, C.byref(cam), _p(iso), iso.size, width, height, int(spp),
                                           int(max_depth), int(seed), int(iso_zero_disables), rgb_ptr, C.byref(rays),
                                           stream_ptr))
@@ -534,40 +499,6 @@ def save_png(rgb: np.ndarray, path: str):
     rc = lib.ho_save_png(_p(rgb), w, h, str(path).encode())
     if rc != HO_OK:
         raise HoError(rc, f"cannot write {path}")
-
-
-RESOLUTIONS = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
-ISO_POOL = [-0.3, -0.2, -0.1, 0.0, 0.1, 0.2, 0.3]
-
-
-def sphere_views(n_views: int = 64, radius: float = 2.5, centre=(0.5, 0.5, 0.5), seed: int = 7,
-                 shrink: int = 1) -> tuple[list, list, list, list]:
-    """n seeded camera views on a Fibonacci sphere around the cube centre, each
-    with a resolution drawn from RESOLUTIONS (divided by `shrink`) and 1-4
-    distinct isovalues drawn from ISO_POOL. Returns cameras, widths, heights,
-    isovalue lists (the uneven multi-view workload)."""
-    rng = np.random.default_rng(seed)
-    golden = np.pi * (3.0 - np.sqrt(5.0))
-    cams, ws, hs, isos = [], [], [], []
-    for i in range(n_views):
-        y = 1.0 - 2.0 * (i + 0.5) / n_views
-        r = np.sqrt(max(0.0, 1.0 - y * y))
-        phi = golden * i
-        pos = tuple(float(c + radius * v) for c, v in zip(centre, (r * np.cos(phi), y, r * np.sin(phi))))
-        vup = (0.0, 0.0, 1.0) if abs(y) > 0.99 else (0.0, 1.0, 0.0)
-        cams.append(Camera(pos, tuple(centre), vup, 60.0))
-        wdt, hgt = RESOLUTIONS[int(rng.integers(len(RESOLUTIONS)))]
-        ws.append(max(1, wdt // shrink))
-        hs.append(max(1, hgt // shrink))
-        k = int(rng.integers(1, 5))
-        isos.append(sorted(float(v) for v in rng.choice(ISO_POOL, size=k, replace=False)))
-    return cams, ws, hs, isos
-
-
-# multi-view workloads: scene workload + views
-MULTIVIEW = {"views64": ("hex48_mixed", dict(n_views=64, seed=7))}
-# Path-tracing workloads: scene, and the per-step sample pass (ho_path_trace).
-PATHS = {"path96": ("hex96_mixed", dict(spp=1, max_depth=4, seed=1))}
 
 
 def workload_context(name: str, device: int = 0, build: bool = True) -> tuple[Context, Workload]:

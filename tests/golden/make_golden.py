@@ -20,6 +20,7 @@ Fixtures (all outputs are the reference's, computed in FP32 by its code):
 from __future__ import annotations
 
 import hashlib
+import os
 import sys
 from pathlib import Path
 
@@ -33,7 +34,10 @@ sys.path.insert(0, str(ROOT / "test-_gb300"))
 import oracle_bind as ob  # noqa: E402
 import horender as hr  # noqa: E402
 
-REF_DIR = Path("/root/reference/FEM-AABB")
+# The reference checkout is named by HORENDER_REFERENCE (its project root);
+# the fixtures that need the reference's own files are skipped without it.
+_REF_ROOT = os.environ.get("HORENDER_REFERENCE")
+REF_DIR = Path(_REF_ROOT) / "FEM-AABB" if _REF_ROOT else None
 ORDER_CAP = 32
 
 
@@ -68,6 +72,8 @@ def scene_payload(arrs: ob.SceneArrays, prefix="scene_"):
 
 
 def make_curvedface():
+    if REF_DIR is None:
+        sys.exit("set HORENDER_REFERENCE to the reference checkout to remake the curved-face fixture")
     rs = ob.RefScene(xml=str(REF_DIR / "Hex_CurvedFace.xml"), fld=str(REF_DIR / "Hex_CurvedFace.fld"))
     arrs = rs.arrays()
     rng = np.random.default_rng(101)

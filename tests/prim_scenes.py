@@ -20,6 +20,23 @@ def mixed_scene(seed=0, n_side=4, curved=True) -> ob.PrimArrays:
     return as_arrays(_mixed(seed, n_side, curved))
 
 
+def shifted(arrs: ob.PrimArrays, dx: float) -> ob.PrimArrays:
+    """The primitives moved by dx along x, curved geometry included: the x
+    block holds the modal expansion of x, and a constant shift is carried by
+    the vertex modes, whose values sum to 1 everywhere."""
+    out = ob.PrimArrays(arrs.kind, arrs.verts + np.array([dx, 0, 0], np.float32), arrs.geom_modes,
+                        arrs.geom_offset, arrs.geom.copy(), arrs.field_modes, arrs.field_offset, arrs.field)
+    for p in range(arrs.n):
+        if arrs.geom_offset[p] >= 0:
+            blk = block_size(int(arrs.kind[p]), [int(v) for v in arrs.geom_modes[p]])
+            o = int(arrs.geom_offset[p])
+            B = basis_matrix(int(arrs.kind[p]), [int(v) for v in arrs.geom_modes[p]],
+                             np.random.default_rng(0).uniform(-1, 1, (200, 3)))
+            one, *_ = np.linalg.lstsq(B, np.ones(200), rcond=None)
+            out.geom[o:o + blk] = (arrs.geom[o:o + blk] + dx * one).astype(np.float32)
+    return out
+
+
 def rays_at_boxes(arrs: ob.PrimArrays, boxes: np.ndarray, n_per: int, rng):
     """Per primitive n_per rays from outside its box towards random points in
     it, with segments [0.001, tmax] (tmax infinite for half of them, else

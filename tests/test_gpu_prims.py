@@ -110,18 +110,7 @@ def test_hexahedra_then_primitives(oracle):
     x in [1.1, 2.1]: the merged answer is the oracle's primitive pass started
     from the product's hexahedron hits."""
     arrs, _ = golden_arrays()
-    shifted = ob.PrimArrays(arrs.kind, arrs.verts + np.array([1.1, 0, 0], np.float32), arrs.geom_modes,
-                            arrs.geom_offset, arrs.geom.copy(), arrs.field_modes, arrs.field_offset, arrs.field)
-    for p in range(arrs.n):  # shift curved geometry too: the x block
-        if arrs.geom_offset[p] >= 0:
-            blk = ps.block_size(int(arrs.kind[p]), [int(v) for v in arrs.geom_modes[p]])
-            o = int(arrs.geom_offset[p])
-            # the x block holds the modal expansion of x; the constant shift
-            # is carried by the vertex modes, whose values sum to 1 everywhere
-            B = ps.basis_matrix(int(arrs.kind[p]), [int(v) for v in arrs.geom_modes[p]],
-                                np.random.default_rng(0).uniform(-1, 1, (200, 3)))
-            one, *_ = np.linalg.lstsq(B, np.ones(200), rcond=None)
-            shifted.geom[o:o + blk] = (arrs.geom[o:o + blk] + 1.1 * one).astype(np.float32)
+    shifted = ps.shifted(arrs, 1.1)
     hexes, w = hr.workload_context("hex4_p4")
     both = hr.Context(0)
     h_arrays = hexes.get_scene()

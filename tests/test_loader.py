@@ -13,6 +13,7 @@ the arrays the reference's own loader made of them. Criteria:
 from __future__ import annotations
 
 import base64
+import os
 import zlib
 from pathlib import Path
 
@@ -24,7 +25,9 @@ from conftest import GOLDEN, scene_arrays_from_ctx
 
 NEK = GOLDEN / "nektar"
 CASES = ["nek_faces", "nek_verts", "nek_raw", "nek_fp32"]
-REF_SAMPLE = Path("/root/reference/FEM-AABB/Hex_CurvedFace.xml")
+# the reference's own sample mesh, read from the checkout HORENDER_REFERENCE names (skipped without it)
+_REF_ROOT = os.environ.get("HORENDER_REFERENCE")
+REF_SAMPLE = Path(_REF_ROOT) / "FEM-AABB" / "Hex_CurvedFace.xml" if _REF_ROOT else None
 
 
 def load(name, fld=None):
@@ -147,7 +150,7 @@ def test_load_appends_to_scene():
     assert s["field_offsets"].tolist() == [0, 216, 432, 459, 486]
 
 
-@pytest.mark.skipif(not REF_SAMPLE.exists(), reason="reference sample mesh not present")
+@pytest.mark.skipif(REF_SAMPLE is None or not REF_SAMPLE.exists(), reason="reference sample mesh not present")
 def test_reference_sample_mesh():
     """The reference's own curved-face sample against the arrays its loader made."""
     g = np.load(GOLDEN / "curvedface.npz")
