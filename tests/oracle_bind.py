@@ -54,6 +54,11 @@ class _PrimsDesc(C.Structure):
     ]
 
 
+class _SynthParams(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("order_min", C.c_int32),
+                ("order_max", C.c_int32), ("curve_amp", C.c_double), ("n_gauss", C.c_int32), ("seed", C.c_uint64)]
+
+
 class _Counters(C.Structure):
     _fields_ = [("newton_iters", C.c_uint64), ("face_iters", C.c_uint64),
                 ("newton_solves", C.c_uint64), ("candidates", C.c_uint64)]
@@ -96,6 +101,9 @@ def lib():
         L.hor_prims_intersect.argtypes = [vp, i32, i32, vp, i64, vp, vp]
         L.hor_prims_map.argtypes = [vp, i32, i32, vp, i64, vp]
         L.hor_prims_trace.argtypes = [vp, i32, vp, i64, vp, i32]
+        L.hor_synth_sizes.argtypes = [C.POINTER(_SynthParams), vp, vp, vp]
+        L.hor_synth_fill.argtypes = [C.POINTER(_SynthParams), i32, vp, vp, vp, vp, vp, vp, vp]
+        L.hor_polish.argtypes = [vp, vp, i64, f32, vp, i32]
         _lib = L
     return _lib
 
@@ -139,6 +147,29 @@ class SceneArrays:
                            z["field"], z["verts"])
 
 
+def synth_scene(nx, ny, nz, order_min, order_max, curve_amp, n_gauss, seed, threads: int = 0) -> SceneArrays:
+    """The seeded synthetic scene that ho_generate_synthetic describes, built
+    by the oracle's own generator (oracle/horender_synth.cpp): no product
+    library is loaded."""
+    prm = _SynthParams(int(nx), int(ny), int(nz), int(order_min), int(order_max), float(curve_amp), int(n_gauss),
+                       int(seed))
+    ne, gl, fl = C.c_int64(), C.c_int64(), C.c_int64()
+    if lib().hor_synth_sizes(C.byref(prm), C.byref(ne), C.byref(gl), C.byref(fl)) != 0:
+        raise ValueError("invalid synthetic scene parameters")
+    n = ne.value
+    verts = np.zeros((n, 8, 3), np.float32)
+    gm = np.zeros((n, 3), np.uint32)
+    go = np.zeros(n, np.int64)
+    g = np.zeros(gl.value, np.float32)
+    fm = np.zeros((n, 3), np.uint32)
+    fo = np.zeros(n, np.int64)
+    f = np.zeros(fl.value, np.float32)
+    rc = lib().hor_synth_fill(C.byref(prm), int(threads), _p(verts), _p(gm), _p(go), _p(g), _p(fm), _p(fo), _p(f))
+    if rc != 0:
+        raise RuntimeError(f"hor_synth_fill failed ({rc})")
+    return SceneArrays(gm, go, g, fm, fo, f, verts)
+
+
 class OracleScene:
     def __init__(self, arrs: SceneArrays):
         self.arrs = arrs
@@ -166,6 +197,18 @@ class OracleScene:
         lib().hor_trace(self.h, precision, _p(rays), rays.shape[0], float(iso), int(iso_on), nt, _p(out),
                         C.byref(cnt))
         return out, {k: getattr(cnt, k) for k, _ in _Counters._fields_}
+
+    def polish(self, rays, hits, iso, threads=None):
+        """The judge's FP64 polish of given hits (HIT_DTYPE, oracle or product
+        hits converted): each hit's defining equations solved to convergence
+        from its own (t, xi). Returns a copy; pad = 1 where it converged."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = np.zeros(rays.shape[0], HIT_DTYPE)
+        for k in ("t", "elem", "face", "kind", "xi", "n", "u"):
+            out[k] = hits[k]
+        nt = threads or os.cpu_count() or 1
+        lib().hor_polish(self.h, _p(rays), rays.shape[0], float(iso), _p(out), nt)
+        return out
 
     def trace_replay(self, rays, iso, iso_on, order, order_n, precision=32):
         rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)

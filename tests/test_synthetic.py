@@ -84,3 +84,25 @@ def test_deterministic_and_order_range():
         assert np.array_equal(a[k], b[k]), k
     m = a["geom_modes"][:, 0]
     assert m.min() >= 3 and m.max() <= 9 and len(np.unique(m)) >= 5
+
+
+@pytest.mark.parametrize("synth", [dict(nx=3, ny=2, nz=4, order_min=2, order_max=8, curve_amp=0.1, n_gauss=16, seed=9),
+                                   hr.WORKLOADS["hex4_p4"].synth()])
+def test_oracle_generator_equals_library(oracle, synth):
+    """The oracle's own generator (oracle/horender_synth.cpp), which the
+    benchmark's CPU arm uses so that it loads no product library, makes the
+    library's scene: same layout, corners and coefficients (identical on a
+    host compiler that does not fuse multiply-adds; within FP32 rounding of
+    the FP64 fit otherwise)."""
+    a = ob.synth_scene(**synth)
+    ctx = hr.Context(0)
+    ctx.generate_synthetic(**synth)
+    s = ctx.get_scene()
+    ctx.close()
+    assert np.array_equal(a.geom_modes.reshape(-1), s["geom_modes"].reshape(-1))
+    assert np.array_equal(a.geom_offset, s["geom_offsets"]) and np.array_equal(a.field_offset, s["field_offsets"])
+    assert np.array_equal(a.verts.reshape(-1), s["corners"].reshape(-1))
+    for x, y in ((a.geom, s["geom"]), (a.field, s["field"])):
+        assert x.shape == y.shape
+        assert np.abs(x - y).max() <= 1e-6 * max(1.0, np.abs(y).max())
+        assert (x == y).mean() > 0.99
