@@ -1,21 +1,36 @@
 """Benchmark: Mrays/s of curved-hex ray/isosurface queries on one GB300.
 
-Workload (default): hex32_p6 — 32^3 = 32,768 hexes of [0,1]^3, P = 6
-geometry and field (7^3 modes per element), sinusoidal curving 0.08 h,
-seeded 64-Gaussian field; 1920x1080 pixel-centre primary rays from a pinhole
+Workload (default): hex64_p5 — 64^3 = 262,144 hexes of [0,1]^3, P = 5
+geometry and field (6^3 modes per element), sinusoidal curving 0.12 h,
+seeded 64-Gaussian field; 3840x2160 pixel-centre primary rays from a pinhole
 camera at (2.5, 2.0, 1.8) looking at (0.5, 0.5, 0.5), 60 deg vertical FOV;
-isovalues {-0.3, 0.0, 0.3} (0.0 traced as a real isovalue). One step = one
-render of all 3 isovalues = 6,220,800 ray queries; a ray query counts as
-completed whether it hits a face, the isosurface, or nothing.
+isovalue 0.1. One step = one render = 8,294,400 ray queries; a ray query
+counts as completed whether it hits a face, the isosurface, or nothing. The
+learned mode (network-predicted Newton starts + element-major batching) is
+the headline; the batched mode (same kernels, cold starts) and the plain mode
+(one thread per ray, the reference's per-ray structure) are timed beside it.
 
   value  : queries/s with the scene resident in HBM, CUDA events around the
-           trace launch on its own stream, L2 flushed (256 MiB write) before
+           trace call on its own stream, L2 flushed (256 MiB write) before
            every timed step, sum over K steps.
-  e2e    : the same through ho_render() with a host image buffer (device ->
-           host copy of the 8-bit images inside the timed region), host clock.
+  e2e    : the same through ho_render_tile() with a host image buffer (device
+           -> host copy of the 8-bit images inside the timed region; with
+           several ranks the gather on rank 0 too), host clock.
+  error_vs_fp64: per mode, a seeded sample of the workload's rays that meet
+           the scene box, traced by the GPU and by the FP64 oracle (TEST
+           INFRASTRUCTURE, used only as the judge): identity agreement, the
+           classes of the differences, and the t / xi / field errors of the
+           agreeing hits against the oracle's hits polished to exact roots.
   cpu_baseline / --impl reference: the oracle's FP32 port of the reference
            algorithm (same per-candidate steps, ordered candidates), all host
-           threads, on a bounded random sample of the workload's rays.
+           threads, on a bounded random sample of the workload's queries; the
+           scene comes from the oracle's own generator, so that arm loads no
+           product library.
+
+--gpus N (under torchrun): the image's rows (or, for a multi-view workload,
+whole views) are split across the ranks; every rank holds the whole scene
+and tree; rank 0 gathers the images on the host. Path tracing runs one
+replica per rank.
 
 Prints one JSON line (rank 0).
 """
@@ -45,10 +60,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hex32_p6")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample time")
+    ap.add_argument("--workload", default="hex64_p5")
+    ap.add_argument("--cpu-queries", type=int, default=65536,
+                    help="reference arm: CPU-port queries over its timed steps together (the GPU line's "
+                         "cpu_baseline entry takes at most 16,384)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-error-check", action="store_true", help="skip the error_vs_fp64 block")
+    ap.add_argument("--error-rays", type=int, default=4096, help="rays of the error_vs_fp64 sample")
     ap.add_argument("--tensor", type=int, default=0, choices=[0, 1],
                     help="1: tensor-core round kernel (orders up to 8), 0: FP32 CUDA-core round kernel")
     ap.add_argument("--mode", default="all", choices=["all", "plain", "batched", "learned"],
@@ -182,111 +201,249 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(workload, seconds, n_iso_sample=None):
-    """Time the oracle's FP32 port on a bounded random sample of rays."""
+# ---- workloads and the config both arms print --------------------------------
+def hex_workload(name):
+    """(scene workload, views or None, path-tracing settings or None) of a
+    hexahedral workload name. Pure Python: no library is loaded."""
+    import workloads as wl
+
+    if name in wl.MULTIVIEW:
+        base, kw = wl.MULTIVIEW[name]
+        return wl.WORKLOADS[base], wl.sphere_views(**kw), None
+    if name in wl.PATHS:
+        base, kw = wl.PATHS[name]
+        return wl.WORKLOADS[base], None, kw
+    return wl.WORKLOADS[name], None, None
+
+
+def queries_per_step(w, views):
+    if views:
+        cams, vw, vh, visos = views
+        return int(sum(a * b * len(c) for a, b, c in zip(vw, vh, visos)))
+    return w.width * w.height * len(w.isovalues)
+
+
+def split_name(name, world):
+    if world <= 1:
+        return "1 GPU"
+    import workloads as wl
+
+    if name in wl.PATHS:
+        return f"{world} GPUs: one replica of the path-traced view per rank"
+    what = "whole views" if name in wl.MULTIVIEW else "image rows"
+    return f"{world} GPUs: {what} split across ranks, scene and tree replicated, images gathered on rank 0"
+
+
+def workload_config(name, world):
+    """The workload description both arms print (identical dicts)."""
+    if name in PRIMS:
+        cfg = PRIMS[name]
+        return {"workload": name, "scene": f"prims_sheet generator (seed {cfg['seed']}, {cfg['n_side']} per side): "
+                                            "prisms on a floor of quads before a wall of triangles, half curved",
+                "rays": f"{cfg['width']}x{cfg['height']} pixel-centre primary rays",
+                "queries_per_step": cfg["width"] * cfg["height"],
+                "l2": "GPU arm: flushed (256 MiB write) before every timed step",
+                "parallelism": split_name(name, world)}
+    w, views, path_kw = hex_workload(name)
+    if views:
+        cams, vw, vh, visos = views
+        rays = (f"{len(cams)} views on a radius-2.5 sphere, resolutions {sorted(set(zip(vw, vh)))}, "
+                "1-4 isovalues each")
+    elif path_kw:
+        rays = (f"{w.width}x{w.height}, path tracing: {path_kw['spp']} jittered path(s) per pixel per step, up to "
+                f"{path_kw['max_depth']} intersections per path, Lambertian bounces")
+    else:
+        rays = f"{w.width}x{w.height} pixel-centre primary rays"
+    return {"workload": name, "mesh": f"{w.nx}^3 = {w.nx ** 3} hexes of [0,1]^3",
+            "order": w.order_max if w.order_min == w.order_max else f"P in {w.order_min}..{w.order_max}",
+            "curve_amp": w.curve_amp, "gaussians": w.n_gauss, "seed": w.seed, "rays": rays,
+            "isovalues": "per view" if views else w.isovalues,
+            "queries_per_step": None if path_kw else queries_per_step(w, views),
+            "l2": "GPU arm: flushed (256 MiB write) before every timed step",
+            "parallelism": split_name(name, world)}
+
+
+def scaling_of(args):
+    """Rows or views of a fixed workload split over the ranks: strong; path
+    tracing runs one replica per rank: weak."""
+    import workloads as wl
+
+    return "weak" if args.workload in wl.PATHS else "strong"
+
+
+# ---- the CPU arm: FP32 oracle port on a bounded sample --------------------------
+CPU_BASELINE_QUERIES = 16384  # the GPU line's cpu_baseline entry (at most)
+
+
+def oracle_scene(w):
+    """The workload's scene built by the oracle's generator (no product library)."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_bind as ob
-    import horender as hr
 
-    ctx = hr.Context(0)
-    ctx.generate_synthetic(**workload.synth())
-    s = ctx.get_scene()
-    ctx.close()
-    arrs = ob.SceneArrays(s["geom_modes"], s["geom_offsets"], s["geom"], s["field_modes"], s["field_offsets"],
-                          s["field"], s["corners"])
-    osc = ob.OracleScene(arrs)
-    cam = workload.camera
-    rays = ob.camera_rays(cam.lookfrom, cam.lookat, cam.vup, cam.vfov_deg, workload.width, workload.height)
-    rng = np.random.default_rng(12345)
+    return ob, ob.OracleScene(ob.synth_scene(**w.synth()))
+
+
+def sample_queries(ob, w, views, n, rng, box_only=False):
+    """n queries drawn uniformly from the workload's queries (box_only: from
+    those whose ray meets the scene box [0,1]^3 widened by 0.05): rays
+    (n x 6), isovalue per query."""
+    if views:
+        cams, vw, vh, visos = views
+        sizes = np.array([a * b * len(c) for a, b, c in zip(vw, vh, visos)], np.int64)
+        first = np.concatenate([[0], np.cumsum(sizes)])
+        q = np.sort(rng.choice(int(first[-1]), size=n, replace=False))
+        view = np.searchsorted(first, q, side="right") - 1
+        rays = np.zeros((n, 6), np.float32)
+        isos = np.zeros(n, np.float32)
+        for v in np.unique(view):
+            m = view == v
+            local = q[m] - first[v]
+            npix = vw[v] * vh[v]
+            c = cams[v]
+            r = ob.camera_rays(c.lookfrom, c.lookat, c.vup, c.vfov_deg, vw[v], vh[v])
+            rays[m] = r[local % npix]
+            isos[m] = np.asarray(visos[v], np.float32)[local // npix]
+        return rays, isos
+    cam = w.camera
+    all_rays = ob.camera_rays(cam.lookfrom, cam.lookat, cam.vup, cam.vfov_deg, w.width, w.height)
+    npix = all_rays.shape[0]
+    pool = np.arange(npix)
+    if box_only:
+        o, d = all_rays[:, :3].astype(np.float64), all_rays[:, 3:].astype(np.float64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            t0, t1 = (-0.05 - o) / d, (1.05 - o) / d
+        pool = np.where(np.maximum(t0, t1).min(1) > np.minimum(t0, t1).max(1))[0]
+    n_iso = len(w.isovalues)
+    q = rng.choice(pool.size * n_iso, size=n, replace=False)
+    return all_rays[pool[q % pool.size]], np.asarray(w.isovalues, np.float32)[q // pool.size]
+
+
+def trace_sample(osc, rays, isos, threads, precision=32):
+    """Oracle trace of a query sample, grouped by isovalue (0.0 is traced as a
+    real isovalue, as the GPU arm does); returns the hits in sample order."""
+    out = None
+    for iso in np.unique(isos):
+        m = isos == iso
+        h, _ = osc.trace(rays[m], float(iso), True, precision=precision, threads=threads)
+        if out is None:
+            out = np.zeros(rays.shape[0], h.dtype)
+        out[m] = h
+    return out
+
+
+def cpu_sample_text(n, threads, dt, path_kw):
+    what = ("primary rays of the path-traced view (the port has no bounce layer)" if path_kw
+            else "queries (ray x isovalue) drawn uniformly from the workload's queries")
+    return (f"{n} {what}; scene from the oracle's own generator; FP32 oracle port of the reference algorithm, "
+            f"{threads} threads, {dt:.1f} s")
+
+
+def cpu_baseline(name, n_queries, seed=12345):
+    """The oracle's FP32 port timed on n_queries sampled queries, all host threads."""
+    w, views, path_kw = hex_workload(name)
+    ob, osc = oracle_scene(w)
+    rng = np.random.default_rng(seed)
+    rays, isos = sample_queries(ob, w, views, n_queries, rng)
     threads = os.cpu_count() or 1
-    n = 64
-    done_rays = 0
-    elapsed = 0.0
-    while True:
-        idx = rng.choice(rays.shape[0], size=n, replace=False)
-        sample = rays[idx]
-        t0 = time.perf_counter()
-        for iso in workload.isovalues:
-            osc.trace(sample, iso, True, precision=32, threads=threads)
-        dt = time.perf_counter() - t0
-        done_rays += n * len(workload.isovalues)
-        elapsed += dt
-        if elapsed >= seconds * 0.5 or n >= rays.shape[0]:
-            break
-        # grow the sample toward the time target
-        n = int(min(rays.shape[0], max(2 * n, n * (seconds - elapsed) / max(dt, 1e-3))))
-    return {"value": done_rays / elapsed / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{done_rays} ray queries ({len(workload.isovalues)} isovalues) drawn uniformly from the "
-                      f"{workload.width}x{workload.height} image, FP32 oracle port, {threads} threads, "
-                      f"{elapsed:.1f} s"}
+    t0 = time.perf_counter()
+    trace_sample(osc, rays, isos, threads)
+    dt = time.perf_counter() - t0
+    return {"value": n_queries / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": cpu_sample_text(n_queries, threads, dt, path_kw)}
 
 
 def run_reference(args, rank, world):
-    import horender as hr
-
-    if args.workload in PRIMS:
-        if rank != 0:
-            return
-        vals, cb = [], None
-        for i in range(args.warmup + args.steps):
-            cb = prims_cpu_baseline(args.workload, max(2.0, args.cpu_seconds / 2))
-            if i >= args.warmup:
-                vals.append(cb["value"])
-        v = float(np.mean(vals))
-        cfg = PRIMS[args.workload]
-        print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                          "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                          "config": {"workload": args.workload, "rays": f"{cfg['width']}x{cfg['height']} primary"},
-                          "cpu_baseline": dict(cb, value=v),
-                          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
-              flush=True)
-        return
-    if args.workload in hr.MULTIVIEW:
-        w = hr.WORKLOADS[hr.MULTIVIEW[args.workload][0]]
-    elif args.workload in hr.PATHS:
-        w = hr.WORKLOADS[hr.PATHS[args.workload][0]]
-    else:
-        w = hr.WORKLOADS[args.workload]
+    """The reference's algorithm on the host cores (the oracle's FP32 port;
+    the reference's own build needs its sources, which the GPU host does not
+    have). Rank 0 alone runs; the warm-up steps trace 256 queries each, the
+    timed steps --cpu-queries together. No product library is loaded."""
     if rank != 0:
         return
-    per_step = []
-    cb = None
-    for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(w, max(2.0, args.cpu_seconds / 2))
-        if i >= args.warmup:
-            per_step.append(cb["value"])
-    v = float(np.mean(per_step))
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": w.name, "mesh": f"{w.nx}^3 hexes", "order": w.order_max,
-                       "rays": f"{w.width}x{w.height}", "isovalues": w.isovalues},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
+    per = max(256, -(-args.cpu_queries // args.steps))
+    if args.workload in PRIMS:
+        vals, cb = [], None
+        for i in range(args.warmup + args.steps):
+            cb = prims_cpu_baseline(args.workload, 256 if i < args.warmup else per, seed=i)
+            if i >= args.warmup:
+                vals.append(cb["value"])
+        v = float(len(vals) / np.sum(1.0 / np.asarray(vals)))
+    else:
+        w, views, path_kw = hex_workload(args.workload)
+        ob, osc = oracle_scene(w)
+        rng = np.random.default_rng(12345)
+        threads = os.cpu_count() or 1
+        n_total, t_total = 0, 0.0
+        for i in range(args.warmup + args.steps):
+            n = 256 if i < args.warmup else per
+            rays, isos = sample_queries(ob, w, views, n, rng)
+            t0 = time.perf_counter()
+            trace_sample(osc, rays, isos, threads)
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                n_total += n
+                t_total += dt
+        v = n_total / t_total / 1e6
+        cb = {"cores": threads, "kind": "port", "sample": cpu_sample_text(n_total, threads, t_total, path_kw)}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": scaling_of(args),
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": workload_config(args.workload, world),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
                              "sample": cb["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def error_vs_fp64(ctx, hr, args, w, views, modes, codes):
+    """Per solver mode, args.error_rays queries (rays that meet the scene box)
+    traced by the GPU and by the FP64 oracle. Identity: agreement and the
+    classes of the differences (tests/parity.py). Errors of the agreeing hits
+    against the oracle's hits polished to the exact roots of their equations:
+    t and the isosurface position in units of the element size h, xi, u."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import parity
+
+    ob, osc = oracle_scene(w)
+    rng = np.random.default_rng(2024)
+    rays, isos = sample_queries(ob, w, views, args.error_rays, rng, box_only=True)
+    threads = os.cpu_count() or 1
+    h = 1.0 / w.nx
+    o64 = trace_sample(osc, rays, isos, threads, precision=64)
+    judge = np.zeros_like(o64)
+    for iso in np.unique(isos):
+        m = isos == iso
+        judge[m] = osc.polish(rays[m], o64[m], float(iso), threads=threads)
+    out = {"rays": int(rays.shape[0]), "h": h, "judge": "FP64 oracle (ordered candidates), hits polished to the exact "
+           "roots of their defining equations", "modes": {}}
+    for mode in modes:
+        ctx.set_mode(codes[mode])
+        g = np.zeros(rays.shape[0], hr.HIT_DTYPE)
+        for iso in np.unique(isos):
+            m = isos == iso
+            g[m] = ctx.intersect(rays[m], float(iso), True)
+        cls = {k: 0 for k in ("differ", "tie", "grazing", "unstable", "other")}
+        for iso in np.unique(isos):
+            m = np.where(isos == iso)[0]
+            c = parity.counts(parity.classify(g[m], o64[m], rays[m], osc, float(iso)))
+            for k in cls:
+                cls[k] += c[k]
+        errs = parity.errors(g, judge, rays, h)
+        out["modes"][mode] = {"identity_agree": float(parity.same_ids(g, o64).mean()), "identity_classes": cls,
+                              "errors": errs}
+    return out
 
 
 def run_gpu(args, rank, world):
     import torch
 
     import horender as hr
+    import shard
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    multi = args.workload in hr.MULTIVIEW
-    path = args.workload in hr.PATHS
-    if multi:  # many views of one scene in one call
-        base, view_kw = hr.MULTIVIEW[args.workload]
-        w = hr.WORKLOADS[base]
-        cams, vw, vh, visos = hr.sphere_views(**view_kw)
-    elif path:  # path tracing: one sample pass per step, every bounce through the engine
-        base, path_kw = hr.PATHS[args.workload]
-        w = hr.WORKLOADS[base]
-    else:
-        w = hr.WORKLOADS[args.workload]
+    w, views, path_kw = hex_workload(args.workload)
+    multi, path = views is not None, path_kw is not None
     if args.width and args.height:
         import dataclasses
 
@@ -298,21 +455,35 @@ def run_gpu(args, rank, world):
     info = ctx.info()
     n_iso = len(w.isovalues)
     W, H = w.width, w.height
-    nq = sum(a * b * len(c) for a, b, c in zip(vw, vh, visos)) if multi else W * H * n_iso
-    rgb = torch.empty(nq * 3, dtype=torch.uint8, device=dev)
+    # this rank's share: whole views, or a band of image rows (path tracing:
+    # every rank traces the whole image, replicas)
+    mine = []
+    if multi:
+        cams, vw, vh, visos = views
+        sizes = [a * b * len(c) for a, b, c in zip(vw, vh, visos)]
+        mine = shard.view_split(sizes, world)[rank]
+        my_views = ([cams[i] for i in mine], [vw[i] for i in mine], [vh[i] for i in mine], [visos[i] for i in mine])
+        nq = int(sum(sizes[i] for i in mine))
+        y0, rows = 0, H
+    else:
+        y0, rows = (0, H) if path else shard.row_band(H, world, rank)
+        nq = W * rows * n_iso
+    rgb = torch.empty(max(nq, 1) * 3, dtype=torch.uint8, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
 
     def step():
-        """One step; returns its ray queries."""
+        """One step of this rank's share; returns its ray queries."""
         if multi:
-            ctx.render_views_device(cams, vw, vh, visos, rgb.data_ptr(), None, sp)
+            if nq:
+                ctx.render_views_device(*my_views, rgb.data_ptr(), None, sp)
         elif path:
             return ctx.path_trace_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), sp, iso_zero_disables=False,
                                          **path_kw)
-        else:
-            ctx.render_device(w.camera, w.isovalues, W, H, rgb.data_ptr(), None, sp, iso_zero_disables=False)
+        elif rows:
+            ctx.render_tile_device(w.camera, w.isovalues, W, H, 0, y0, W, rows, rgb.data_ptr(), None, sp,
+                                   iso_zero_disables=False)
         return nq
 
     tuned = {}
@@ -408,8 +579,9 @@ def run_gpu(args, rank, world):
         kernel_name = "plain_kernel"
     achieved_tflops = flops / kernel_s / 1e12
 
-    # e2e: public API, host image buffer, D2H inside the timed region
-    host_rgb = torch.empty((nq, 3) if multi else (n_iso, H, W, 3), dtype=torch.uint8).pin_memory()
+    # e2e: public API, host image buffers, D2H inside the timed region; with
+    # several ranks the gather of the images on rank 0 is inside it too
+    host_rgb = torch.empty(max(nq, 1) * 3, dtype=torch.uint8).pin_memory()
     e2e_rays = 0
     torch.cuda.synchronize()
     barrier(world)
@@ -417,26 +589,30 @@ def run_gpu(args, rank, world):
     ctx.set_mode(codes[head])
     for _ in range(0 if args.no_e2e else args.steps):
         if multi:
-            ctx.render_views(cams, vw, vh, visos, rgb_out=host_rgb.numpy())
+            part = host_rgb.numpy()[: nq * 3]
+            if nq:
+                ctx.render_views(*my_views, rgb_out=part)
+            if world > 1:
+                shard.gather_views([part], [[r] for r in range(world)], world, rank)
         elif path:
             img, r = ctx.path_trace(w.camera, w.isovalues, W, H, iso_zero_disables=False, **path_kw)
-            host_rgb.numpy()[...] = img
+            host_rgb.numpy()[: img.size] = img.reshape(-1)
             e2e_rays += r
         else:
-            ctx.render(w.camera, w.isovalues, W, H, iso_zero_disables=False, rgb_out=host_rgb.numpy())
+            band = host_rgb.numpy()[: nq * 3].reshape(n_iso, rows, W, 3)
+            if rows:
+                ctx.render_tile(w.camera, w.isovalues, W, H, 0, y0, W, rows, iso_zero_disables=False, rgb_out=band)
+            if world > 1:
+                shard.gather_rows(band, H, world, rank)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    e2e = None if args.no_e2e else (e2e_rays if path else queries) / e2e_s / 1e6
+    e2e = None if args.no_e2e else sum_over_ranks(e2e_rays if path else nq * args.steps, world) / e2e_s / 1e6
     del host_rgb
 
-    peaks = {}
-    pk = ROOT / "MEASURED_PEAKS.json"
-    if pk.exists():
-        peaks = json.loads(pk.read_text())
     fp32_peak = fp32_peak_tflops(torch, dev)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "scaling": scaling_of(args), "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "impl": "gb300", "mode": {"learned": "learned-init + batched", "batched": "batched (cold-start Newton)",
                                   "plain": "plain (thread per ray, cold-start Newton)"}[head],
         "plain": mode_summary("plain"),
@@ -446,18 +622,10 @@ def run_gpu(args, rank, world):
         else None,
         "training": train,
         "autotune": tuned,
-        "config": {"workload": args.workload if (multi or path) else w.name, "mesh": f"{w.nx}^3 = {w.nx**3} hexes",
-                   "order": w.order_max if w.order_min == w.order_max else f"P in {w.order_min}..{w.order_max}",
-                   "modes_per_dir": N, "curve_amp": w.curve_amp, "gaussians": w.n_gauss,
-                   "rays": (f"{len(cams)} views on a radius-2.5 sphere, resolutions "
-                            f"{sorted(set(zip(vw, vh)))}, 1-4 isovalues each") if multi else
-                           (f"{W}x{H}, path tracing: {path_kw['spp']} jittered path(s) per pixel per step, up to "
-                            f"{path_kw['max_depth']} intersections per path, Lambertian bounces") if path else f"{W}x{H}",
-                   "isovalues": "per view" if multi else w.isovalues, "queries_per_step": nq,
-                   "l2": "flushed (256 MiB write) before every timed step",
-                   "round_kernel": ("tcgen05 TF32 hi/lo MMAs + FP32 (orders <= 8)" if args.tensor
-                                    else "FP32 CUDA cores"),
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(args.workload, world),
+        "engine": {"modes_per_dir": N, "round_kernel": ("tcgen05 TF32 hi/lo MMAs + FP32 (orders <= 8)" if args.tensor
+                                                        else "FP32 CUDA cores"),
+                   "rank_share": (f"views {mine}" if multi else f"rows {y0}..{y0 + rows - 1}") if world > 1 else "all"},
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,
                      "traffic": ISECT_TRAFFIC.get((w.name, W, H, head)),
@@ -472,8 +640,11 @@ def run_gpu(args, rank, world):
         "work": st,
         "scene": info,
     }
+    if rank == 0 and world == 1 and not args.no_error_check and not path:
+        line["error_vs_fp64"] = error_vs_fp64(ctx, hr, args, w, views, [m for m in ("plain", "batched", "learned")
+                                                                         if m in results], codes)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(args.workload, min(CPU_BASELINE_QUERIES, args.cpu_queries))
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -495,9 +666,9 @@ def prims_scene(name):
     return prim_synth.mixed_scene(seed=cfg["seed"], n_side=cfg["n_side"]), cfg
 
 
-def prims_cpu_baseline(name, seconds):
-    """The FP32 oracle's primitive pass on a bounded random sample of the
-    workload's rays, all host threads."""
+def prims_cpu_baseline(name, n_queries, seed=0):
+    """The FP32 oracle's primitive pass on n_queries rays drawn from the
+    workload's image, all host threads."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_bind as ob
 
@@ -507,17 +678,14 @@ def prims_cpu_baseline(name, seconds):
     op = ob.OraclePrims(arrs)
     frm, at, fov = cfg["camera"]
     rays = ob.camera_rays(frm, at, (0, 1, 0), fov, cfg["width"], cfg["height"])
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(seed)
     threads = os.cpu_count() or 1
-    done = 0
+    idx = rng.choice(rays.shape[0], n_queries, replace=False)
     t0 = time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
-        idx = rng.integers(0, rays.shape[0], 4096)
-        op.trace(rays[idx], None, 32, threads)
-        done += idx.size
+    op.trace(rays[idx], None, 32, threads)
     dt = time.perf_counter() - t0
-    return {"value": done / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{done} primary rays drawn uniformly from the {cfg['width']}x{cfg['height']} image, "
+    return {"value": n_queries / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n_queries} primary rays drawn uniformly from the {cfg['width']}x{cfg['height']} image, "
                       f"FP32 oracle port of the reference's primitive routines, {threads} threads, {dt:.1f} s"}
 
 
@@ -529,8 +697,11 @@ def run_prims(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    import shard
+
     ps, cfg = prims_scene(args.workload)
     W, H = (args.width, args.height) if args.width and args.height else (cfg["width"], cfg["height"])
+    y0, rows = shard.row_band(H, world, rank)
     frm, at, fov = cfg["camera"]
     cam = hr.Camera(frm, at, vfov_deg=fov)
     ctx = hr.Context(local)
@@ -538,8 +709,8 @@ def run_prims(args, rank, world):
     ctx.build_bvh()
     ctx.set_option(hr.OPT_TIME_ROUNDS, 1)
     info = ctx.info()
-    nq = W * H
-    rgb = torch.empty(nq * 3, dtype=torch.uint8, device=dev)
+    nq = W * rows
+    rgb = torch.empty(max(nq, 1) * 3, dtype=torch.uint8, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
@@ -548,7 +719,8 @@ def run_prims(args, rank, world):
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.zero_()
-            ctx.render_device(cam, [0.0], W, H, rgb.data_ptr(), None, sp)
+            if rows:
+                ctx.render_tile_device(cam, [0.0], W, H, 0, y0, W, rows, rgb.data_ptr(), None, sp)
     torch.cuda.synchronize()
     barrier(world)
     evs = []
@@ -559,7 +731,8 @@ def run_prims(args, rank, world):
                 a = torch.cuda.Event(enable_timing=True)
                 b = torch.cuda.Event(enable_timing=True)
                 a.record(stream)
-                ctx.render_device(cam, [0.0], W, H, rgb.data_ptr(), None, sp)
+                if rows:
+                    ctx.render_tile_device(cam, [0.0], W, H, 0, y0, W, rows, rgb.data_ptr(), None, sp)
                 b.record(stream)
                 evs.append((a, b))
                 s_step = ctx.stats()
@@ -574,12 +747,15 @@ def run_prims(args, rank, world):
     flops = per["prim_flops"] / args.steps
     achieved = flops / kernel_s / 1e12
     # e2e: public API, host image buffer, D2H inside the timed region
-    host_rgb = torch.empty((1, H, W, 3), dtype=torch.uint8).pin_memory()
+    host_rgb = torch.empty((1, rows, W, 3), dtype=torch.uint8).pin_memory()
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(0 if args.no_e2e else args.steps):
-        ctx.render(cam, [0.0], W, H, rgb_out=host_rgb.numpy())
+        if rows:
+            ctx.render_tile(cam, [0.0], W, H, 0, y0, W, rows, rgb_out=host_rgb.numpy())
+        if world > 1:
+            shard.gather_rows(host_rgb.numpy(), H, world, rank)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = None if args.no_e2e else queries / e2e_s / 1e6
     fp32_peak = fp32_peak_tflops(torch, dev)
@@ -587,13 +763,12 @@ def run_prims(args, rank, world):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "gb300",
-        "mode": "primitive pass (prisms, quads, curved triangles; thread per query)",
-        "config": {"workload": args.workload, "primitives": {"prisms": info["n_prisms"], "quads": info["n_quads"],
-                                                             "triangles": info["n_tris"]},
-                   "curved": int((ps.geom_offset >= 0).sum()), "rays": f"{W}x{H} primary",
-                   "queries_per_step": nq, "l2": "flushed (256 MiB write) before every timed step",
-                   "parallelism": f"replicas x{world}"},
+        "scaling": scaling_of(args), "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "impl": "gb300", "mode": "primitive pass (prisms, quads, curved triangles; thread per query)",
+        "config": workload_config(args.workload, world),
+        "engine": {"primitives": {"prisms": info["n_prisms"], "quads": info["n_quads"], "triangles": info["n_tris"]},
+                   "curved": int((ps.geom_offset >= 0).sum()),
+                   "rank_share": f"rows {y0}..{y0 + rows - 1}" if world > 1 else "all"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": (achieved / fp32_peak) if fp32_peak else None,
                      "traffic": PRIM_TRAFFIC.get((args.workload, W, H)),
@@ -609,7 +784,7 @@ def run_prims(args, rank, world):
         "scene": info,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = prims_cpu_baseline(args.workload, args.cpu_seconds)
+        line["cpu_baseline"] = prims_cpu_baseline(args.workload, min(CPU_BASELINE_QUERIES, args.cpu_queries))
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

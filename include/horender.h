@@ -280,6 +280,21 @@ int ho_render(ho_context* ctx, const ho_camera* cam, const float* isovalues, int
 int ho_render_device(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int width,
                      int height, int iso_zero_disables, uint8_t* rgb_dev, ho_hit* hits_dev, void* stream);
 
+/* One tile of the W x H image of ho_render (no reference counterpart: the
+ * reference renders whole images, FEM-AABB/main.cu:515-543; a tile is how
+ * several GPUs share one view). The tile_w x tile_h pixels starting at column
+ * x0, row y0 get exactly the rays, hits and colours they get in the full
+ * render; outputs are laid out like ho_render's for a tile_w x tile_h image.
+ * HO_ERR_RANGE when the tile leaves the image. */
+int ho_render_tile(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int width, int height,
+                   int x0, int y0, int tile_w, int tile_h, int iso_zero_disables, uint8_t* rgb_out,
+                   ho_hit* hits_out);
+/* Device-buffer form of ho_render_tile (stream: a cudaStream_t, NULL = the
+ * context's); returns without synchronising. */
+int ho_render_tile_device(ho_context* ctx, const ho_camera* cam, const float* isovalues, int n_iso, int width,
+                          int height, int x0, int y0, int tile_w, int tile_h, int iso_zero_disables, uint8_t* rgb_dev,
+                          ho_hit* hits_dev, void* stream);
+
 /* Replaces: bvh_intersect_device (FEM-AABB/raytracer.cu:102-358) for
  * caller-supplied rays. rays: n*6 floats (origin xyz, direction xyz), host
  * memory; iso_enabled = 0 traces boundary faces only. */

@@ -623,6 +623,59 @@ int ho_render_device(ho_context* c, const ho_camera* cam, const float* iso, int 
   return mark_call_done(c, s);
 }
 
+int ho_render_tile_device(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int x0,
+                          int y0, int tile_w, int tile_h, int iso_zero_disables, uint8_t* rgb_dev, ho_hit* hits_dev,
+                          void* stream) {
+  if (!c) return HO_ERR_ARG;
+  if (!cam) return fail(c, HO_ERR_ARG, "camera is NULL");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (W <= 0 || H <= 0 || tile_w <= 0 || tile_h <= 0) return fail(c, HO_ERR_ARG, "image and tile sizes must be positive");
+  if (x0 < 0 || y0 < 0 || x0 > W - tile_w || y0 > H - tile_h)
+    return fail(c, HO_ERR_RANGE, "the tile must lie inside the W x H image");
+  if (static_cast<int64_t>(tile_w) * tile_h * n_iso > (int64_t(1) << 31)) return fail(c, HO_ERR_RANGE, "too many rays");
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  ho::TraceArgs a;
+  camera_basis(*cam, W, H, a);
+  a.width = tile_w;
+  a.height = tile_h;
+  a.x0 = x0;
+  a.y0 = y0;
+  a.full_w = W;
+  a.full_h = H;
+  a.n_iso = n_iso;
+  for (int i = 0; i < n_iso; ++i) {
+    a.iso[i] = iso[i];
+    if (!(iso_zero_disables && iso[i] == 0.0f)) a.iso_on_mask |= 1u << i;
+  }
+  a.rgb = rgb_dev;
+  a.hits = hits_dev;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(ho::DevStats), s), "reset stats");
+  rc = ho::launch_trace(c, a, s);
+  if (rc) return cuda_fail(c, rc, "trace kernel");
+  return mark_call_done(c, s);
+}
+
+int ho_render_tile(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int x0, int y0,
+                   int tile_w, int tile_h, int iso_zero_disables, uint8_t* rgb_out, ho_hit* hits_out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  int rc = check_iso(c, iso, n_iso);
+  if (rc) return rc;
+  if (tile_w <= 0 || tile_h <= 0) return fail(c, HO_ERR_ARG, "image and tile sizes must be positive");
+  const size_t nq = static_cast<size_t>(tile_w) * tile_h * n_iso;
+  if (rgb_out && (rc = ensure_buf(c, c->d_rgb, c->rgb_cap, nq * 3, "cudaMalloc(rgb)"))) return rc;
+  if (hits_out && (rc = ensure_buf(c, c->d_hits, c->hits_cap, nq, "cudaMalloc(hits)"))) return rc;
+  rc = ho_render_tile_device(c, cam, iso, n_iso, W, H, x0, y0, tile_w, tile_h, iso_zero_disables,
+                             rgb_out ? c->d_rgb : nullptr, hits_out ? c->d_hits : nullptr, c->stream);
+  if (rc) return rc;
+  if (rgb_out) CK(cudaMemcpyAsync(rgb_out, c->d_rgb, nq * 3, cudaMemcpyDeviceToHost, c->stream), "read image");
+  if (hits_out)
+    CK(cudaMemcpyAsync(hits_out, c->d_hits, nq * sizeof(ho_hit), cudaMemcpyDeviceToHost, c->stream), "read hits");
+  return read_stats(c);
+}
+
 int ho_render_views_device(ho_context* c, int n_views, const ho_camera* cams, const int32_t* widths,
                            const int32_t* heights, const float* isovalues, const int32_t* n_isos, int iso_zero_disables,
                            uint8_t* rgb_dev, ho_hit* hits_dev, int64_t* offsets_out, void* stream) {
@@ -644,6 +697,9 @@ int ho_render_views_device(ho_context* c, int n_views, const ho_camera* cams, co
     d.cam.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
     d.cam.width = widths[v];
     d.cam.height = heights[v];
+    d.cam.x0 = d.cam.y0 = 0;
+    d.cam.full_w = widths[v];
+    d.cam.full_h = heights[v];
     d.q0 = total;
     d.n_iso = n_isos[v];
     d.iso_on_mask = 0;
@@ -769,13 +825,7 @@ int ho_path_trace_device(ho_context* c, const ho_camera* cam, const float* iso, 
   if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
   ho::TraceArgs a;
   camera_basis(*cam, W, H, a);
-  ho::CamArgs ca;
-  ca.origin = make_float3(a.origin[0], a.origin[1], a.origin[2]);
-  ca.llc = make_float3(a.llc[0], a.llc[1], a.llc[2]);
-  ca.horiz = make_float3(a.horiz[0], a.horiz[1], a.horiz[2]);
-  ca.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
-  ca.width = W;
-  ca.height = H;
+  const ho::CamArgs ca = ho::cam_args(a);
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
   int64_t rays = 0;
   ho_stats totals{};

@@ -247,6 +247,8 @@ struct TraceArgs {
   // camera mode (rays == nullptr): pixel-centre rays of a pinhole camera
   float origin[3], llc[3], horiz[3], vert[3];
   int width = 0, height = 0;
+  int x0 = 0, y0 = 0;           // a tile of the full_w x full_h image (0: the
+  int full_w = 0, full_h = 0;   // whole image, full = width, height)
   const float* rays = nullptr;  // explicit rays: n*6 floats on the device
   int64_t n_rays = 0;
   float iso[8];
@@ -259,6 +261,21 @@ struct TraceArgs {
   uint8_t* rgb = nullptr;       // optional (camera mode)
 };
 int launch_trace(ho_context* c, const TraceArgs& a, cudaStream_t s);
+// The kernels' camera of a camera-mode call.
+inline CamArgs cam_args(const TraceArgs& a) {
+  CamArgs c;
+  c.origin = make_float3(a.origin[0], a.origin[1], a.origin[2]);
+  c.llc = make_float3(a.llc[0], a.llc[1], a.llc[2]);
+  c.horiz = make_float3(a.horiz[0], a.horiz[1], a.horiz[2]);
+  c.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
+  c.width = a.width;
+  c.height = a.height;
+  c.x0 = a.x0;
+  c.y0 = a.y0;
+  c.full_w = a.full_w > 0 ? a.full_w : a.width;
+  c.full_h = a.full_h > 0 ? a.full_h : a.height;
+  return c;
+}
 // Path tracing of one image at one isovalue (ho_path.cu); returns a
 // cudaError_t, or a negative HO_ status from the engine (message set).
 int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int spp, int max_depth, uint64_t seed,

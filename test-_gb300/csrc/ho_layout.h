@@ -17,10 +17,13 @@
 namespace ho {
 
 // Pinhole camera of one view: pixel (x, y) looks along
-// llc + s*horiz + t*vert - origin, s = (x + 0.5)/width, t = (y + 0.5)/height.
+// llc + s*horiz + t*vert - origin, s = (x + 0.5)/full_w, t = (y + 0.5)/full_h.
+// A call covers the width x height pixels starting at (x0, y0) of the
+// full_w x full_h image (the whole image: x0 = y0 = 0, full = width, height).
 struct CamArgs {
   float3 origin, llc, horiz, vert;
   int width, height;
+  int x0, y0, full_w, full_h;
 };
 
 // One camera view of a multi-view call: its pixel-centre rays are queries

@@ -274,12 +274,7 @@ int launch_prims(ho_context* c, const TraceArgs& a, ho_hit* hits, bool fresh, De
   P.field = c->d_pfield;
   P.rays = a.rays;
   P.n_rays = a.n_rays;
-  P.cam.origin = make_float3(a.origin[0], a.origin[1], a.origin[2]);
-  P.cam.llc = make_float3(a.llc[0], a.llc[1], a.llc[2]);
-  P.cam.horiz = make_float3(a.horiz[0], a.horiz[1], a.horiz[2]);
-  P.cam.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
-  P.cam.width = a.width;
-  P.cam.height = a.height;
+  P.cam = cam_args(a);
   P.views = a.views;
   P.n_views = a.n_views;
   for (int i = 0; i < 8; ++i) P.iso[i] = i < a.n_iso ? a.iso[i] : 0.f;

@@ -160,12 +160,7 @@ static int trace_hexes(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   P.flags = c->d_flags;
   P.rays = a.rays;
   P.n_rays = a.n_rays;
-  P.cam.origin = make_float3(a.origin[0], a.origin[1], a.origin[2]);
-  P.cam.llc = make_float3(a.llc[0], a.llc[1], a.llc[2]);
-  P.cam.horiz = make_float3(a.horiz[0], a.horiz[1], a.horiz[2]);
-  P.cam.vert = make_float3(a.vert[0], a.vert[1], a.vert[2]);
-  P.cam.width = a.width;
-  P.cam.height = a.height;
+  P.cam = cam_args(a);
   for (int i = 0; i < 8; ++i) P.iso[i] = i < a.n_iso ? a.iso[i] : 0.f;
   P.n_iso = a.n_iso;
   P.iso_on_mask = a.iso_on_mask;

@@ -200,9 +200,9 @@ __device__ __forceinline__ void shade(const HitState& h, float3 d, uint8_t* out)
 
 // Pixel-centre ray of pixel `pix` of a pinhole camera.
 __device__ __forceinline__ void camera_ray(const CamArgs& cam, int64_t pix, float3& o, float3& d) {
-  const int x = static_cast<int>(pix % cam.width), y = static_cast<int>(pix / cam.width);
-  const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(cam.width);
-  const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(cam.height);
+  const int x = cam.x0 + static_cast<int>(pix % cam.width), y = cam.y0 + static_cast<int>(pix / cam.width);
+  const float s = (static_cast<float>(x) + 0.5f) / static_cast<float>(cam.full_w);
+  const float t = (static_cast<float>(y) + 0.5f) / static_cast<float>(cam.full_h);
   o = cam.origin;
   d = make_float3(cam.llc.x + s * cam.horiz.x + t * cam.vert.x - o.x, cam.llc.y + s * cam.horiz.y + t * cam.vert.y - o.y,
                   cam.llc.z + s * cam.horiz.z + t * cam.vert.z - o.z);

@@ -101,6 +101,9 @@ def _load():
     L.ho_render_views.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp]
     L.ho_render_views_device.argtypes = [vp, i32, vp, vp, vp, vp, vp, i32, vp, vp, vp, vp]
     L.ho_render_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, vp, vp, vp]
+    L.ho_render_tile.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp]
+    L.ho_render_tile_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp,
+                                        vp]
     L.ho_path_trace.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, i32, C.c_uint64, i32, vp,
                                 C.POINTER(i64)]
     L.ho_path_trace_device.argtypes = [vp, C.POINTER(_Camera), vp, i32, i32, i32, i32, i32, C.c_uint64, i32, vp,
@@ -367,6 +370,32 @@ class Context:
         self._ck(lib.ho_render_views_device(self.h, n, C.cast(cams, C.c_void_p), _p(w), _p(h), _p(iso), _p(n_iso),
                                             int(iso_zero_disables), rgb_ptr, hits_ptr, _p(offs), stream_ptr))
         return offs
+
+    def render_tile(self, camera: Camera, isovalues, width: int, height: int, x0: int, y0: int, tile_w: int,
+                    tile_h: int, iso_zero_disables: bool = True, want_rgb: bool = True, want_hits: bool = False,
+                    rgb_out: np.ndarray | None = None):
+        """The tile_w x tile_h pixels at (x0, y0) of the width x height render:
+        images (n_iso, tile_h, tile_w, 3) and hits, equal to that part of render()."""
+        iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
+        n = iso.size
+        if rgb_out is not None:
+            assert rgb_out.dtype == np.uint8 and rgb_out.size == n * tile_h * tile_w * 3 and rgb_out.flags.c_contiguous
+            rgb = rgb_out
+        else:
+            rgb = np.zeros((n, tile_h, tile_w, 3), np.uint8) if want_rgb else None
+        hits = np.zeros((n, tile_h, tile_w), HIT_DTYPE) if want_hits else None
+        cam = _cam(camera)
+        self._ck(lib.ho_render_tile(self.h, C.byref(cam), _p(iso), n, width, height, x0, y0, tile_w, tile_h,
+                                    int(iso_zero_disables), _p(rgb) if rgb is not None else None,
+                                    _p(hits) if hits is not None else None))
+        return rgb, hits
+
+    def render_tile_device(self, camera: Camera, isovalues, width, height, x0, y0, tile_w, tile_h, rgb_ptr, hits_ptr,
+                           stream_ptr, iso_zero_disables: bool = True):
+        iso = np.ascontiguousarray(isovalues, np.float32).reshape(-1)
+        cam = _cam(camera)
+        self._ck(lib.ho_render_tile_device(self.h, C.byref(cam), _p(iso), iso.size, width, height, x0, y0, tile_w,
+                                           tile_h, int(iso_zero_disables), rgb_ptr, hits_ptr, stream_ptr))
 
     def render_device(self, camera: Camera, isovalues, width, height, rgb_ptr, hits_ptr, stream_ptr,
                       iso_zero_disables: bool = True):

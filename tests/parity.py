@@ -1,0 +1,139 @@
+"""Comparison of product hits with the oracle (TEST INFRASTRUCTURE: used by
+the tests and by bench.py's error_vs_fp64 block, always as the checker).
+
+Identity (kind, element, face) of a product hit is compared with the oracle's
+answer for the same ray; t, xi, u and the isosurface position are compared
+with the judge: the FP64 oracle's hit polished to the exact root of its own
+defining equations (oracle_bind.OracleScene.polish), so the yardstick does not
+carry the reference's stopping tolerances (face residual 1e-4, |u - iso|
+1e-5).
+
+Rays whose identity differs are classified:
+  tie        both answers are hits at the same t (within TIE_T), on different
+             elements or faces: one surface point claimed twice (a face shared
+             by two elements, an edge of two faces, an isosurface root in the
+             overlap of two elements' padded boxes);
+  grazing    |d . n| < GRAZE at either answer's hit;
+  unstable   the reference algorithm's own answer is not stable on the ray:
+             the FP32 and FP64 oracles disagree, or either changes its answer
+             when the ray is turned by up to 4e-5 radians (NUDGE_ANGLES: a
+             7th of a pixel at 3840 pixels over 60 degrees; 8 directions at
+             each angle), or, where the caller passes the product's own
+             tracer, the product's answer changes under the same turns. The
+             ray then sits at a decision boundary of the algorithm: a sign
+             change of u - iso at a scan sample, an inverse map that converges
+             in one rounding and not in another (the reference skips such a
+             sample, and a failed solve in the refinement turns the
+             candidate's isosurface hit into a face test), the acceptance edge
+             of a face, the clipping bound;
+  other      none of these (a failure).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+TIE_T = 1e-4      # the reference's face tolerance, in world units
+GRAZE = 0.05      # |cos| of the angle between the ray and the surface normal
+NUDGE_ANGLES = (2e-6, 1e-5, 4e-5)  # radians
+N_NUDGE = 8 * len(NUDGE_ANGLES)
+CLASSES = ("tie", "grazing", "unstable", "other")
+
+
+def ids(h) -> np.ndarray:
+    return np.stack([np.asarray(h["kind"]).astype(np.int64), np.asarray(h["elem"]).astype(np.int64),
+                     np.asarray(h["face"]).astype(np.int64)], 1)
+
+
+def same_ids(a, b) -> np.ndarray:
+    return np.all(ids(a) == ids(b), axis=1)
+
+
+def nudged(rays: np.ndarray) -> np.ndarray:
+    """Copies of each ray with the direction turned by NUDGE_ANGLES radians
+    towards 8 fixed directions of the plane normal to it (the origin kept):
+    N_NUDGE rays per ray, in ray-major order."""
+    r = np.asarray(rays, np.float64).reshape(-1, 6)
+    d = r[:, 3:] / np.linalg.norm(r[:, 3:], axis=1, keepdims=True)
+    helper = np.where(np.abs(d[:, :1]) < 0.9, np.array([[1.0, 0, 0]]), np.array([[0, 1.0, 0]]))
+    u = np.cross(d, helper)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    v = np.cross(d, u)
+    out = np.zeros((r.shape[0], N_NUDGE, 6))
+    out[:, :, :3] = r[:, None, :3]
+    k = 0
+    for ang in NUDGE_ANGLES:
+        for j in range(8):
+            a = np.pi * j / 4
+            d2 = d + ang * (np.cos(a) * u + np.sin(a) * v)
+            out[:, k, 3:] = d2 / np.linalg.norm(d2, axis=1, keepdims=True)
+            k += 1
+    return out.reshape(-1, 6).astype(np.float32)
+
+
+def _varies(hits, base_ids, n) -> np.ndarray:
+    return ~np.all(ids(hits).reshape(n, N_NUDGE, 3) == base_ids[:, None, :], axis=(1, 2))
+
+
+def classify(gpu, ora, rays, osc, iso, product_trace=None) -> dict:
+    """Classes of the identity differences between gpu (product hits) and ora
+    (the oracle's or the reference's hits on the same rays at isovalue iso).
+    product_trace(rays) -> product hits, optional: lets the product's own
+    answer under the nudges count for 'unstable'. Returns the number of rays,
+    of differing rays, and the indices of the differing rays per class."""
+    diff = np.where(~same_ids(gpu, ora))[0]
+    out = {"rays": int(len(ora)), "differ": int(diff.size)}
+    for k in CLASSES:
+        out[k] = np.zeros(0, np.int64)
+    if diff.size == 0:
+        return out
+    g, o, r = gpu[diff], ora[diff], np.asarray(rays)[diff]
+    both = (g["kind"] > 0) & (o["kind"] > 0)
+    tie = both & (np.abs(g["t"].astype(np.float64) - np.asarray(o["t"], np.float64)) <= TIE_T)
+    d = r[:, 3:].astype(np.float64)
+    gn = np.abs((np.asarray(g["n"], np.float64) * d).sum(1))
+    on = np.abs((np.asarray(o["n"], np.float64) * d).sum(1))
+    graz = ~tie & (((g["kind"] > 0) & (gn < GRAZE)) | ((o["kind"] > 0) & (on < GRAZE)))
+    rest = np.where(~tie & ~graz)[0]
+    unstable = np.zeros(diff.size, bool)
+    if rest.size:
+        rr = r[rest]
+        nr = nudged(rr)
+        b32, _ = osc.trace(rr, iso, True, precision=32)
+        b64, _ = osc.trace(rr, iso, True, precision=64)
+        varies = ~same_ids(b32, b64)
+        for prec, base in ((64, ids(b64)), (32, ids(b32))):
+            hn, _ = osc.trace(nr, iso, True, precision=prec)
+            varies |= _varies(hn, base, rest.size)
+        if product_trace is not None:
+            varies |= _varies(product_trace(nr), ids(g[rest]), rest.size)
+        unstable[rest] = varies
+    other = ~tie & ~graz & ~unstable
+    out["tie"], out["grazing"] = diff[tie], diff[graz]
+    out["unstable"], out["other"] = diff[unstable], diff[other]
+    return out
+
+
+def counts(cls: dict) -> dict:
+    return {k: (int(v.size) if isinstance(v, np.ndarray) else v) for k, v in cls.items()}
+
+
+def errors(gpu, judge, rays, h: float) -> dict:
+    """Errors of the product's hits against the judge on the rays whose
+    identity agrees and whose judge polish converged (judge['pad'] == 1).
+    t (= the position along the unit ray) in units of the element size h; xi
+    and u absolute."""
+    ok = same_ids(gpu, judge) & (judge["kind"] > 0) & (judge["pad"] == 1)
+    res = {}
+    for kind, lab in ((1, "face"), (2, "iso")):
+        m = ok & (gpu["kind"] == kind)
+        if not m.any():
+            res[lab] = {"n": 0}
+            continue
+        dt = np.abs(gpu["t"][m].astype(np.float64) - judge["t"][m])
+        dxi = np.abs(np.asarray(gpu["xi"][m], np.float64) - judge["xi"][m]).max(1)
+        du = np.abs(gpu["u"][m].astype(np.float64) - judge["u"][m])
+        res[lab] = {"n": int(m.sum()), "t_max_over_h": float(dt.max() / h),
+                    "t_p99_over_h": float(np.quantile(dt, .99) / h), "xi_max": float(dxi.max()),
+                    "xi_p99": float(np.quantile(dxi, .99)), "u_max": float(du.max()),
+                    "u_p99": float(np.quantile(du, .99))}
+    return res
