@@ -79,7 +79,7 @@ def _trace_rows(ob, osc, w, W, H, y0, rows):
     return rgb.reshape(1, rows, W, 3), hits.reshape(1, rows, W)
 
 
-VIEWS = [((2.5, 2.0, 1.8), 21, 13), ((-1.5, 0.4, 2.2), 9, 30), ((0.5, 3.0, 0.5), 16, 16), ((2.2, -1.0, -0.8), 7, 5),
+VIEWS = [((2.5, 2.0, 1.8), 21, 13), ((-1.5, 0.4, 2.2), 9, 30), ((0.4, 0.6, 3.0), 16, 16), ((2.2, -1.0, -0.8), 7, 5),
          ((-1.0, -1.5, 1.0), 25, 8)]
 
 
