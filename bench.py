@@ -424,7 +424,8 @@ def error_vs_fp64(ctx, hr, args, w, views, modes, codes):
         cls = {k: 0 for k in ("differ", "tie", "grazing", "unstable", "other")}
         for iso in np.unique(isos):
             m = np.where(isos == iso)[0]
-            c = parity.counts(parity.classify(g[m], o64[m], rays[m], osc, float(iso)))
+            c = parity.counts(parity.classify(g[m], o64[m], rays[m], osc, float(iso),
+                                              product_trace=lambda r, v=float(iso): ctx.intersect(r, v, True)))
             for k in cls:
                 cls[k] += c[k]
         errs = parity.errors(g, judge, rays, h)

@@ -154,6 +154,8 @@ typedef struct {
   uint64_t prim_kernel_ns;   /* HO_OPT_TIME_ROUNDS: device time of the
                                 primitive pass (CUDA events), else 0          */
   uint64_t prim_node_visits; /* primitive-tree nodes visited by that pass     */
+  uint64_t fp64_polished;    /* hits whose t, xi and u the FP64 polish moved to
+                                the exact root of their defining equations   */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */
@@ -341,11 +343,16 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     enqueues one more than the previous call needed; rays
  *                     still in flight afterwards get further rounds, one
  *                     read-back each.
- * HO_OPT_FP64_CHECK   1 (default): every hit of a batched / learned call is
- *                     re-evaluated in FP64 (position residual, and field
- *                     residual for isosurface hits); a failing hit is traced
- *                     again by the plain solver (HO_FLAG_FALLBACK), and is
- *                     flagged HO_FLAG_FP64_FAIL if that fails too; 0: off.
+ * HO_OPT_FP64_CHECK   1 (default): every hit is re-evaluated in FP64
+ *                     (position residual, and field residual for isosurface
+ *                     hits). A passing hit is polished: a Newton step on its
+ *                     defining equations (FP64 residual, FP32 Jacobian) moves
+ *                     t, xi and u to the exact root, within FP32 rounding of
+ *                     t (ho_stats.fp64_polished counts them). In batched /
+ *                     learned mode a failing hit is traced again by the plain
+ *                     solver (HO_FLAG_FALLBACK) and flagged
+ *                     HO_FLAG_FP64_FAIL if that fails too; in plain mode it
+ *                     is flagged. 0: off (the solvers' own answers).
  * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
  *                     default: the kernel's pair slots, 20 per warp up to 7
  *                     modes per direction, 12 at 8, 8 at 9, times 4 warps in

@@ -16,6 +16,8 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <thread>
+#include <atomic>
 
 #include "fem/ModalBasis.cuh"
 #include "fem/PrismElement.cuh"
@@ -329,13 +331,20 @@ int ref_hit_hex(void* p, int elem, const float* rays, const float* seg, int64_t 
 // kind (0 miss, 1 face, 2 iso), elem, face, t, xi(3), normal(3), material, pad.
 // order (optional, n x order_cap): elements visited (box test passed), in
 // visit order, -1 padded; order_n[i] = how many (may exceed order_cap).
-int ref_trace_order(void* p, const float* rays, int64_t n, float iso, float* out, int32_t* order, int order_cap,
-                    int32_t* order_n);
-int ref_trace(void* p, const float* rays, int64_t n, float iso, float* out) {
-  return ref_trace_order(p, rays, n, iso, out, nullptr, 0, nullptr);
-}
+// iso_mode: 0 = the renderer's rule (isovalue 0 turns the isosurface off,
+// raytracer.cu:207); 1 = FindIsosurfaceOnRayHex is called for every
+// isovalue, 0 included (how an isovalue of 0 is compared at all).
+int ref_trace_order_iso(void* p, const float* rays, int64_t n, float iso, int iso_mode, float* out, int32_t* order,
+                        int order_cap, int32_t* order_n);
 int ref_trace_order(void* p, const float* rays, int64_t n, float iso, float* out, int32_t* order, int order_cap,
                     int32_t* order_n) {
+  return ref_trace_order_iso(p, rays, n, iso, 0, out, order, order_cap, order_n);
+}
+int ref_trace(void* p, const float* rays, int64_t n, float iso, float* out) {
+  return ref_trace_order_iso(p, rays, n, iso, 0, out, nullptr, 0, nullptr);
+}
+int ref_trace_order_iso(void* p, const float* rays, int64_t n, float iso, int iso_mode, float* out, int32_t* order,
+                        int order_cap, int32_t* order_n) {
   RefScene* s = static_cast<RefScene*>(p);
   if (!s->bvh_built) {
     std::vector<Sphere> sp;
@@ -348,7 +357,14 @@ int ref_trace_order(void* p, const float* rays, int64_t n, float iso, float* out
   }
   const auto& nodes = s->bvh.nodes;
   const auto& prims = s->bvh.primitive_indices;
-  for (int64_t ri = 0; ri < n; ++ri) {
+  // rays are independent: the reference's element routines keep no state,
+  // so the host walk runs on every hardware thread (each ray writes its own
+  // output slots)
+  std::atomic<int64_t> next_ray{0};
+  auto walk = [&] {
+  for (;;) {
+    const int64_t ri = next_ray.fetch_add(1);
+    if (ri >= n) break;
     ::Ray ray(make_float3(rays[6 * ri], rays[6 * ri + 1], rays[6 * ri + 2]),
               make_float3(rays[6 * ri + 3], rays[6 * ri + 4], rays[6 * ri + 5]));
     float rec_t = FLT_MAX;
@@ -379,7 +395,7 @@ int ref_trace_order(void* p, const float* rays, int64_t n, float iso, float* out
           ++nvis;
           float th;
           float3 rst, g;
-          const bool iso_ok = (iso != 0.0f) && elem.fieldCoefficients != nullptr && elem.fieldModes.x > 0 &&
+          const bool iso_ok = (iso_mode == 1 || iso != 0.0f) && elem.fieldCoefficients != nullptr && elem.fieldModes.x > 0 &&
                               elem.fieldModes.y > 0 && elem.fieldModes.z > 0;
           if (iso_ok && zidingyi::FindIsosurfaceOnRayHex(elem, hr, te, tx, iso, th, rst, g)) {
             if (th > 0.001f && th < rec_t) {
@@ -421,6 +437,13 @@ int ref_trace_order(void* p, const float* rays, int64_t n, float iso, float* out
     o[7] = hit_n.x; o[8] = hit_n.y; o[9] = hit_n.z;
     o[10] = float(mat); o[11] = 0.f;
   }
+  };
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  std::vector<std::thread> pool;
+  for (unsigned k = 1; k < nt; ++k) pool.emplace_back(walk);
+  walk();
+  for (auto& th : pool) th.join();
   return 0;
 }
 

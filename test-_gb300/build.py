@@ -27,8 +27,10 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", str
           "-I", str(CSRC)]
 CU_FLAGS = ARCH + COMMON + ["--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 # per-file extras: the primitive pass rounds every operation on its own, as
-# the reference's FP32 host code does (its start searches branch on exact values)
-FILE_FLAGS = {"ho_prim.cu": ["--fmad=false"]}
+# the reference's FP32 host code does (its start searches branch on exact
+# values); the host scene numerics fuse no multiply-adds, so a seeded scene
+# has the same bits on x86-64 and aarch64 hosts (as far as their libm agrees)
+FILE_FLAGS = {"ho_prim.cu": ["--fmad=false"], "ho_scene.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def sources() -> list[Path]:
@@ -59,7 +61,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if src.suffix == ".cu":
             cmd = [NVCC] + CU_FLAGS + FILE_FLAGS.get(src.name, []) + ["-c", str(src), "-o", str(obj)]
         else:
-            cmd = [NVCC] + ARCH + COMMON + ["-x", "c++", "-c", str(src), "-o", str(obj)]
+            cmd = [NVCC] + ARCH + COMMON + FILE_FLAGS.get(src.name, []) + ["-x", "c++", "-c", str(src), "-o", str(obj)]
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)))
     failed = []
     for src, p in procs:

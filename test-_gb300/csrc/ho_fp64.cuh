@@ -1,0 +1,274 @@
+// FP64 evaluation of a hit and its polish, shared by the final check of the
+// batched / learned engines (ho_check.cuh) and the plain kernel.
+//
+// The FP32 solves stop on the reference's own criteria (inverse-map step
+// below 1e-5, surface residual below 1e-4, isosurface |f| below 1e-5). The
+// check re-evaluates the returned point in FP64 from the element's
+// coefficients: the position x(xi) against o + t d, and for an isosurface
+// hit the field u(xi) against the isovalue.
+//
+// The polish: those stopping rules leave t uncertain by up to their
+// tolerances (a face hit is accepted at the first iterate whose residual is
+// below 1e-4, so its t can be off by 1e-4 / |d.n|). A hit that passes the
+// check takes a Newton step on the equations that define it, with the FP64
+// residual just computed and the FP32 Jacobian at the hit:
+//   face f:      x(xi) = o + t d, xi's fixed coordinate held (unknowns: the
+//                two free coordinates and t), a 3x3 solve;
+//   isosurface:  x(xi) = o + t d and u(xi) = iso (unknowns: xi and t), a
+//                4x4 solve through J^-1.
+// The step's error is quadratic in its size plus the FP32 Jacobian's
+// relative error times its size, so from a residual of 1e-4 it lands within
+// about 1e-8; a step larger than that is followed by up to two more with the
+// residual re-evaluated in FP64 and the same Jacobian. The hit keeps its
+// element, face and kind; t, xi and u move to the root of the same equations,
+// which leaves t within FP32 rounding of the exact root. A step in t larger
+// than 1e-3 or in xi larger than 0.05, a non-finite one, or one that takes a
+// face hit's free coordinates out of [-1.001, 1.001] leaves the hit as the
+// solver returned it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ho_device.cuh"
+#include "ho_layout.h"
+
+namespace ho {
+
+// Tolerances of the check, FP64 and absolute (the scene is O(1)): the face
+// acceptance 1e-4 and the isosurface criterion 1e-5, each with room for the
+// FP32 rounding of the returned point.
+constexpr double kCheckFaceTol = 1.5e-4;
+constexpr double kCheckIsoPosTol = 1e-4;
+constexpr double kCheckIsoFieldTol = 2e-5;
+
+// Modified-A basis values in FP64, the recurrence of basis_val.
+template <int N>
+__device__ __forceinline__ void basis_val64(double x, double (&a)[N]) {
+  a[0] = 0.5 * (1.0 - x);
+  if (N > 1) a[1] = 0.5 * (1.0 + x);
+  const double w = 0.25 * (1.0 - x * x);
+  double pm2 = 1.0, pm1 = 2.0 * x;
+#pragma unroll
+  for (int i = 2; i < N; ++i) {
+    const int m = i - 2;
+    double p;
+    if (m == 0) p = 1.0;
+    else if (m == 1) p = pm1;
+    else {
+      const double A = double((2 * m + 1) * (m + 1)) / double(m * (m + 2));
+      const double B = double(m + 1) / double(m + 2);
+      p = A * x * pm1 - B * pm2;
+      pm2 = pm1;
+      pm1 = p;
+    }
+    a[i] = w * p;
+  }
+}
+
+// Knuth's TwoSum: s + e == a + b exactly (round-to-nearest FP32; the
+// intrinsics keep the compiler from fusing or reordering the steps).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Value of one coefficient block (rows padded to row_stride(N), a multiple of
+// 4 floats, so a row is RS/4 aligned float4 loads), FP64-accurate.
+//
+// The coefficients are FP32, so the innermost sums sum_i c_i a_i are formed
+// in double-single arithmetic on the FP32 pipes: a_i = ah_i + al_i (two
+// floats), c_i ah_i = p + ep exactly (FMA-based TwoProduct), the running sum
+// kept as sh + sl with TwoSum, the small parts added in FP32. That is about
+// 2^-44 relative per row, below FP64's own rounding of the outer sums, and
+// avoids an FP64 conversion and FMA per coefficient (FP64 runs at a small
+// fraction of the FP32 rate here). The sums over j and k, and the residuals,
+// are FP64.
+template <int N>
+__device__ double value64(const float* __restrict__ blk, const float (&ah)[N], const float (&al)[N],
+                          const double (&as)[N], const double (&at)[N]) {
+  constexpr int RS = row_stride(N);
+  static_assert(RS % 4 == 0, "rows are whole float4s");
+  double v = 0.0;
+#pragma unroll 1
+  for (int k = 0; k < N; ++k) {
+    double q = 0.0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const float4* row = reinterpret_cast<const float4*>(blk + (k * N + j) * RS);
+      float c[RS];
+#pragma unroll
+      for (int i4 = 0; i4 < RS / 4; ++i4) {
+        const float4 t4 = __ldg(row + i4);
+        c[4 * i4] = t4.x;
+        c[4 * i4 + 1] = t4.y;
+        c[4 * i4 + 2] = t4.z;
+        c[4 * i4 + 3] = t4.w;
+      }
+      float sh = 0.f, sl = 0.f;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        const float p = __fmul_rn(c[i], ah[i]);
+        const float ep = __fmaf_rn(c[i], ah[i], -p);
+        float s, es;
+        two_sum(sh, p, s, es);
+        sh = s;
+        sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(es, ep), __fmul_rn(c[i], al[i])));
+      }
+      q = fma(static_cast<double>(sh) + static_cast<double>(sl), as[j], q);
+    }
+    double atk = 0.0;  // at[k] by selection: the array stays in registers
+#pragma unroll
+    for (int kk = 0; kk < N; ++kk)
+      if (kk == k) atk = at[kk];
+    v = fma(q, atk, v);
+  }
+  return v;
+}
+
+// The FP64 residual vector r = x(xi) - (o + t d) of a point in element elem,
+// and the field value u(xi) (0 when unused).
+template <int N>
+__device__ __noinline__ void fp64_residual_vec(const float* __restrict__ rec_all, int elem, float3 o, float3 d,
+                                               double t, double x0, double x1, double x2, bool want_field,
+                                               double* __restrict__ r, double& u) {
+  const float* rec = rec_all + static_cast<int64_t>(elem) * record_floats(N);
+  double ar[N], as[N], at[N];
+  basis_val64<N>(x0, ar);
+  basis_val64<N>(x1, as);
+  basis_val64<N>(x2, at);
+  float ah[N], al[N];  // ar as two floats
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    ah[i] = static_cast<float>(ar[i]);
+    al[i] = static_cast<float>(ar[i] - static_cast<double>(ah[i]));
+  }
+  r[0] = value64<N>(rec, ah, al, as, at) - (static_cast<double>(o.x) + t * d.x);
+  r[1] = value64<N>(rec + block_floats(N), ah, al, as, at) - (static_cast<double>(o.y) + t * d.y);
+  r[2] = value64<N>(rec + 2 * block_floats(N), ah, al, as, at) - (static_cast<double>(o.z) + t * d.z);
+  u = want_field ? value64<N>(rec + 3 * block_floats(N), ah, al, as, at) : 0.0;
+}
+
+// The FP64 residuals of a hit at xi in element elem: the largest component
+// of x(xi) - (o + t d), and the field value u(xi) (0 when unused).
+template <int N>
+__device__ void fp64_residuals(const float* __restrict__ rec_all, int elem, float3 o, float3 d, float t, float3 xi,
+                               bool want_field, double& rpos, double& u) {
+  double r[3];
+  fp64_residual_vec<N>(rec_all, elem, o, d, t, xi.x, xi.y, xi.z, want_field, r, u);
+  rpos = fmax(fabs(r[0]), fmax(fabs(r[1]), fabs(r[2])));
+}
+
+// Newton steps of the polish at most: the first uses the FP64 residual of the
+// check; each later one re-evaluates it at the new point and keeps the first
+// step's FP32 Jacobian (a chord step, whose error shrinks by about the
+// relative change of J across the first step).
+constexpr int kPolishSteps = 3;
+
+// One Newton step on a hit's defining equations (file header): from the
+// FP64 residual r and field value u at (t, xi), with the FP32 Jacobian J and
+// xi-gradient g of the field at the hit. Returns false when the step is not
+// usable (singular, too large, not finite).
+__device__ __forceinline__ bool polish_step(const HitState& h, float3 d, float iso, const float (&J)[9], float3 g,
+                                            const double (&r)[3], double u, double (&dx)[3], double& dt) {
+  if (h.kind == HO_HIT_FACE) {
+    int fixed, ua, va;
+    float val;
+    face_param(h.face, fixed, val, ua, va);
+    // Cramer's rule on [J_u J_v -d] (du, dv, dt) = -r
+    const double a0 = J[ua], a1 = J[3 + ua], a2 = J[6 + ua];
+    const double b0 = J[va], b1 = J[3 + va], b2 = J[6 + va];
+    const double c0 = -static_cast<double>(d.x), c1 = -static_cast<double>(d.y), c2 = -static_cast<double>(d.z);
+    const double det = a0 * (b1 * c2 - b2 * c1) - b0 * (a1 * c2 - a2 * c1) + c0 * (a1 * b2 - a2 * b1);
+    if (!(fabs(det) > 0.0)) return false;
+    const double q0 = -r[0], q1 = -r[1], q2 = -r[2];
+    const double du = (q0 * (b1 * c2 - b2 * c1) - b0 * (q1 * c2 - q2 * c1) + c0 * (q1 * b2 - q2 * b1)) / det;
+    const double dv = (a0 * (q1 * c2 - q2 * c1) - q0 * (a1 * c2 - a2 * c1) + c0 * (a1 * q2 - a2 * q1)) / det;
+    dt = (a0 * (b1 * q2 - b2 * q1) - b0 * (a1 * q2 - a2 * q1) + q0 * (a1 * b2 - a2 * b1)) / det;
+    dx[0] = dx[1] = dx[2] = 0.0;
+    dx[ua] = du;
+    dx[va] = dv;
+  } else {
+    // J dxi - d dt = -r, g . dxi = -(u - iso): dxi = a + b dt with
+    // a = -J^-1 r, b = J^-1 d
+    const double j0 = J[0], j1 = J[1], j2 = J[2], j3 = J[3], j4 = J[4], j5 = J[5], j6 = J[6], j7 = J[7], j8 = J[8];
+    const double k0 = j4 * j8 - j5 * j7, k1 = j2 * j7 - j1 * j8, k2 = j1 * j5 - j2 * j4;
+    const double k3 = j5 * j6 - j3 * j8, k4 = j0 * j8 - j2 * j6, k5 = j2 * j3 - j0 * j5;
+    const double k6 = j3 * j7 - j4 * j6, k7 = j1 * j6 - j0 * j7, k8 = j0 * j4 - j1 * j3;
+    const double det = j0 * k0 + j1 * k3 + j2 * k6;
+    if (!(fabs(det) > 0.0)) return false;
+    const double id = 1.0 / det;
+    const double a[3] = {-(k0 * r[0] + k1 * r[1] + k2 * r[2]) * id, -(k3 * r[0] + k4 * r[1] + k5 * r[2]) * id,
+                         -(k6 * r[0] + k7 * r[1] + k8 * r[2]) * id};
+    const double b[3] = {(k0 * d.x + k1 * d.y + k2 * d.z) * id, (k3 * d.x + k4 * d.y + k5 * d.z) * id,
+                         (k6 * d.x + k7 * d.y + k8 * d.z) * id};
+    const double gb = g.x * b[0] + g.y * b[1] + g.z * b[2];
+    if (!(fabs(gb) > 0.0)) return false;
+    dt = (-(u - static_cast<double>(iso)) - (g.x * a[0] + g.y * a[1] + g.z * a[2])) / gb;
+    for (int k = 0; k < 3; ++k) dx[k] = a[k] + b[k] * dt;
+  }
+  // a face hit accepted at a residual of 1e-4 is up to about 1e-4 / |J| off
+  // in xi (|J| is about half the element size): the limits leave room for that
+  const double mx = fmax(fabs(dx[0]), fmax(fabs(dx[1]), fabs(dx[2])));
+  return fabs(dt) <= 1e-3 && mx <= 0.05;  // also false for a NaN step
+}
+
+// The FP64 check of a hit (a miss always passes) and, when it passes, the
+// polish (file header). Returns whether the hit passed; polished is set when
+// the hit's t, xi and u were refined.
+template <int N>
+__device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint32_t* __restrict__ eflags, float3 o,
+                                  float3 d, float iso, HitState& h, bool& polished) {
+  polished = false;
+  if (h.kind == HO_HIT_MISS) return true;
+  const bool iso_hit = h.kind != HO_HIT_FACE;
+  const bool has_field = iso_hit || (__ldg(eflags + h.elem) & 1u) != 0;
+  double r[3], u;
+  fp64_residual_vec<N>(rec_all, h.elem, o, d, h.t, h.xi.x, h.xi.y, h.xi.z, has_field, r, u);
+  const double rpos = fmax(fabs(r[0]), fmax(fabs(r[1]), fabs(r[2])));
+  if (!iso_hit) {
+    if (rpos > kCheckFaceTol) return false;
+  } else if (rpos > kCheckIsoPosTol || fabs(u - static_cast<double>(iso)) > kCheckIsoFieldTol) {
+    return false;
+  }
+  // FP32 Jacobian and field gradient at the hit
+  const CoefRef<false> c{rec_all + static_cast<int64_t>(h.elem) * record_floats(N)};
+  float xJ[12];
+  geom_eval_raw<N, false>(c, h.xi, xJ);
+  const float J[9] = {xJ[1], xJ[2], xJ[3], xJ[5], xJ[6], xJ[7], xJ[9], xJ[10], xJ[11]};
+  float3 g = make_float3(0.f, 0.f, 0.f);
+  if (has_field) {
+    float ug[4];
+    field_eval_raw<N, false>(c.at(3 * block_floats(N)), h.xi, ug);
+    g = make_float3(ug[1], ug[2], ug[3]);
+  }
+  double t = h.t, x0 = h.xi.x, x1 = h.xi.y, x2 = h.xi.z, un = u;
+  for (int step = 0; step < kPolishSteps; ++step) {
+    double dx[3], dt;
+    if (!polish_step(h, d, iso, J, g, r, u, dx, dt)) return true;
+    t += dt;
+    x0 += dx[0];
+    x1 += dx[1];
+    x2 += dx[2];
+    un = u + (g.x * dx[0] + g.y * dx[1] + g.z * dx[2]);
+    // a step this small leaves an error far below FP32 rounding of t and xi
+    const double mx = fmax(fabs(dx[0]), fmax(fabs(dx[1]), fabs(dx[2])));
+    if (step + 1 == kPolishSteps || (mx <= 1e-5 && fabs(dt) <= 1e-7)) break;
+    fp64_residual_vec<N>(rec_all, h.elem, o, d, t, x0, x1, x2, has_field, r, u);
+    un = u;
+  }
+  if (h.kind == HO_HIT_FACE) {
+    int fixed, ua, va;
+    float val;
+    face_param(h.face, fixed, val, ua, va);
+    const double pu = ua == 0 ? x0 : (ua == 1 ? x1 : x2), pv = va == 0 ? x0 : (va == 1 ? x1 : x2);
+    if (!(fabs(pu) <= 1.001 && fabs(pv) <= 1.001)) return true;
+  }
+  h.t = static_cast<float>(t);
+  h.xi = make_float3(static_cast<float>(x0), static_cast<float>(x1), static_cast<float>(x2));
+  if (has_field) h.u = static_cast<float>(un);
+  polished = true;
+  return true;
+}
+
+}  // namespace ho

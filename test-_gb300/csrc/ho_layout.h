@@ -87,6 +87,7 @@ enum StatSlot {
   ST_PRIM_ITERS,
   ST_PRIM_FLOPS,
   ST_PRIM_NODES,
+  ST_POLISHED,  // hits refined by the FP64 polish (check and plain kernels)
   ST_COUNT
 };
 

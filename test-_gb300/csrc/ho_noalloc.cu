@@ -146,6 +146,7 @@ extern "C" int ho_intersect_device_noalloc(ho_context* c, int64_t n, const float
   P.cand_e = nullptr;
   P.pred = nullptr;
   P.pred_items = 0;
+  P.fp64 = 0;
   if (c->n_elem == 0) {  // primitives only
     TraceArgs a;
     a.rays = rays_dev;

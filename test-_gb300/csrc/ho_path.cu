@@ -218,6 +218,7 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
     tot.prim_flops += st.prim_flops;
     tot.prim_kernel_ns += st.prim_kernel_ns;
     tot.prim_node_visits += st.prim_node_visits;
+    tot.fp64_polished += st.fp64_polished;
     tot.graph = st.graph;
     tot.max_modes = st.max_modes;
     tot.status |= st.status;

@@ -169,6 +169,7 @@ static int trace_hexes(ho_context* c, const TraceArgs& a, cudaStream_t s) {
   P.hits = a.hits;
   P.rgb = a.rgb;
   P.stats = c->d_stats;
+  P.fp64 = c->fp64_check ? 1 : 0;
   int64_t n_queries, n_threads;
   if (a.rays) {
     n_queries = a.n_rays * a.n_iso;

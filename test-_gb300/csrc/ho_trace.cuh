@@ -19,6 +19,7 @@
 #include <atomic>
 
 #include "ho_device.cuh"
+#include "ho_fp64.cuh"
 #include "ho_host.h"
 #include "ho_learn.h"
 
@@ -60,6 +61,7 @@ struct TraceParams {
   const float* desc;      // element descriptors (scale k at [45])
   const int32_t* cand_e;  // [item][kPredK] candidate elements the predictions belong to
   const float* pred;      // [item][kPredK][8] network outputs
+  int fp64;               // plain kernel: FP64 check + polish of every hit (HO_OPT_FP64_CHECK)
 };
 
 __device__ __forceinline__ bool key_less(float ta, int ea, float tb, int eb) {
@@ -478,8 +480,16 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
   if (active) query_ray(P, q, o, d, iso, iso_on);
   Work w;
   HitState best = miss_state();
-  if (active) best = plain_trace<N>(P, o, d, iso, iso_on, w);
+  bool polished = false;
+  if (active) {
+    best = plain_trace<N>(P, o, d, iso, iso_on, w);
+    // the FP64 check and polish of the engines' final pass; the plain solver
+    // is the fallback itself, so a failing hit is only flagged
+    if (P.fp64 && !fp64_check_polish<N>(P.rec, P.flags, o, d, iso, best, polished)) best.flags |= HO_FLAG_FP64_FAIL;
+  }
   flush_work(P.stats, w, active);
+  const unsigned pm = __ballot_sync(kFull, polished);
+  if ((threadIdx.x & 31) == 0 && pm) atomicAdd(&P.stats->c[ST_POLISHED], static_cast<unsigned long long>(__popc(pm)));
   if (active) write_result(P, q, d, best, w.newton + w.face);
 }
 

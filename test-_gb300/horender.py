@@ -71,7 +71,8 @@ class _Stats(C.Structure):
         ("fp64_failed", C.c_uint64), ("fp64_failed_after_fallback", C.c_uint64), ("round_flops", C.c_uint64),
         ("kernel_launches", C.c_uint64), ("round_kernel_ns", C.c_uint64), ("round_launches", C.c_uint64),
         ("tail_rays", C.c_uint64), ("prim_candidates", C.c_uint64), ("prim_iters", C.c_uint64),
-        ("prim_flops", C.c_uint64), ("prim_kernel_ns", C.c_uint64), ("prim_node_visits", C.c_uint64)]
+        ("prim_flops", C.c_uint64), ("prim_kernel_ns", C.c_uint64), ("prim_node_visits", C.c_uint64),
+        ("fp64_polished", C.c_uint64)]
 
 
 def _load():

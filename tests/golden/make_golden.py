@@ -15,7 +15,11 @@ Fixtures (all outputs are the reference's, computed in FP32 by its code):
   hex8_p6.npz     checksum of a seeded 8^3, P=6 scene (curving 0.08 h, 64
                   Gaussians, seed 2); 2048 traced rays, isovalues +-0.3.
   hex32_p6.npz    checksum of the seeded hex32_p6 scene (too large to store)
-                  + 192 traced rays per isovalue (+-0.3) through its cube.
+                  + 4096 rays through its cube traced at each isovalue
+                  (-0.3, 0.0, 0.3; 0.0 with FindIsosurfaceOnRayHex called,
+                  which the renderer skips at 0), with the visit order.
+  hex64_p5.npz    the same for hex64_p5 (64^3 hexes, P=5, iso 0.1), 2048
+                  rays.
 """
 from __future__ import annotations
 
@@ -32,7 +36,7 @@ sys.path.insert(0, str(ROOT / "tests"))
 sys.path.insert(0, str(ROOT / "test-_gb300"))
 
 import oracle_bind as ob  # noqa: E402
-import horender as hr  # noqa: E402
+import workloads as hr  # noqa: E402  (workload definitions; no product library)
 
 # The reference checkout is named by HORENDER_REFERENCE (its project root);
 # the fixtures that need the reference's own files are skipped without it.
@@ -42,14 +46,11 @@ ORDER_CAP = 32
 
 
 def scene_arrays(name=None, **synth):
-    ctx = hr.Context(0)
+    """A workload's scene from the oracle's generator (the same arrays the
+    product's ho_generate_synthetic makes; the tests check the digest)."""
     if name:
         synth = hr.WORKLOADS[name].synth()
-    ctx.generate_synthetic(**synth)
-    s = ctx.get_scene()
-    ctx.close()
-    return ob.SceneArrays(s["geom_modes"], s["geom_offsets"], s["geom"], s["field_modes"], s["field_offsets"],
-                          s["field"], s["corners"])
+    return ob.synth_scene(**synth)
 
 
 def digest(arrs: ob.SceneArrays) -> str:
@@ -174,11 +175,10 @@ def make_hex8():
     print("hex8_p6: kinds", np.bincount(payload["trace_p03"][:, 0].astype(int), minlength=3))
 
 
-def make_hex32():
-    arrs = scene_arrays("hex32_p6")
-    w = hr.WORKLOADS["hex32_p6"]
+def scene_box_rays(w, n, seed):
+    """n of the workload's pixel-centre rays that meet the scene box (the
+    others are trivially misses), drawn without replacement."""
     rays = ob.camera_rays(w.camera.lookfrom, w.camera.lookat, w.camera.vup, w.camera.vfov_deg, w.width, w.height)
-    # rays that meet the scene box (the others are trivially misses)
     o, d = rays[:, :3].astype(np.float64), rays[:, 3:].astype(np.float64)
     with np.errstate(divide="ignore", invalid="ignore"):
         t0 = (-0.01 - o) / d
@@ -186,20 +186,45 @@ def make_hex32():
     te = np.minimum(t0, t1).max(1)
     tx = np.maximum(t0, t1).min(1)
     inside = np.where(tx > te)[0]
-    rng = np.random.default_rng(404)
-    sub = rays[rng.choice(inside, 192, replace=False)]
+    rng = np.random.default_rng(seed)
+    return rays[np.sort(rng.choice(inside, n, replace=False))]
+
+
+def iso_tag(iso):
+    return ("m" if iso < 0 else "p") + f"{abs(iso):.1f}".replace(".", "")
+
+
+def make_workload_fixture(name, n_rays, seed, out):
+    """The reference's traces of n_rays rays at every isovalue of a workload,
+    with its visit order. Isovalue 0.0 is traced with the isosurface on
+    (FindIsosurfaceOnRayHex called at 0.0; the renderer would turn it off)."""
+    w = hr.WORKLOADS[name]
+    arrs = scene_arrays(name)
+    sub = scene_box_rays(w, n_rays, seed)
     rs = ob.RefScene(arrs)
     payload = {}
-    for tag, iso in (("m03", -0.3), ("p03", 0.3)):
-        tr, order, cnt = trace_fixture(rs, sub, iso)
+    for iso in w.isovalues:
+        tag = iso_tag(iso)
+        tr, order, cnt = rs.trace(sub, iso, order_cap=ORDER_CAP, iso_always=True)
+        assert cnt.max() <= ORDER_CAP, cnt.max()
         payload[f"trace_{tag}"], payload[f"order_{tag}"], payload[f"count_{tag}"] = tr, order, cnt
-    np.savez_compressed(HERE / "hex32_p6.npz", digest=np.array(digest(arrs)), rays=sub, **payload)
-    print("hex32_p6: kinds", np.bincount(payload["trace_p03"][:, 0].astype(int), minlength=3))
+        print(f"{name} iso {iso}: kinds {np.bincount(tr[:, 0].astype(int), minlength=3)}, most candidates {cnt.max()}",
+              flush=True)
+    np.savez_compressed(HERE / out, digest=np.array(digest(arrs)), rays=sub,
+                        isovalues=np.asarray(w.isovalues, np.float32), **payload)
+
+
+def make_hex32():
+    make_workload_fixture("hex32_p6", 4096, 404, "hex32_p6.npz")
+
+
+def make_hex64():
+    make_workload_fixture("hex64_p5", 2048, 505, "hex64_p5.npz")
 
 
 if __name__ == "__main__":
     if not ob.ref_available():
         sys.exit("oracle/_ref/libref.so is missing: run oracle/build_ref.sh in a checkout with the reference")
-    which = sys.argv[1:] or ["curvedface", "hex4", "hex8", "hex32"]
+    which = sys.argv[1:] or ["curvedface", "hex4", "hex8", "hex32", "hex64"]
     for w in which:
         globals()[f"make_{w}"]()

@@ -392,6 +392,7 @@ def ref():
         L.ref_hit_hex.argtypes = [vp, i32, vp, vp, i64, vp]
         L.ref_trace.argtypes = [vp, vp, i64, f32, vp]
         L.ref_trace_order.argtypes = [vp, vp, i64, f32, vp, vp, i32, vp]
+        L.ref_trace_order_iso.argtypes = [vp, vp, i64, f32, i32, vp, vp, i32, vp]
         _ref = L
     return _ref
 
@@ -487,17 +488,19 @@ class RefScene:
         ref().ref_hit_hex(self.h, elem, _p(rays), _p(seg), rays.shape[0], _p(out))
         return out
 
-    def trace(self, rays, iso, order_cap: int = 0):
+    def trace(self, rays, iso, order_cap: int = 0, iso_always: bool = False):
         """Reference traversal; returns (n x 12 results) or, with order_cap > 0,
-        (results, visit order n x order_cap, visit counts)."""
+        (results, visit order n x order_cap, visit counts). iso_always: call
+        FindIsosurfaceOnRayHex at every isovalue, 0.0 included (the renderer
+        turns the isosurface off at 0)."""
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
         out = np.zeros((rays.shape[0], 12), np.float32)
-        if order_cap <= 0:
-            ref().ref_trace(self.h, _p(rays), rays.shape[0], float(iso), _p(out))
-            return out
-        order = np.zeros((rays.shape[0], order_cap), np.int32)
+        order = np.zeros((rays.shape[0], max(order_cap, 1)), np.int32)
         cnt = np.zeros(rays.shape[0], np.int32)
-        ref().ref_trace_order(self.h, _p(rays), rays.shape[0], float(iso), _p(out), _p(order), order_cap, _p(cnt))
+        ref().ref_trace_order_iso(self.h, _p(rays), rays.shape[0], float(iso), int(iso_always), _p(out),
+                                  _p(order) if order_cap > 0 else None, order_cap, _p(cnt))
+        if order_cap <= 0:
+            return out
         return out, order, cnt
 
 

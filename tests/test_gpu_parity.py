@@ -227,7 +227,8 @@ def test_autotune_picks_a_candidate_and_keeps_results(small):
 def test_fp64_check_and_plain_fallback(small):
     """Every hit is re-evaluated in FP64; a hit that fails is traced again by
     the plain solver. With the check on, the rays that were re-traced equal
-    plain mode's answers and every other ray equals the unchecked answer."""
+    plain mode's answers and every other ray has the unchecked answer's
+    identity, with t, xi and u polished to the exact root."""
     ctx, w, arrs, osc = small
     W = H = 96
     ctx.set_mode(hr.MODE_BATCHED)
@@ -251,7 +252,10 @@ def test_fp64_check_and_plain_fallback(small):
     for k in ("kind", "elem", "face"):
         assert np.array_equal(h1[k][fb], hp[k][fb])
         assert np.array_equal(h1[k][~fb], h0[k][~fb])
-    assert np.array_equal(h1["t"][~fb], h0["t"][~fb])
+    # the check polishes the hits it passes: t moves by at most the solvers'
+    # tolerance, to the exact root (test_gpu_golden holds it to the judge)
+    assert np.abs(h1["t"][~fb] - h0["t"][~fb]).max() < 5e-4
+    assert s1["fp64_polished"] > 0.9 * s1["fp64_checked"]
     failed_final = (h1["flags"] & hr.FLAG_FP64_FAIL) != 0
     assert int(failed_final.sum()) == s1["fp64_failed_after_fallback"]
 

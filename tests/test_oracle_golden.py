@@ -49,8 +49,9 @@ def _ref_ids(tr):
     return tr[:, 0].astype(int), tr[:, 1].astype(int), tr[:, 2].astype(int)
 
 
-def _check_replay_bit_exact(osc, rays, iso, tr, order, cnt):
-    rep = osc.trace_replay(rays, iso, iso != 0.0, order, cnt, precision=32)
+def _check_replay_bit_exact(osc, rays, iso, tr, order, cnt, iso_on=None):
+    iso_on = iso != 0.0 if iso_on is None else iso_on
+    rep = osc.trace_replay(rays, iso, iso_on, order, cnt, precision=32)
     k, e, f = _ref_ids(tr)
     assert np.array_equal(rep["kind"], k) and np.array_equal(rep["elem"], e) and np.array_equal(rep["face"], f)
     hit = k > 0
@@ -59,8 +60,9 @@ def _check_replay_bit_exact(osc, rays, iso, tr, order, cnt):
     assert np.array_equal(rep["n"][hit].astype(np.float32), tr[hit, 7:10])
 
 
-def _check_ordered_policy(osc, rays, iso, tr, order, cnt, min_agree=0.995):
-    out, _ = osc.trace(rays, iso, iso != 0.0, precision=32)
+def _check_ordered_policy(osc, rays, iso, tr, order, cnt, min_agree=0.995, iso_on=None):
+    iso_on = iso != 0.0 if iso_on is None else iso_on
+    out, _ = osc.trace(rays, iso, iso_on, precision=32)
     k, e, f = _ref_ids(tr)
     same = (out["kind"] == k) & (out["elem"] == e) & (out["face"] == f)
     assert same.mean() >= min_agree, same.mean()
@@ -71,7 +73,7 @@ def _check_ordered_policy(osc, rays, iso, tr, order, cnt, min_agree=0.995):
     # order through the same per-candidate policy gives the reference's answer
     bad = np.where(~same)[0]
     if bad.size:
-        rep = osc.trace_replay(rays[bad], iso, iso != 0.0, order[bad], cnt[bad], precision=32)
+        rep = osc.trace_replay(rays[bad], iso, iso_on, order[bad], cnt[bad], precision=32)
         assert np.array_equal(rep["kind"], k[bad]) and np.array_equal(rep["elem"], e[bad])
     return same
 
@@ -164,17 +166,21 @@ def test_hex8_traces(oracle, name, synth):
         _check_ordered_policy(osc, z["rays"], iso, z[f"trace_{tag}"], z[f"order_{tag}"], z[f"count_{tag}"])
 
 
-def test_hex32_traces(oracle):
-    import horender as hr
+@pytest.mark.parametrize("name", ["hex32_p6", "hex64_p5"])
+def test_workload_traces(oracle, name):
+    """The benchmark workloads' fixtures (4096 / 2048 rays through the cube at
+    every isovalue, 0.0 with the isosurface on): the scene from the oracle's
+    generator has the fixture's digest; replaying the reference's visit order
+    reproduces every traced ray bit for bit; the product's ascending order
+    agrees on at least 98% of rays and every disagreement is the order."""
+    import workloads
 
-    path = GOLDEN / "hex32_p6.npz"
-    if not path.exists():
-        pytest.skip("hex32_p6 fixture not generated")
-    z = np.load(path)
-    arrs = _synth_arrays(**hr.WORKLOADS["hex32_p6"].synth())
+    z = np.load(GOLDEN / f"{name}.npz")
+    arrs = ob.synth_scene(**workloads.WORKLOADS[name].synth())
     assert _digest(arrs) == str(z["digest"])
     osc = ob.OracleScene(arrs)
-    for tag, iso in (("m03", -0.3), ("p03", 0.3)):
-        _check_replay_bit_exact(osc, z["rays"], iso, z[f"trace_{tag}"], z[f"order_{tag}"], z[f"count_{tag}"])
-        _check_ordered_policy(osc, z["rays"], iso, z[f"trace_{tag}"], z[f"order_{tag}"], z[f"count_{tag}"],
-                              min_agree=0.98)
+    for iso in [float(v) for v in z["isovalues"]]:
+        tag = ("m" if iso < 0 else "p") + f"{abs(iso):.1f}".replace(".", "")
+        args = (osc, z["rays"], iso, z[f"trace_{tag}"], z[f"order_{tag}"], z[f"count_{tag}"])
+        _check_replay_bit_exact(*args, iso_on=True)
+        _check_ordered_policy(*args, min_agree=0.98, iso_on=True)
