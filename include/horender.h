@@ -223,7 +223,8 @@ int ho_get_prim_boxes(ho_context* ctx, float* out);
  * corners: n*8*3 floats (XML vertex order); geom_modes / field_modes: n*3;
  * geom_offsets[i]: float index of element i's x block in geom (y, z blocks
  * follow, each nx*ny*nz floats), -1 = trilinear from corners;
- * field_offsets[i]: float index into field, -1 = no field. */
+ * field_offsets[i]: float index into field, -1 = no field. HO_ERR_ARG for a
+ * NaN or infinite corner or coefficient (nothing is added). */
 int ho_add_hexes(ho_context* ctx, int64_t n, const float* corners, const uint32_t* geom_modes,
                  const float* geom, int64_t geom_len, const int64_t* geom_offsets,
                  const uint32_t* field_modes, const float* field, int64_t field_len,

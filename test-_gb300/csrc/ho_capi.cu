@@ -254,6 +254,14 @@ void ho_destroy(ho_context* c) {
 
 const char* ho_last_error(const ho_context* c) { return c ? c->err.c_str() : "null context"; }
 
+// Every value finite (a NaN or infinite coordinate or coefficient would reach
+// the solvers as a NaN iterate; it is refused at the door instead).
+static bool all_finite(const float* v, int64_t n) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
 int ho_add_hexes(ho_context* c, int64_t n, const float* corners, const uint32_t* gm, const float* geom,
                  int64_t geom_len, const int64_t* goff, const uint32_t* fm, const float* field, int64_t field_len,
                  const int64_t* foff) {
@@ -272,7 +280,11 @@ int ho_add_hexes(ho_context* c, int64_t n, const float* corners, const uint32_t*
       }
       if (!geom || goff[i] + 3 * cnt > geom_len)
         return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": geometry coefficients out of range");
+      if (!all_finite(geom + goff[i], 3 * cnt))
+        return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": non-finite geometry coefficient");
     }
+    if (!all_finite(corners + 24 * i, 24))
+      return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": non-finite corner");
     if (foff[i] >= 0) {
       int64_t cnt = 1;
       for (int a = 0; a < 3; ++a) {
@@ -282,6 +294,8 @@ int ho_add_hexes(ho_context* c, int64_t n, const float* corners, const uint32_t*
       }
       if (!field || foff[i] + cnt > field_len)
         return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": field coefficients out of range");
+      if (!all_finite(field + foff[i], cnt))
+        return fail(c, HO_ERR_ARG, "element " + std::to_string(i) + ": non-finite field coefficient");
     }
   }
   for (int64_t i = 0; i < n; ++i) {
@@ -342,7 +356,11 @@ int add_prims(ho_context* c, int kind, int nv, int dims, int64_t n, const float*
           return fail(c, HO_ERR_RANGE, "primitive " + std::to_string(i) + ": geometry modes must be in [1, 9]");
       if (!geom || goff[i] + 3 * prim_block_len(kind, m) > geom_len)
         return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": geometry coefficients out of range");
+      if (!all_finite(geom + goff[i], 3 * prim_block_len(kind, m)))
+        return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": non-finite geometry coefficient");
     }
+    if (!all_finite(verts + static_cast<int64_t>(nv) * 3 * i, nv * 3))
+      return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": non-finite vertex");
     if (foff[i] >= 0) {
       modes(fm, i, m);
       for (int a = 0; a < dims; ++a)
@@ -350,6 +368,8 @@ int add_prims(ho_context* c, int kind, int nv, int dims, int64_t n, const float*
           return fail(c, HO_ERR_RANGE, "primitive " + std::to_string(i) + ": field modes must be in [1, 9]");
       if (!field || foff[i] + prim_block_len(kind, m) > field_len)
         return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": field coefficients out of range");
+      if (!all_finite(field + foff[i], prim_block_len(kind, m)))
+        return fail(c, HO_ERR_ARG, "primitive " + std::to_string(i) + ": non-finite field coefficient");
     }
   }
   for (int64_t i = 0; i < n; ++i) {

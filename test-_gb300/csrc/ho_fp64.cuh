@@ -23,8 +23,9 @@
 // element, face and kind; t, xi and u move to the root of the same equations,
 // which leaves t within FP32 rounding of the exact root. A step in t larger
 // than 1e-3 or in xi larger than 0.05, a non-finite one, or one that takes a
-// face hit's free coordinates out of [-1.001, 1.001] leaves the hit as the
-// solver returned it.
+// face hit's free coordinates beyond 1.05 in magnitude (the reference
+// accepts up to 1.001, and an accepted hit's exact root can lie a little
+// further out) leaves the hit as the solver returned it.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -262,7 +263,9 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
     float val;
     face_param(h.face, fixed, val, ua, va);
     const double pu = ua == 0 ? x0 : (ua == 1 ? x1 : x2), pv = va == 0 ? x0 : (va == 1 ? x1 : x2);
-    if (!(fabs(pu) <= 1.001 && fabs(pv) <= 1.001)) return true;
+    // the reference accepts a face hit up to 1.001 in its free coordinates;
+    // the exact root of an accepted hit can lie a little further out
+    if (!(fabs(pu) <= 1.05 && fabs(pv) <= 1.05)) return true;
   }
   h.t = static_cast<float>(t);
   h.xi = make_float3(static_cast<float>(x0), static_cast<float>(x1), static_cast<float>(x2));

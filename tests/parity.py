@@ -74,7 +74,7 @@ def _varies(hits, base_ids, n) -> np.ndarray:
     return ~np.all(ids(hits).reshape(n, N_NUDGE, 3) == base_ids[:, None, :], axis=(1, 2))
 
 
-def classify(gpu, ora, rays, osc, iso, product_trace=None) -> dict:
+def classify(gpu, ora, rays, osc, iso, product_trace=None, iso_on=True) -> dict:
     """Classes of the identity differences between gpu (product hits) and ora
     (the oracle's or the reference's hits on the same rays at isovalue iso).
     product_trace(rays) -> product hits, optional: lets the product's own
@@ -98,11 +98,11 @@ def classify(gpu, ora, rays, osc, iso, product_trace=None) -> dict:
     if rest.size:
         rr = r[rest]
         nr = nudged(rr)
-        b32, _ = osc.trace(rr, iso, True, precision=32)
-        b64, _ = osc.trace(rr, iso, True, precision=64)
+        b32, _ = osc.trace(rr, iso, iso_on, precision=32)
+        b64, _ = osc.trace(rr, iso, iso_on, precision=64)
         varies = ~same_ids(b32, b64)
         for prec, base in ((64, ids(b64)), (32, ids(b32))):
-            hn, _ = osc.trace(nr, iso, True, precision=prec)
+            hn, _ = osc.trace(nr, iso, iso_on, precision=prec)
             varies |= _varies(hn, base, rest.size)
         if product_trace is not None:
             varies |= _varies(product_trace(nr), ids(g[rest]), rest.size)
@@ -137,3 +137,31 @@ def errors(gpu, judge, rays, h: float) -> dict:
                     "xi_p99": float(np.quantile(dxi, .99)), "u_max": float(du.max()),
                     "u_p99": float(np.quantile(du, .99))}
     return res
+
+
+POS_TOL = 1e-5    # hit position error bound, in element sizes
+XI_TOL = 1e-5
+U_TOL = 1e-5
+
+
+def check_against_oracle(gpu, rays, osc, iso, iso_on, h, product_trace=None, label=""):
+    """The product's hits on given rays against the FP64 oracle: every
+    identity difference classified (no 'other'), and t / xi / u of the
+    agreeing hits within POS_TOL * h / XI_TOL / U_TOL of the judge (the
+    oracle's hits polished to exact roots). Returns the class counts."""
+    ref, _ = osc.trace(rays, iso, iso_on, precision=64)
+    c = classify(gpu, ref, rays, osc, iso, product_trace=product_trace, iso_on=iso_on)
+    cnt = counts(c)
+    print(f"{label}: {cnt}")
+    for i in c["other"][:5]:
+        print("   other", i, gpu[i][["kind", "elem", "face", "t"]], ref[i][["kind", "elem", "face", "t"]])
+    assert c["other"].size == 0, cnt
+    judge = osc.polish(rays, ref, iso)
+    err = errors(gpu, judge, rays, h)
+    print(f"   errors vs FP64 judge: {err}")
+    for lab, e in err.items():
+        if e["n"]:
+            assert e["t_max_over_h"] <= POS_TOL, (lab, e)
+            assert e["xi_max"] <= XI_TOL, (lab, e)
+            assert e["u_max"] <= U_TOL, (lab, e)
+    return cnt

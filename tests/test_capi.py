@@ -81,6 +81,30 @@ def test_add_hexes_validation_leaves_scene_unchanged():
         assert np.array_equal(s2["geom"][: s["geom"].size], s["geom"])
 
 
+@pytest.mark.parametrize("where", ["corner", "geom", "field"])
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_non_finite_inputs_refused(where, bad):
+    """A NaN or infinite corner or coefficient is refused with HO_ERR_ARG and
+    the scene is left as it was (it would otherwise reach the solvers as a NaN
+    iterate); the same for a primitive's vertex."""
+    with hr.Context(0) as ctx:
+        ctx.generate_synthetic(1, 1, 1, 2, 2, 0.0, 1, 1)
+        s = ctx.get_scene()
+        arr = {"corner": s["corners"].copy(), "geom": s["geom"].copy(), "field": s["field"].copy()}
+        arr[where].reshape(-1)[3] = bad
+        with pytest.raises(hr.HoError) as ei:
+            ctx.add_hexes(arr["corner"], s["geom_modes"], arr["geom"], s["geom_offsets"], s["field_modes"],
+                          arr["field"], s["field_offsets"])
+        assert ei.value.code == -1 and "non-finite" in str(ei.value)
+        assert ctx.info()["n_elem"] == 1
+        verts = np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]]], np.float32)
+        verts[0, 2, 1] = bad
+        with pytest.raises(hr.HoError) as ei:
+            ctx.add_quads(verts, np.zeros((1, 2), np.uint32), np.zeros(0, np.float32), np.array([-1]),
+                          np.zeros((1, 2), np.uint32), np.zeros(0, np.float32), np.array([-1]))
+        assert ei.value.code == -1 and ctx.info()["n_quads"] == 0
+
+
 def test_trilinear_elements_accepted():
     with hr.Context(0) as ctx:
         corners = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]],

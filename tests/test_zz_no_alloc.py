@@ -5,8 +5,10 @@ device-wide synchronisation). Its scratch is a fixed device array for at most
 HO_NOALLOC_MAX_RAYS rays per call.
 
 Checked through the C ABI against the regular entry point, on two calls in a
-row, with the tolerance the other GPU tests use (hit identity on >= 99.9% of
-rays, t within 2e-4); the second call takes no device memory; a call over the
+row (hit identity on >= 99.9% of rays; t within 5e-4: the regular entry
+point polishes its hits to the exact roots in FP64, this one returns the
+solvers' own answers, which stop at a face residual of 1e-4); the second call
+takes no device memory; a call over the
 limit is refused with HO_ERR_RANGE; no ray reports an incomplete tree walk.
 A second case puts prisms, quads and triangles beside the hexahedra, so the
 call's primitive pass runs after its hexahedron kernels. This file sorts last
@@ -50,7 +52,7 @@ def test_noalloc_matches_regular_entry_point_on_two_calls():
         same = (got["kind"] == ref["kind"]) & (got["elem"] == ref["elem"]) & (got["face"] == ref["face"])
         assert same.mean() >= 0.999, (call, same.mean())
         hit = same & (ref["kind"] > 0)
-        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 2e-4, call
+        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 5e-4, call
         assert (ref["kind"] > 0).sum() > 1000
         assert not (got["flags"] & hr.FLAG_INCOMPLETE).any()
         free.append(torch.cuda.mem_get_info()[0])
@@ -96,6 +98,6 @@ def test_noalloc_hexahedra_with_primitives():
         same = (got["kind"] == ref["kind"]) & (got["elem"] == ref["elem"]) & (got["face"] == ref["face"])
         assert same.mean() >= 0.999, (call, same.mean())
         hit = same & (ref["kind"] > 0)
-        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 2e-4, call
+        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 5e-4, call
         assert not (got["flags"] & hr.FLAG_INCOMPLETE).any()
     ctx.close()
