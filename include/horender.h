@@ -378,6 +378,12 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     without a device). Both fit in FP64 in the same order.
  * HO_OPT_LAST_FIT_GPU (read only) 1 when the last ho_load_xml_fld fitted on
  *                     the GPU.
+ * HO_OPT_WARM_CAP     learned mode, round kernel: Newton iterations a
+ *                     network-started inverse map may take before it restarts
+ *                     cold (default 4, 1..50). Any value gives the same
+ *                     answers (the cold restart is the plain solver); it
+ *                     trades iterations of failing warm starts against cold
+ *                     restarts.
  * HO_OPT_TIME_ROUNDS  0 (default); 1: a pair of CUDA events brackets each
  *                     round's intersection launches (event nodes of the graph)
  *                     and ho_stats.round_kernel_ns / round_launches report
@@ -392,6 +398,7 @@ int ho_set_mode(ho_context* ctx, int mode);
 #define HO_OPT_TAIL 7
 #define HO_OPT_GPU_FIT 8
 #define HO_OPT_LAST_FIT_GPU 9
+#define HO_OPT_WARM_CAP 10
 int ho_set_option(ho_context* ctx, int option, int64_t value);
 /* Path tracing with Lambertian bounces (replaces: render_kernel at spp
  * samples and depth max_depth, FEM-AABB/raytracer.cu:410-476, with

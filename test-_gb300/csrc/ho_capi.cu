@@ -946,6 +946,10 @@ int ho_set_option(ho_context* c, int option, int64_t value) {
       if (value < -1 || value > 1) return fail(c, HO_ERR_RANGE, "HO_OPT_GPU_FIT takes -1, 0 or 1");
       c->gpu_fit = static_cast<int>(value);
       return HO_OK;
+    case HO_OPT_WARM_CAP:
+      if (value < 1 || value > 50) return fail(c, HO_ERR_RANGE, "HO_OPT_WARM_CAP must be in [1, 50]");
+      c->warm_cap = static_cast<int>(value);
+      return HO_OK;
     default:
       return fail(c, HO_ERR_ARG, "unknown option " + std::to_string(option));
   }
@@ -962,6 +966,7 @@ int ho_get_option(ho_context* c, int option, int64_t* value) {
     case HO_OPT_GPU_FIT: *value = c->gpu_fit; return HO_OK;
     case HO_OPT_LAST_FIT_GPU: *value = c->last_fit_gpu ? 1 : 0; return HO_OK;
     case HO_OPT_ROUNDS: *value = c->round_count; return HO_OK;
+    case HO_OPT_WARM_CAP: *value = c->warm_cap; return HO_OK;
     case HO_OPT_ROUND_CHUNK:
       *value = c->round_chunk > 0 ? c->round_chunk : ho::round_batch_default(c->N > 0 ? c->N : 2, c->use_tc);
       return HO_OK;

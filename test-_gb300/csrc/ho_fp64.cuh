@@ -17,12 +17,12 @@
 //   isosurface:  x(xi) = o + t d and u(xi) = iso (unknowns: xi and t), a
 //                4x4 solve through J^-1.
 // The step's error is quadratic in its size plus the FP32 Jacobian's
-// relative error times its size, so from a residual of 1e-4 it lands within
-// about 1e-8; a step larger than that is followed by up to two more with the
-// residual re-evaluated in FP64 and the same Jacobian. The hit keeps its
+// relative error times its size, so from a residual of 1e-4 it usually lands
+// within about 1e-8; a larger step is followed by up to three more with the
+// residual re-evaluated in FP64 (kPolishSteps). The hit keeps its
 // element, face and kind; t, xi and u move to the root of the same equations,
 // which leaves t within FP32 rounding of the exact root. A step in t larger
-// than 1e-3 or in xi larger than 0.05, a non-finite one, or one that takes a
+// than 2e-2 or in xi larger than 0.25, a non-finite one, or one that takes a
 // face hit's free coordinates beyond 1.05 in magnitude (the reference
 // accepts up to 1.001, and an accepted hit's exact root can lie a little
 // further out) leaves the hit as the solver returned it.
@@ -161,10 +161,11 @@ __device__ void fp64_residuals(const float* __restrict__ rec_all, int elem, floa
 }
 
 // Newton steps of the polish at most: the first uses the FP64 residual of the
-// check; each later one re-evaluates it at the new point and keeps the first
-// step's FP32 Jacobian (a chord step, whose error shrinks by about the
-// relative change of J across the first step).
-constexpr int kPolishSteps = 3;
+// check; each later one re-evaluates it at the new point, and also the FP32
+// Jacobian when the step before moved xi by more than 1e-3 (otherwise it
+// keeps the previous one: a chord step, whose error shrinks by about the
+// relative change of J across that step).
+constexpr int kPolishSteps = 4;
 
 // One Newton step on a hit's defining equations (file header): from the
 // FP64 residual r and field value u at (t, xi), with the FP32 Jacobian J and
@@ -208,10 +209,11 @@ __device__ __forceinline__ bool polish_step(const HitState& h, float3 d, float i
     dt = (-(u - static_cast<double>(iso)) - (g.x * a[0] + g.y * a[1] + g.z * a[2])) / gb;
     for (int k = 0; k < 3; ++k) dx[k] = a[k] + b[k] * dt;
   }
-  // a face hit accepted at a residual of 1e-4 is up to about 1e-4 / |J| off
-  // in xi (|J| is about half the element size): the limits leave room for that
+  // a face hit accepted at a residual of 1e-4 is up to about 1e-4 / |d.n|
+  // off in t and that over |J| (about half the element size) in xi, which on
+  // near-grazing rays reaches 1e-2 and 0.2: the limits leave room for that
   const double mx = fmax(fabs(dx[0]), fmax(fabs(dx[1]), fabs(dx[2])));
-  return fabs(dt) <= 1e-3 && mx <= 0.05;  // also false for a NaN step
+  return fabs(dt) <= 2e-2 && mx <= 0.25;  // also false for a NaN step
 }
 
 // The FP64 check of a hit (a miss always passes) and, when it passes, the
@@ -234,15 +236,21 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
   }
   // FP32 Jacobian and field gradient at the hit
   const CoefRef<false> c{rec_all + static_cast<int64_t>(h.elem) * record_floats(N)};
-  float xJ[12];
-  geom_eval_raw<N, false>(c, h.xi, xJ);
-  const float J[9] = {xJ[1], xJ[2], xJ[3], xJ[5], xJ[6], xJ[7], xJ[9], xJ[10], xJ[11]};
+  float J[9];
   float3 g = make_float3(0.f, 0.f, 0.f);
-  if (has_field) {
-    float ug[4];
-    field_eval_raw<N, false>(c.at(3 * block_floats(N)), h.xi, ug);
-    g = make_float3(ug[1], ug[2], ug[3]);
-  }
+  auto jacobian_at = [&](float3 xi) {
+    float xJ[12];
+    geom_eval_raw<N, false>(c, xi, xJ);
+    J[0] = xJ[1]; J[1] = xJ[2]; J[2] = xJ[3];
+    J[3] = xJ[5]; J[4] = xJ[6]; J[5] = xJ[7];
+    J[6] = xJ[9]; J[7] = xJ[10]; J[8] = xJ[11];
+    if (has_field) {
+      float ug[4];
+      field_eval_raw<N, false>(c.at(3 * block_floats(N)), xi, ug);
+      g = make_float3(ug[1], ug[2], ug[3]);
+    }
+  };
+  jacobian_at(h.xi);
   double t = h.t, x0 = h.xi.x, x1 = h.xi.y, x2 = h.xi.z, un = u;
   for (int step = 0; step < kPolishSteps; ++step) {
     double dx[3], dt;
@@ -255,6 +263,8 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
     // a step this small leaves an error far below FP32 rounding of t and xi
     const double mx = fmax(fabs(dx[0]), fmax(fabs(dx[1]), fabs(dx[2])));
     if (step + 1 == kPolishSteps || (mx <= 1e-5 && fabs(dt) <= 1e-7)) break;
+    if (mx > 1e-3)
+      jacobian_at(make_float3(static_cast<float>(x0), static_cast<float>(x1), static_cast<float>(x2)));
     fp64_residual_vec<N>(rec_all, h.elem, o, d, t, x0, x1, x2, has_field, r, u);
     un = u;
   }

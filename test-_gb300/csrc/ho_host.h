@@ -215,6 +215,7 @@ struct ho_context {
   ho::RoundBufs rounds;
   // batched / learned engine options (ho_set_option)
   int round_chunk = 0;       // pairs per element batch (0: the kernel's pair slots)
+  int warm_cap = 4;          // round kernel: iterations of a warm-started solve before its cold restart
   int round_count = 16;      // rounds enqueued before the completion check (at most)
   int tail_after = 4;        // rounds before the warp-per-ray tail finishes every ray (0: no tail)
   int gpu_fit = -1;          // loader's modal fit: -1 on the GPU when one is present, 0 host, 1 GPU

@@ -320,6 +320,7 @@ static RoundParams round_params(ho_context* c, const TraceParams& P) {
   R.cand_e = P.cand_e;
   R.pred = P.pred;
   R.pred_items = P.pred_items;
+  R.warm_cap = c->warm_cap;
   return R;
 }
 

@@ -108,6 +108,7 @@ struct RoundParams {
   const int32_t* cand_e;
   const float* pred;
   unsigned pred_items;
+  int warm_cap;  // iterations of a warm-started solve before its cold restart
 };
 
 // Task word: kind (3 bits) | pair (5 bits) | argument (8 bits).
@@ -126,7 +127,6 @@ struct PairSm {
   int fl;        // bit 0 has field, 1 iso on, 2 prediction available, 3 a warm start was rejected
   int pend;      // tasks of the current phase still running
   uint32_t okm;  // samples that converged
-  uint32_t donem;  // learned pairs: samples finished (converged or not), for the sample waves
   // result under construction
   float ht, hx[3], hg[3];
   int hface;
@@ -209,43 +209,14 @@ __device__ __forceinline__ void push_task(unsigned* tail, uint16_t* ring, int ca
   ring[s % cap] = static_cast<uint16_t>(w);
 }
 
-// Learned pairs take their 17 isosurface samples in three waves. Samples 0,
-// 4, 8, 12 and 16 start from the network's prediction; sample i = 2 mod 4
-// from the midpoint of the converged samples i - 2 and i + 2; an odd sample
-// from the midpoint of its converged neighbours i - 1 and i + 1 (the network's
-// prediction where a neighbour did not converge). Midpoints of converged
-// neighbours are within about (segment / 16)^2 |xi''| / 2 of the sample's
-// root, so most later-wave solves converge in two iterations. Every sample
-// still converges by the reference's rule (step below 1e-5) or restarts cold,
-// so the samples, and the bracket taken from them, are the same.
-constexpr int kWaveA = 5;
-
-// A sample of a learned pair finished: queue each later-wave sample whose two
-// neighbours have now both finished (the lane that finishes the second
-// neighbour sees both bits and queues it, exactly once).
-template <int N, class WS>
-__device__ __forceinline__ void sample_waves(WS& W, int pp, int i) {
-  constexpr int R = RoundCfg<N>::Ring;
-  PairSm& p = W.pr[pp];
-  const uint32_t done = atomicOr(&p.donem, 1u << i) | (1u << i);
-  const int nc = (i & 3) == 0 ? 4 : ((i & 1) == 0 ? 2 : 0);  // wave A: 4 children, B: 2, C: none
-  for (int k = 0; k < nc; ++k) {
-    const int c = i + (k == 0 ? -1 : (k == 1 ? 1 : (k == 2 ? -2 : 2)));
-    if (c < 0 || c >= kSamples) continue;
-    const int st = (c & 1) ? 1 : 2;
-    if (((done >> (c - st)) & 1u) && ((done >> (c + st)) & 1u))
-      push_task(&W.tail, W.ring, R, task_word(TK_SAMPLE, pp, c));
-  }
-}
-
 // Start an inverse-map solve of f(t) at t from xi0 (warm: capped, with a cold
 // restart on failure).
-__device__ __forceinline__ void start_sample_solve(LaneSolve& s, float t, bool warm, float3 xi0) {
+__device__ __forceinline__ void start_sample_solve(LaneSolve& s, float t, bool warm, float3 xi0, int warm_cap) {
   s.t = t;
   s.warm = warm;
   s.xi = warm ? xi0 : make_float3(0.f, 0.f, 0.f);
   s.it = 0;
-  s.cap = warm ? kWarmCap : 50;
+  s.cap = warm ? warm_cap : 50;
   s.post = false;
 }
 
@@ -389,7 +360,7 @@ __device__ __forceinline__ void face_phase(WS& W, int pp, const float* __restric
 
 // Begin a popped task.
 template <int N, bool L, class WS>
-__device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s) {
+__device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s, int warm_cap) {
   s.task = static_cast<int>(tw);
   s.kind = static_cast<int>(tw >> 13);
   s.pp = static_cast<int>((tw >> 8) & 31u);
@@ -404,18 +375,7 @@ __device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s) {
   if (s.kind == TK_SAMPLE) {
     const float t = p.te + (p.tx - p.te) * (float(s.arg) / 16.0f);
     const bool warm = L && (p.fl & 4);
-    float3 xi0 = make_float3(0.f, 0.f, 0.f);
-    if (warm) {
-      xi0 = pair_pred<N>(p).at(t);
-      const int i = s.arg;
-      if (i & 3) {  // a later wave: the midpoint of its converged neighbours
-        const int st = (i & 1) ? 1 : 2;
-        const uint32_t ok = p.okm;
-        if (((ok >> (i - st)) & 1u) && ((ok >> (i + st)) & 1u))
-          xi0 = lerp3(ld3(p.sx[i - st]), ld3(p.sx[i + st]), 0.5f);
-      }
-    }
-    start_sample_solve(s, t, warm, xi0);
+    start_sample_solve(s, t, warm, warm ? pair_pred<N>(p).at(t) : make_float3(0.f, 0.f, 0.f), warm_cap);
   } else if (s.kind == TK_FSEED) {
     const int f = s.arg / 9, sd = s.arg - 9 * f;
     int fixed, ua, va;
@@ -441,7 +401,7 @@ __device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s) {
     s.xi = p0;
     s.t = tau0;
     s.it = 0;
-    s.cap = kWarmCap;
+    s.cap = warm_cap;
     s.warm = true;
     s.post = false;
     s.inited = true;
@@ -498,15 +458,8 @@ __device__ __noinline__ int admit_pair(WS* Wp, const RoundParams* P, int slot, R
   p.its = 0;
   if ((fl & 3) == 3) {
     p.pend = kSamples;
-    p.donem = 0u;
-    if (L && (fl & 4)) {  // learned: the first wave only (sample_waves)
-      const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kWaveA));
-      for (int i = 0; i < kWaveA; ++i)
-        W.ring[(base + i) % R] = static_cast<uint16_t>(task_word(TK_SAMPLE, slot, 4 * i));
-    } else {
-      const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kSamples));
-      for (int i = 0; i < kSamples; ++i) W.ring[(base + i) % R] = static_cast<uint16_t>(task_word(TK_SAMPLE, slot, i));
-    }
+    const unsigned base = atomicAdd(&W.tail, static_cast<unsigned>(kSamples));
+    for (int i = 0; i < kSamples; ++i) W.ring[(base + i) % R] = static_cast<uint16_t>(task_word(TK_SAMPLE, slot, i));
     return 0;
   }
   return start_faces<N, L>(Wp, slot, fbox, P);
@@ -683,7 +636,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
         }
       }
       const unsigned rank = __popc(idle & ((1u << lane) - 1u));
-      if (s.task < 0 && rank < avail) begin_task<N, L>(W, W.ring[(head + rank) % R], s);
+      if (s.task < 0 && rank < avail) begin_task<N, L>(W, W.ring[(head + rank) % R], s, P.warm_cap);
       __syncwarp();
       if (lane == 0) {
         W.head = head + min(avail, static_cast<unsigned>(__popc(idle)));
@@ -891,7 +844,6 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
         const bool warm_pair = L && (p.fl & 4);
         s.task = -1;
         if (s.kind == TK_SAMPLE) {
-          if (warm_pair) sample_waves<N>(W, pp, s.arg);
           if (atomicSub(&p.pend, 1) == 1) {
             // all 17 samples done: first sign change between consecutive good samples
             int prev = -1, found = -1;
@@ -921,7 +873,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
               s.task = 0;
               s.kind = TK_REFINE;
               s.pp = pp;
-              start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f));
+              start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f), P.warm_cap);
             } else {
               face_phase<N, L>(W, pp, fbox, &P, w, s);
             }
@@ -943,7 +895,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
               p.ct = ct;
               p.rstage = 1;
               s.task = 0;
-              start_sample_solve(s, ct, warm_pair, s.xi);
+              start_sample_solve(s, ct, warm_pair, s.xi, P.warm_cap);
             }
           } else {  // Newton candidate solve ended
             float ct = p.ct, csf;
@@ -983,7 +935,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
                 p.mt = 0.5f * (p.rlt + p.rrt);
                 p.rstage = 0;
                 s.task = 0;
-                start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f));
+                start_sample_solve(s, p.mt, warm_pair, lerp3(ld3(p.lsx), ld3(p.rxi), 0.5f), P.warm_cap);
               }
             }
             if (found) {  // the field value at the root's xi, then the hit

@@ -26,7 +26,7 @@ ERRORS = {-1: "HO_ERR_ARG", -2: "HO_ERR_CUDA", -3: "HO_ERR_STATE", -4: "HO_ERR_I
           -6: "HO_ERR_NOMEM", -7: "HO_ERR_RANGE", -8: "HO_ERR_DEVICE"}
 MODE_PLAIN, MODE_LEARNED, MODE_BATCHED = 0, 1, 2
 OPT_GRAPH, OPT_ROUNDS, OPT_ROUND_CHUNK, OPT_FP64_CHECK, OPT_TIME_ROUNDS, OPT_TENSOR, OPT_TAIL = 1, 2, 3, 4, 5, 6, 7
-OPT_GPU_FIT, OPT_LAST_FIT_GPU = 8, 9
+OPT_GPU_FIT, OPT_LAST_FIT_GPU, OPT_WARM_CAP = 8, 9, 10
 MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2

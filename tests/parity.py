@@ -48,6 +48,18 @@ def same_ids(a, b) -> np.ndarray:
     return np.all(ids(a) == ids(b), axis=1)
 
 
+ROOT_T = 1e-3     # two hits of the same element and face further apart than this are different roots
+
+
+def same_hit(gpu, ref, judge=None) -> np.ndarray:
+    """Same kind, element and face and, for hits, the same root: within
+    ROOT_T of the judge's t (the reference's own t where no judge is given)."""
+    s = same_ids(gpu, ref)
+    t_ref = np.asarray((judge if judge is not None else ref)["t"], np.float64)
+    near = np.abs(np.asarray(gpu["t"], np.float64) - t_ref) <= ROOT_T
+    return s & ((np.asarray(ref["kind"]) == 0) | near)
+
+
 def nudged(rays: np.ndarray) -> np.ndarray:
     """Copies of each ray with the direction turned by NUDGE_ANGLES radians
     towards 8 fixed directions of the plane normal to it (the origin kept):
@@ -74,13 +86,15 @@ def _varies(hits, base_ids, n) -> np.ndarray:
     return ~np.all(ids(hits).reshape(n, N_NUDGE, 3) == base_ids[:, None, :], axis=(1, 2))
 
 
-def classify(gpu, ora, rays, osc, iso, product_trace=None, iso_on=True) -> dict:
+def classify(gpu, ora, rays, osc, iso, product_trace=None, iso_on=True, judge=None) -> dict:
     """Classes of the identity differences between gpu (product hits) and ora
-    (the oracle's or the reference's hits on the same rays at isovalue iso).
-    product_trace(rays) -> product hits, optional: lets the product's own
-    answer under the nudges count for 'unstable'. Returns the number of rays,
-    of differing rays, and the indices of the differing rays per class."""
-    diff = np.where(~same_ids(gpu, ora))[0]
+    (the oracle's or the reference's hits on the same rays at isovalue iso):
+    a different kind, element or face, or the same ones at a different root
+    (same_hit; judge: ora's hits polished, if available). product_trace(rays)
+    -> product hits, optional: lets the product's own answer under the nudges
+    count for 'unstable'. Returns the number of rays, of differing rays, and
+    the indices of the differing rays per class."""
+    diff = np.where(~same_hit(gpu, ora, judge))[0]
     out = {"rays": int(len(ora)), "differ": int(diff.size)}
     for k in CLASSES:
         out[k] = np.zeros(0, np.int64)
@@ -100,7 +114,7 @@ def classify(gpu, ora, rays, osc, iso, product_trace=None, iso_on=True) -> dict:
         nr = nudged(rr)
         b32, _ = osc.trace(rr, iso, iso_on, precision=32)
         b64, _ = osc.trace(rr, iso, iso_on, precision=64)
-        varies = ~same_ids(b32, b64)
+        varies = ~same_hit(b32, b64)
         for prec, base in ((64, ids(b64)), (32, ids(b32))):
             hn, _ = osc.trace(nr, iso, iso_on, precision=prec)
             varies |= _varies(hn, base, rest.size)
@@ -122,7 +136,7 @@ def errors(gpu, judge, rays, h: float) -> dict:
     identity agrees and whose judge polish converged (judge['pad'] == 1).
     t (= the position along the unit ray) in units of the element size h; xi
     and u absolute."""
-    ok = same_ids(gpu, judge) & (judge["kind"] > 0) & (judge["pad"] == 1)
+    ok = same_hit(gpu, judge, judge) & (judge["kind"] > 0) & (judge["pad"] == 1)
     res = {}
     for kind, lab in ((1, "face"), (2, "iso")):
         m = ok & (gpu["kind"] == kind)
@@ -130,17 +144,24 @@ def errors(gpu, judge, rays, h: float) -> dict:
             res[lab] = {"n": 0}
             continue
         dt = np.abs(gpu["t"][m].astype(np.float64) - judge["t"][m])
-        dxi = np.abs(np.asarray(gpu["xi"][m], np.float64) - judge["xi"][m]).max(1)
-        du = np.abs(gpu["u"][m].astype(np.float64) - judge["u"][m])
+        # xi and u where both preimages lie in the padded element (|xi| <= 1.5):
+        # beyond it the map need not be one to one, and the same point can
+        # have another preimage (and field value) there
+        gx, jx = np.asarray(gpu["xi"][m], np.float64), np.asarray(judge["xi"][m], np.float64)
+        inside = (np.abs(gx).max(1) <= 1.5) & (np.abs(jx).max(1) <= 1.5)
+        dxi = np.abs(gx - jx).max(1)[inside]
+        du = np.abs(gpu["u"][m].astype(np.float64) - judge["u"][m])[inside]
+        if not inside.any():
+            dxi = du = np.zeros(1)
         res[lab] = {"n": int(m.sum()), "t_max_over_h": float(dt.max() / h),
                     "t_p99_over_h": float(np.quantile(dt, .99) / h), "xi_max": float(dxi.max()),
                     "xi_p99": float(np.quantile(dxi, .99)), "u_max": float(du.max()),
-                    "u_p99": float(np.quantile(du, .99))}
+                    "u_p99": float(np.quantile(du, .99)), "other_preimage": int((~inside).sum())}
     return res
 
 
 POS_TOL = 1e-5    # hit position error bound, in element sizes
-XI_TOL = 1e-5
+XI_TOL = 5e-5     # reference coordinates (xi steps are world steps over |J|, about h / 2)
 U_TOL = 1e-5
 
 
@@ -150,13 +171,13 @@ def check_against_oracle(gpu, rays, osc, iso, iso_on, h, product_trace=None, lab
     agreeing hits within POS_TOL * h / XI_TOL / U_TOL of the judge (the
     oracle's hits polished to exact roots). Returns the class counts."""
     ref, _ = osc.trace(rays, iso, iso_on, precision=64)
-    c = classify(gpu, ref, rays, osc, iso, product_trace=product_trace, iso_on=iso_on)
+    judge = osc.polish(rays, ref, iso)
+    c = classify(gpu, ref, rays, osc, iso, product_trace=product_trace, iso_on=iso_on, judge=judge)
     cnt = counts(c)
     print(f"{label}: {cnt}")
     for i in c["other"][:5]:
         print("   other", i, gpu[i][["kind", "elem", "face", "t"]], ref[i][["kind", "elem", "face", "t"]])
     assert c["other"].size == 0, cnt
-    judge = osc.polish(rays, ref, iso)
     err = errors(gpu, judge, rays, h)
     print(f"   errors vs FP64 judge: {err}")
     for lab, e in err.items():

@@ -194,9 +194,18 @@ def test_smallest_engine_limits_give_the_same_answers(small):
     finally:
         for o, v in saved.items():
             ctx.set_option(o, v)
-    assert st["status"] == 0 and st["rounds"] >= 2
+    print("smallest limits:", {k: st[k] for k in ("status", "rounds", "tail_rays", "fp64_polished")})
+    assert st["status"] == 0 and st["rounds"] >= 2 and st["tail_rays"] == 0
     h0, h1 = h0.reshape(-1), h1.reshape(-1)
-    assert np.array_equal(h0["kind"], h1["kind"]) and np.array_equal(h0["elem"], h1["elem"])
-    assert np.array_equal(h0["face"], h1["face"])
-    m = h0["kind"] > 0
+    # the default call finishes its last rays in the warp-per-ray tail, whose
+    # face Newton rounds differently in the last bits: rays at a decision
+    # boundary may answer differently, every other ray identically
+    import oracle_bind as ob
+
+    rays = ob.camera_rays(w.camera.lookfrom, w.camera.lookat, w.camera.vup, w.camera.vfov_deg, W, H)
+    c = parity.classify(h1, h0, rays, osc, w.isovalues[0],
+                        product_trace=lambda r: ctx.intersect(r, w.isovalues[0], True))
+    print("smallest limits vs defaults:", parity.counts(c))
+    assert c["other"].size == 0 and c["differ"] <= 10
+    m = parity.same_hit(h0, h1) & (h0["kind"] > 0)
     assert np.abs(h0["t"][m] - h1["t"][m]).max() <= 1e-6

@@ -5,10 +5,9 @@ device-wide synchronisation). Its scratch is a fixed device array for at most
 HO_NOALLOC_MAX_RAYS rays per call.
 
 Checked through the C ABI against the regular entry point, on two calls in a
-row (hit identity on >= 99.9% of rays; t within 5e-4: the regular entry
-point polishes its hits to the exact roots in FP64, this one returns the
-solvers' own answers, which stop at a face residual of 1e-4); the second call
-takes no device memory; a call over the
+row, with the FP64 check and polish of the regular entry point turned off
+(this entry point returns the solvers' own answers): hit identity on >= 99.9%
+of rays, t within 2e-4; the second call takes no device memory; a call over the
 limit is refused with HO_ERR_RANGE; no ray reports an incomplete tree walk.
 A second case puts prisms, quads and triangles beside the hexahedra, so the
 call's primitive pass runs after its hexahedron kernels. This file sorts last
@@ -38,7 +37,9 @@ def test_noalloc_matches_regular_entry_point_on_two_calls():
     n = rays.shape[0]
     iso = w.isovalues[0]
     ctx.set_mode(hr.MODE_BATCHED)
-    ref = ctx.intersect(rays, iso, True)  # the existing entry point
+    ctx.set_option(hr.OPT_FP64_CHECK, 0)  # this entry point returns the solvers' own answers
+    ref = ctx.intersect(rays, iso, True)
+    ctx.set_option(hr.OPT_FP64_CHECK, 1)  # the existing entry point
     d_rays = torch.from_numpy(rays).cuda()
     d_out = torch.zeros(n * hr.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
@@ -52,7 +53,7 @@ def test_noalloc_matches_regular_entry_point_on_two_calls():
         same = (got["kind"] == ref["kind"]) & (got["elem"] == ref["elem"]) & (got["face"] == ref["face"])
         assert same.mean() >= 0.999, (call, same.mean())
         hit = same & (ref["kind"] > 0)
-        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 5e-4, call
+        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 2e-4, call
         assert (ref["kind"] > 0).sum() > 1000
         assert not (got["flags"] & hr.FLAG_INCOMPLETE).any()
         free.append(torch.cuda.mem_get_info()[0])
@@ -85,7 +86,9 @@ def test_noalloc_hexahedra_with_primitives():
     rays = ob.camera_rays(cam.lookfrom, cam.lookat, cam.vup, cam.vfov_deg, 120, 90)
     n = rays.shape[0]
     iso = w.isovalues[0]
+    ctx.set_option(hr.OPT_FP64_CHECK, 0)  # this entry point returns the solvers' own answers
     ref = ctx.intersect(rays, iso, True)
+    ctx.set_option(hr.OPT_FP64_CHECK, 1)
     assert (ref["kind"] >= hr.HIT_PRISM).sum() > 100 and (ref["kind"] == hr.HIT_FACE).sum() > 100
     d_rays = torch.from_numpy(rays).cuda()
     d_out = torch.zeros(n * hr.HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
@@ -98,6 +101,6 @@ def test_noalloc_hexahedra_with_primitives():
         same = (got["kind"] == ref["kind"]) & (got["elem"] == ref["elem"]) & (got["face"] == ref["face"])
         assert same.mean() >= 0.999, (call, same.mean())
         hit = same & (ref["kind"] > 0)
-        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 5e-4, call
+        assert np.abs(got["t"][hit] - ref["t"][hit]).max() < 2e-4, call
         assert not (got["flags"] & hr.FLAG_INCOMPLETE).any()
     ctx.close()
