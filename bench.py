@@ -66,6 +66,8 @@ def parse():
                          "cpu_baseline entry takes at most 16,384)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default element batch size (profiling runs: fewer launches)")
     ap.add_argument("--no-error-check", action="store_true", help="skip the error_vs_fp64 block")
     ap.add_argument("--error-rays", type=int, default=4096, help="rays of the error_vs_fp64 sample")
     ap.add_argument("--tensor", type=int, default=0, choices=[0, 1],
@@ -73,7 +75,8 @@ def parse():
     ap.add_argument("--mode", default="all", choices=["all", "plain", "batched", "learned"],
                     help="learned: learned-init + batched (the headline); batched: the same kernels with cold "
                          "starts; plain: one thread per ray, the reference algorithm's structure")
-    ap.add_argument("--train-samples", type=int, default=2_000_000)
+    ap.add_argument("--train-samples", type=int, default=20_000_000,
+                    help="training pairs from the plain solver (the learned configuration names 20 M)")
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling)")
     ap.add_argument("--height", type=int, default=0, help="override the workload's image height (profiling)")
@@ -491,7 +494,7 @@ def run_gpu(args, rank, world):
 
     def timed(mode):
         ctx.set_mode(mode)
-        if mode != hr.MODE_PLAIN:  # the round kernel's element batch size, picked on this workload
+        if mode != hr.MODE_PLAIN and not args.no_autotune:  # the round kernel's element batch size
             tuned[{hr.MODE_BATCHED: "batched", hr.MODE_LEARNED: "learned"}[mode]] = ctx.autotune(
                 w.camera, w.isovalues, W, H)
         # CUDA events around each round's intersection launches (event nodes of the call's graph)
