@@ -54,6 +54,9 @@ extern "C" {
 #define HO_FLAG_OVERFLOW 4u      /* candidate list restarted (more than K boxes)     */
 #define HO_FLAG_INCOMPLETE 8u    /* the tree walk met its stack limit: candidates may
                                     be missing from this ray's answer                */
+#define HO_FLAG_TIE 16u          /* the hit displaced another within 1e-4 in t (one
+                                    surface point claimed twice) and the FP64 tie
+                                    rule chose between the two (FP64 check on)       */
 
 typedef struct ho_context ho_context;
 
@@ -156,6 +159,12 @@ typedef struct {
   uint64_t prim_node_visits; /* primitive-tree nodes visited by that pass     */
   uint64_t fp64_polished;    /* hits whose t, xi and u the FP64 polish moved to
                                 the exact root of their defining equations   */
+  uint64_t fp64_ties;        /* rays whose best hit displaced another within
+                                1e-4 in t (one surface point claimed twice),
+                                weighed by the FP64 tie rule                  */
+  uint64_t fp64_ties_swapped;  /* of those, rays where the displaced hit won
+                                (nearer exact root, or the same point and the
+                                lower element / face index)                  */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

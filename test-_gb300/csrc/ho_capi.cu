@@ -164,6 +164,8 @@ int read_stats(ho_context* c) {
   s.prim_flops = ds.c[ho::ST_PRIM_FLOPS];
   s.prim_node_visits = ds.c[ho::ST_PRIM_NODES];
   s.fp64_polished = ds.c[ho::ST_POLISHED];
+  s.fp64_ties = ds.c[ho::ST_TIES];
+  s.fp64_ties_swapped = ds.c[ho::ST_TIES_SWAPPED];
   s.prim_kernel_ns = 0;
   if (c->prim_timed) {
     float ms = 0.f;

@@ -57,15 +57,16 @@ cudaError_t launch_residuals_n(const float* rec, const uint32_t* flags, int64_t 
   return cudaGetLastError();
 }
 
-// One thread per listed ray (the queued rays with a hit): FP64 check;
-// failures are listed.
+// One thread per listed ray (the queued rays with a hit): FP64 check and
+// polish, then the FP64 tie rule against the ray's tie partner; failures are
+// listed.
 template <int N>
 __global__ void __launch_bounds__(128) check_kernel(TraceParams P, RayState* __restrict__ st,
                                                     const uint32_t* __restrict__ list,
                                                     const unsigned* __restrict__ n_list,
                                                     uint32_t* __restrict__ fail_list, unsigned* __restrict__ n_fail) {
   const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
-  bool checked = false, failed = false, polished = false;
+  bool checked = false, failed = false, polished = false, tied = false, swapped = false;
   if (k < *n_list) {
     const unsigned item = list[k];
     RayState& r = st[item];
@@ -76,17 +77,28 @@ __global__ void __launch_bounds__(128) check_kernel(TraceParams P, RayState* __r
       query_ray(P, P.work[item], o, d, iso, iso_on);
       checked = true;
       HitState h = r.best;
-      failed = !fp64_check_polish<N>(P.rec, P.flags, o, d, iso, h, polished);
-      if (failed) fail_list[atomicAdd(n_fail, 1u)] = item;
-      else if (polished) r.best = h;
+      double t64;
+      failed = !fp64_check_polish<N>(P.rec, P.flags, o, d, iso, h, polished, &t64);
+      if (failed) {
+        fail_list[atomicAdd(n_fail, 1u)] = item;
+      } else {
+        if (r.tie.kind != HO_HIT_MISS) {
+          tied = true;
+          swapped = fp64_tie_rule<N>(P.rec, P.flags, o, d, iso, h, t64, r.tie);
+        }
+        if (polished || swapped) r.best = h;
+      }
     }
   }
   const unsigned cm = __ballot_sync(0xffffffffu, checked), fm = __ballot_sync(0xffffffffu, failed),
-                 pm = __ballot_sync(0xffffffffu, polished);
+                 pm = __ballot_sync(0xffffffffu, polished), tm = __ballot_sync(0xffffffffu, tied),
+                 sm = __ballot_sync(0xffffffffu, swapped);
   if ((threadIdx.x & 31) == 0) {
     if (cm) atomicAdd(&P.stats->c[ST_CHECKED], static_cast<unsigned long long>(__popc(cm)));
     if (fm) atomicAdd(&P.stats->c[ST_CHECK_FAIL], static_cast<unsigned long long>(__popc(fm)));
     if (pm) atomicAdd(&P.stats->c[ST_POLISHED], static_cast<unsigned long long>(__popc(pm)));
+    if (tm) atomicAdd(&P.stats->c[ST_TIES], static_cast<unsigned long long>(__popc(tm)));
+    if (sm) atomicAdd(&P.stats->c[ST_TIES_SWAPPED], static_cast<unsigned long long>(__popc(sm)));
   }
 }
 
@@ -105,14 +117,20 @@ __global__ void __launch_bounds__(kTraceBlock) fallback_kernel(TraceParams P, Ra
     float iso;
     bool iso_on;
     query_ray(P, P.work[item], o, d, iso, iso_on);
-    HitState b = plain_trace<N>(P, o, d, iso, iso_on, w);
+    HitState tie;
+    HitState b = plain_trace<N>(P, o, d, iso, iso_on, w, &tie);
     b.flags |= HO_FLAG_FALLBACK | (st[item].best.flags & HO_FLAG_OVERFLOW);
     bool polished;
-    if (!fp64_check_polish<N>(P.rec, P.flags, o, d, iso, b, polished)) {
+    double t64;
+    if (!fp64_check_polish<N>(P.rec, P.flags, o, d, iso, b, polished, &t64)) {
       b.flags |= HO_FLAG_FP64_FAIL;
       atomicAdd(&P.stats->c[ST_CHECK_FINAL], 1ull);
-    } else if (polished) {
-      atomicAdd(&P.stats->c[ST_POLISHED], 1ull);
+    } else {
+      if (polished) atomicAdd(&P.stats->c[ST_POLISHED], 1ull);
+      if (tie.kind != HO_HIT_MISS) {
+        atomicAdd(&P.stats->c[ST_TIES], 1ull);
+        if (fp64_tie_rule<N>(P.rec, P.flags, o, d, iso, b, t64, tie)) atomicAdd(&P.stats->c[ST_TIES_SWAPPED], 1ull);
+      }
     }
     st[item].best = b;
     st[item].its += static_cast<int>(w.newton + w.face);

@@ -846,11 +846,29 @@ struct HitState {
   uint32_t flags;
 };
 
+// Two candidates' hits this close in t claim one surface point: a face shared
+// by two elements, an edge of two faces, a root in the overlap of two padded
+// boxes. The reference keeps whichever its visit order and FP32 rounding put
+// first. A hit that displaces the best one by less than this keeps the
+// displaced hit as the ray's tie partner, and the final FP64 check decides
+// between the two (fp64_tie_rule).
+constexpr float kTieT = 1e-4f;
+
+// The best hit is about to become a hit at t_new (< best.t): keep the old one
+// as the tie partner when it is within kTieT, and drop a partner that the new
+// hit leaves further than that.
+__device__ __forceinline__ void note_tie(const HitState& best, float t_new, HitState* tie) {
+  if (!tie) return;
+  if (best.kind != HO_HIT_MISS && best.t - t_new <= kTieT) *tie = best;
+  else if (tie->kind != HO_HIT_MISS && tie->t - t_new > kTieT) tie->kind = HO_HIT_MISS;
+}
+
 // Per-candidate policy of the reference's hex branch: iso search on the
 // padded-box segment when enabled; if it finds nothing, nearest curved face.
 template <int N, bool SM>
 __device__ void visit_candidate(const Elem<N, SM>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d,
-                                float te, float tx, float iso, bool iso_on, HitState& best, Work& w) {
+                                float te, float tx, float iso, bool iso_on, HitState& best, Work& w,
+                                HitState* tie = nullptr) {
   ++w.cand;
   float th;
   float3 xi, g;
@@ -858,6 +876,7 @@ __device__ void visit_candidate(const Elem<N, SM>& e, const float* __restrict__ 
     if (th > 0.001f && th < best.t) {
       float3 n = normalize3(g);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+      note_tie(best, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = -1;
@@ -882,6 +901,7 @@ __device__ void visit_candidate(const Elem<N, SM>& e, const float* __restrict__ 
       else n = cross3(dr, ds);
       n = normalize3(n);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+      note_tie(best, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = face;
@@ -1029,7 +1049,8 @@ __device__ bool hit_hex_warp(const Elem<N, SM>& e, const float* __restrict__ fbo
 // Warp version of visit_candidate: every lane holds the same `best`.
 template <int N, bool L, bool SM>
 __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox, int eidx, float3 o, float3 d, float te,
-                           float tx, float iso, bool iso_on, HitState& best, Work& w, Work& wu, const Pred& pr) {
+                           float tx, float iso, bool iso_on, HitState& best, Work& w, Work& wu, const Pred& pr,
+                           HitState* tie = nullptr) {
   ++wu.cand;
   float th;
   float3 xi, g;
@@ -1037,6 +1058,7 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
     if (th > 0.001f && th < best.t) {
       float3 n = normalize3(g);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+      note_tie(best, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = -1;
@@ -1067,6 +1089,7 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
       else n = cross3(dr, ds);
       n = normalize3(n);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
+      note_tie(best, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = face;

@@ -221,8 +221,9 @@ __device__ __forceinline__ bool polish_step(const HitState& h, float3 d, float i
 // the hit's t, xi and u were refined.
 template <int N>
 __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint32_t* __restrict__ eflags, float3 o,
-                                  float3 d, float iso, HitState& h, bool& polished) {
+                                  float3 d, float iso, HitState& h, bool& polished, double* t64 = nullptr) {
   polished = false;
+  if (t64) *t64 = h.t;
   if (h.kind == HO_HIT_MISS) return true;
   const bool iso_hit = h.kind != HO_HIT_FACE;
   const bool has_field = iso_hit || (__ldg(eflags + h.elem) & 1u) != 0;
@@ -280,7 +281,33 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
   h.t = static_cast<float>(t);
   h.xi = make_float3(static_cast<float>(x0), static_cast<float>(x1), static_cast<float>(x2));
   if (has_field) h.u = static_cast<float>(un);
+  if (t64) *t64 = t;
   polished = true;
+  return true;
+}
+
+// The FP64 tie rule between a ray's best hit (already checked and polished,
+// exact root at t_best) and its tie partner: the partner is checked and
+// polished the same way; if it passes, the nearer exact root wins, and where
+// the two roots coincide within 1e-7 of t (one surface point: a shared face,
+// an edge), the lower element index, then the lower face index. Returns true
+// when the partner replaced the best hit (flags carried over); the answer
+// carries HO_FLAG_TIE either way.
+template <int N>
+__device__ bool fp64_tie_rule(const float* __restrict__ rec_all, const uint32_t* __restrict__ eflags, float3 o,
+                              float3 d, float iso, HitState& best, double t_best, HitState tie) {
+  best.flags |= HO_FLAG_TIE;
+  bool polished;
+  double t_tie;
+  if (!fp64_check_polish<N>(rec_all, eflags, o, d, iso, tie, polished, &t_tie)) return false;
+  const double eps = 1e-7 * fmax(1.0, fabs(t_best));
+  bool wins;
+  if (t_tie < t_best - eps) wins = true;
+  else if (t_tie > t_best + eps) wins = false;
+  else wins = tie.elem < best.elem || (tie.elem == best.elem && tie.face < best.face);
+  if (!wins) return false;
+  tie.flags = best.flags;
+  best = tie;
   return true;
 }
 

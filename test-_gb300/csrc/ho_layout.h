@@ -88,6 +88,8 @@ enum StatSlot {
   ST_PRIM_FLOPS,
   ST_PRIM_NODES,
   ST_POLISHED,  // hits refined by the FP64 polish (check and plain kernels)
+  ST_TIES,      // rays with a tie partner that the FP64 tie rule weighed
+  ST_TIES_SWAPPED,  // of those, rays whose partner won
   ST_COUNT
 };
 

@@ -52,8 +52,8 @@ constexpr int64_t kNoAllocMaxRays = HO_NOALLOC_MAX_RAYS;
 
 // byte layout of the scratch array
 constexpr size_t kNaStats = 0;                                         // DevStats
-constexpr size_t kNaCounters = 256;                                    // queue length, next item
-constexpr size_t kNaWork = 512;                                        // int32 per ray
+constexpr size_t kNaCounters = 512;                                    // queue length, next item
+constexpr size_t kNaWork = 768;                                        // int32 per ray
 constexpr size_t kNaKbuf = kNaWork + 4 * kNoAllocMaxRays;              // float2 x kCandK per ray
 constexpr size_t kNaKovf = kNaKbuf + 8 * kCandK * kNoAllocMaxRays;     // uint8 per ray
 constexpr size_t kNaBytes = kNaKovf + kNoAllocMaxRays;

@@ -219,6 +219,8 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
     tot.prim_kernel_ns += st.prim_kernel_ns;
     tot.prim_node_visits += st.prim_node_visits;
     tot.fp64_polished += st.fp64_polished;
+    tot.fp64_ties += st.fp64_ties;
+    tot.fp64_ties_swapped += st.fp64_ties_swapped;
     tot.graph = st.graph;
     tot.max_modes = st.max_modes;
     tot.status |= st.status;

@@ -20,6 +20,7 @@ __global__ void round_init_kernel(RayState* __restrict__ st, const uint8_t* __re
   if (i >= *qcount) return;
   RayState r;
   r.best = miss_state();
+  r.tie = miss_state();
   r.cursor = 0;
   r.pass = 0;
   r.kt = -FLT_MAX;

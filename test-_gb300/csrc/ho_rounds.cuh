@@ -70,6 +70,7 @@ struct RoundBatch {
 // Per queue item state kept across rounds.
 struct RayState {
   HitState best;
+  HitState tie;  // the hit the best one displaced within kTieT (else a miss)
   int cursor;   // next candidate in the item's list
   int pass;     // 0: the classify pass's list (with predictions); >0 re-collected
   float kt;     // last visited key (entry t, element)
@@ -412,6 +413,7 @@ __device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s, int
 __device__ __forceinline__ void commit_hit(const RoundParams& P, const PairSm& p, int kind, int face, float t, float3 xi,
                                            float3 n, float u) {
   HitState& b = P.state[p.item].best;
+  note_tie(b, t, &P.state[p.item].tie);
   b.t = t;
   b.elem = p.elem;
   b.face = face;
@@ -1021,7 +1023,7 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
     float iso;
     bool iso_on;
     query_ray(P, P.work[item], o, d, iso, iso_on);
-    HitState best = r.best;
+    HitState best = r.best, tie = r.tie;
     float kt = r.kt;
     int ke = r.ke, pass = r.pass, first = r.cursor;
     bool overflow = r.ovf != 0;
@@ -1075,7 +1077,7 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
             pr.te = te;
           }
           visit_warp<N, L>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
-                           best, w, wu, pr);
+                           best, w, wu, pr, &tie);
         }
         kt = ct;
         ke = ce;
@@ -1098,6 +1100,7 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
     __syncwarp();
     if (lane == 0) {
       r.best = best;
+      r.tie = tie;
       r.its += static_cast<int>(its + wu.newton + wu.face - it0);
       r.done = 1;
     }

@@ -403,8 +403,10 @@ __global__ void __launch_bounds__(kTraceBlock) isect_kernel(TraceParams P) {
 // the sequential cold-start algorithm (visit_candidate), walking the tree
 // again when more than kCandK candidates were in range.
 template <int N>
-__device__ HitState plain_trace(const TraceParams& P, float3 o, float3 d, float iso, bool iso_on, Work& w) {
+__device__ HitState plain_trace(const TraceParams& P, float3 o, float3 d, float iso, bool iso_on, Work& w,
+                                HitState* tie = nullptr) {
   HitState best = miss_state();
+  if (tie) *tie = miss_state();
   float kt = -FLT_MAX;
   int ke = -1;
   for (;;) {
@@ -440,7 +442,7 @@ __device__ HitState plain_trace(const TraceParams& P, float3 o, float3 d, float 
         el.c = CoefRef<false>{P.rec + static_cast<int64_t>(ce) * record_floats(N)};
         el.has_field = (__ldg(P.flags + ce) & 1u) != 0;
         visit_candidate<N>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on, best,
-                           w);
+                           w, tie);
       }
       kt = ct;
       ke = ce;
@@ -481,15 +483,30 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
   Work w;
   HitState best = miss_state();
   bool polished = false;
+  int tie_seen = 0, tie_swapped = 0;
   if (active) {
-    best = plain_trace<N>(P, o, d, iso, iso_on, w);
-    // the FP64 check and polish of the engines' final pass; the plain solver
-    // is the fallback itself, so a failing hit is only flagged
-    if (P.fp64 && !fp64_check_polish<N>(P.rec, P.flags, o, d, iso, best, polished)) best.flags |= HO_FLAG_FP64_FAIL;
+    HitState tie;
+    best = plain_trace<N>(P, o, d, iso, iso_on, w, &tie);
+    // the FP64 check, polish and tie rule of the engines' final pass; the
+    // plain solver is the fallback itself, so a failing hit is only flagged
+    if (P.fp64) {
+      double t64;
+      if (!fp64_check_polish<N>(P.rec, P.flags, o, d, iso, best, polished, &t64)) {
+        best.flags |= HO_FLAG_FP64_FAIL;
+      } else if (tie.kind != HO_HIT_MISS) {
+        tie_seen = 1;
+        tie_swapped = fp64_tie_rule<N>(P.rec, P.flags, o, d, iso, best, t64, tie) ? 1 : 0;
+      }
+    }
   }
   flush_work(P.stats, w, active);
-  const unsigned pm = __ballot_sync(kFull, polished);
-  if ((threadIdx.x & 31) == 0 && pm) atomicAdd(&P.stats->c[ST_POLISHED], static_cast<unsigned long long>(__popc(pm)));
+  const unsigned pm = __ballot_sync(kFull, polished), tm = __ballot_sync(kFull, tie_seen),
+                 sm = __ballot_sync(kFull, tie_swapped);
+  if ((threadIdx.x & 31) == 0) {
+    if (pm) atomicAdd(&P.stats->c[ST_POLISHED], static_cast<unsigned long long>(__popc(pm)));
+    if (tm) atomicAdd(&P.stats->c[ST_TIES], static_cast<unsigned long long>(__popc(tm)));
+    if (sm) atomicAdd(&P.stats->c[ST_TIES_SWAPPED], static_cast<unsigned long long>(__popc(sm)));
+  }
   if (active) write_result(P, q, d, best, w.newton + w.face);
 }
 

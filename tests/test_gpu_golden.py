@@ -123,6 +123,9 @@ def test_against_reference_and_judge(golden, mode):
         g = ctx.intersect(rays, iso, True)  # 0.0 traced as a real isovalue, as the fixture is
         st = ctx.stats()
         assert st["status"] == 0 and st["fp64_failed_after_fallback"] == 0
+        # every ray the FP64 tie rule weighed carries the tie flag
+        tied = (g["flags"] & hr.FLAG_TIE) != 0
+        assert int(tied.sum()) == st["fp64_ties"] and st["fp64_ties_swapped"] <= st["fp64_ties"]
 
         def trace(r, iso=iso):
             return ctx.intersect(r, iso, True)
@@ -131,7 +134,8 @@ def test_against_reference_and_judge(golden, mode):
         agree = 1.0 - ex["differ"] / rays.shape[0]
         print(f"{name} {mode} iso {iso}: rays {rays.shape[0]}, hits {int((ref['kind'] > 0).sum())}, identical "
               f"{agree:.4f}; differ {ex['differ']}: order-dependent {ex['order_dependent']}, tie {ex['tie']}, "
-              f"grazing {ex['grazing']}, unstable {ex['unstable']}, unexplained {len(ex['unexplained'])}")
+              f"grazing {ex['grazing']}, unstable {ex['unstable']}, unexplained {len(ex['unexplained'])}; "
+              f"FP64 tie rule: weighed {st['fp64_ties']}, partner won {st['fp64_ties_swapped']}")
         for i in ex["unexplained"][:5]:
             print("   unexplained", i, g[i][["kind", "elem", "face", "t"]], ref[i][["kind", "elem", "face", "t"]])
         assert not ex["unexplained"]
