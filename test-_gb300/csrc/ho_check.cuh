@@ -58,15 +58,17 @@ cudaError_t launch_residuals_n(const float* rec, const uint32_t* flags, int64_t 
 }
 
 // One thread per listed ray (the queued rays with a hit): FP64 check and
-// polish, then the FP64 tie rule against the ray's tie partner; failures are
-// listed.
+// polish; failures are listed from the front of fail_list, rays that passed
+// with a tie partner from its back (tie_end downwards: a listed ray goes to
+// at most one of the two lists, so they do not meet).
 template <int N>
 __global__ void __launch_bounds__(128) check_kernel(TraceParams P, RayState* __restrict__ st,
                                                     const uint32_t* __restrict__ list,
                                                     const unsigned* __restrict__ n_list,
-                                                    uint32_t* __restrict__ fail_list, unsigned* __restrict__ n_fail) {
+                                                    uint32_t* __restrict__ fail_list, unsigned* __restrict__ n_fail,
+                                                    uint32_t* __restrict__ tie_end, unsigned* __restrict__ n_tie) {
   const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;
-  bool checked = false, failed = false, polished = false, tied = false, swapped = false;
+  bool checked = false, failed = false, polished = false;
   if (k < *n_list) {
     const unsigned item = list[k];
     RayState& r = st[item];
@@ -77,29 +79,52 @@ __global__ void __launch_bounds__(128) check_kernel(TraceParams P, RayState* __r
       query_ray(P, P.work[item], o, d, iso, iso_on);
       checked = true;
       HitState h = r.best;
-      double t64;
-      failed = !fp64_check_polish<N>(P.rec, P.flags, o, d, iso, h, polished, &t64);
+      failed = !fp64_check_polish<N>(P.rec, P.flags, o, d, iso, h, polished);
       if (failed) {
         fail_list[atomicAdd(n_fail, 1u)] = item;
       } else {
-        if (r.tie.kind != HO_HIT_MISS) {
-          tied = true;
-          swapped = fp64_tie_rule<N>(P.rec, P.flags, o, d, iso, h, t64, r.tie);
-        }
-        if (polished || swapped) r.best = h;
+        if (polished) r.best = h;
+        if (r.tie.kind != HO_HIT_MISS) *(tie_end - atomicAdd(n_tie, 1u)) = item;
       }
     }
   }
   const unsigned cm = __ballot_sync(0xffffffffu, checked), fm = __ballot_sync(0xffffffffu, failed),
-                 pm = __ballot_sync(0xffffffffu, polished), tm = __ballot_sync(0xffffffffu, tied),
-                 sm = __ballot_sync(0xffffffffu, swapped);
+                 pm = __ballot_sync(0xffffffffu, polished);
   if ((threadIdx.x & 31) == 0) {
     if (cm) atomicAdd(&P.stats->c[ST_CHECKED], static_cast<unsigned long long>(__popc(cm)));
     if (fm) atomicAdd(&P.stats->c[ST_CHECK_FAIL], static_cast<unsigned long long>(__popc(fm)));
     if (pm) atomicAdd(&P.stats->c[ST_POLISHED], static_cast<unsigned long long>(__popc(pm)));
-    if (tm) atomicAdd(&P.stats->c[ST_TIES], static_cast<unsigned long long>(__popc(tm)));
-    if (sm) atomicAdd(&P.stats->c[ST_TIES_SWAPPED], static_cast<unsigned long long>(__popc(sm)));
   }
+}
+
+// The rays the check listed with a tie partner, one thread each (grid-stride
+// over the device-side count): the FP64 tie rule. A separate pass so that
+// the partners, about 3% of the hits and spread over most warps, do not
+// serialise the check's warps. The best hit is polished already; its exact
+// root t is taken again by the same polish (one FP64 evaluation).
+template <int N>
+__global__ void __launch_bounds__(128) tie_kernel(TraceParams P, RayState* __restrict__ st,
+                                                  const uint32_t* __restrict__ tie_end,
+                                                  const unsigned* __restrict__ n_tie) {
+  const unsigned n = *n_tie;
+  unsigned long long weighed = 0, swapped = 0;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const unsigned item = *(tie_end - k);
+    RayState& r = st[item];
+    float3 o, d;
+    float iso;
+    bool iso_on;
+    query_ray(P, P.work[item], o, d, iso, iso_on);
+    HitState b = r.best;
+    bool polished;
+    double t64;
+    if (!fp64_check_polish<N>(P.rec, P.flags, o, d, iso, b, polished, &t64)) continue;
+    ++weighed;
+    if (fp64_tie_rule<N>(P.rec, P.flags, o, d, iso, b, t64, r.tie)) ++swapped;
+    r.best = b;
+  }
+  if (weighed) atomicAdd(&P.stats->c[ST_TIES], weighed);
+  if (swapped) atomicAdd(&P.stats->c[ST_TIES_SWAPPED], swapped);
 }
 
 // The failed rays, traced again by the plain cold-start solver (grid-stride
@@ -146,30 +171,36 @@ __global__ void __launch_bounds__(kTraceBlock) fallback_kernel(TraceParams P, Ra
   if (w.map) atomicAdd(&P.stats->c[ST_MAP], static_cast<unsigned long long>(w.map));
 }
 
+// fail_list holds n_cap entries (n_cap >= the listed rays); n_fail and
+// n_tie are zeroed by the caller.
 template <int N>
 cudaError_t launch_check_n(const TraceParams& P, RayState* st, const uint32_t* list, const unsigned* n_list,
-                           uint32_t* fail_list, unsigned* n_fail, int64_t n_cap, int sms, cudaStream_t s) {
-  check_kernel<N><<<static_cast<unsigned>((n_cap + 127) / 128), 128, 0, s>>>(P, st, list, n_list, fail_list, n_fail);
+                           uint32_t* fail_list, unsigned* n_fail, unsigned* n_tie, int64_t n_cap, int sms,
+                           cudaStream_t s) {
+  uint32_t* tie_end = fail_list + (n_cap - 1);
+  check_kernel<N><<<static_cast<unsigned>((n_cap + 127) / 128), 128, 0, s>>>(P, st, list, n_list, fail_list, n_fail,
+                                                                              tie_end, n_tie);
+  tie_kernel<N><<<sms * 2, 128, 0, s>>>(P, st, tie_end, n_tie);
   fallback_kernel<N><<<sms * 2, kTraceBlock, 0, s>>>(P, st, fail_list, n_fail);
   return cudaGetLastError();
 }
 
 extern template cudaError_t launch_check_n<2>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<3>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<4>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<5>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<6>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<7>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<8>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 extern template cudaError_t launch_check_n<9>(const TraceParams&, RayState*, const uint32_t*, const unsigned*,
-                                              uint32_t*, unsigned*, int64_t, int, cudaStream_t);
+                                              uint32_t*, unsigned*, unsigned*, int64_t, int, cudaStream_t);
 
 extern template cudaError_t launch_residuals_n<2>(const float*, const uint32_t*, int64_t, const float*, const ho_hit*,
                                                   double*, cudaStream_t);

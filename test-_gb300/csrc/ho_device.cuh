@@ -854,13 +854,14 @@ struct HitState {
 // between the two (fp64_tie_rule).
 constexpr float kTieT = 1e-4f;
 
-// The best hit is about to become a hit at t_new (< best.t): keep the old one
-// as the tie partner when it is within kTieT, and drop a partner that the new
-// hit leaves further than that.
-__device__ __forceinline__ void note_tie(const HitState& best, float t_new, HitState* tie) {
+// The best hit (t = best_t; a miss has FLT_MAX) is about to become a hit at
+// t_new < best_t: keep the old one as the tie partner when it is within
+// kTieT, else drop the partner (it lies behind the old best, so further than
+// kTieT from the new hit too). Blind stores: no read of the partner.
+__device__ __forceinline__ void note_tie(const HitState& best, float best_t, float t_new, HitState* tie) {
   if (!tie) return;
-  if (best.kind != HO_HIT_MISS && best.t - t_new <= kTieT) *tie = best;
-  else if (tie->kind != HO_HIT_MISS && tie->t - t_new > kTieT) tie->kind = HO_HIT_MISS;
+  if (best_t - t_new <= kTieT) *tie = best;
+  else tie->kind = HO_HIT_MISS;
 }
 
 // Per-candidate policy of the reference's hex branch: iso search on the
@@ -876,7 +877,7 @@ __device__ void visit_candidate(const Elem<N, SM>& e, const float* __restrict__ 
     if (th > 0.001f && th < best.t) {
       float3 n = normalize3(g);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
-      note_tie(best, th, tie);
+      note_tie(best, best.t, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = -1;
@@ -901,7 +902,7 @@ __device__ void visit_candidate(const Elem<N, SM>& e, const float* __restrict__ 
       else n = cross3(dr, ds);
       n = normalize3(n);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
-      note_tie(best, th, tie);
+      note_tie(best, best.t, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = face;
@@ -1058,7 +1059,7 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
     if (th > 0.001f && th < best.t) {
       float3 n = normalize3(g);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
-      note_tie(best, th, tie);
+      note_tie(best, best.t, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = -1;
@@ -1089,7 +1090,7 @@ __device__ void visit_warp(const Elem<N, SM>& e, const float* __restrict__ fbox,
       else n = cross3(dr, ds);
       n = normalize3(n);
       if (n.x * d.x + n.y * d.y + n.z * d.z > 0.f) n = make_float3(-n.x, -n.y, -n.z);
-      note_tie(best, th, tie);
+      note_tie(best, best.t, th, tie);
       best.t = th;
       best.elem = eidx;
       best.face = face;

@@ -294,7 +294,7 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
 // when the partner replaced the best hit (flags carried over); the answer
 // carries HO_FLAG_TIE either way.
 template <int N>
-__device__ bool fp64_tie_rule(const float* __restrict__ rec_all, const uint32_t* __restrict__ eflags, float3 o,
+__device__ __noinline__ bool fp64_tie_rule(const float* __restrict__ rec_all, const uint32_t* __restrict__ eflags, float3 o,
                               float3 d, float iso, HitState& best, double t_best, HitState tie) {
   best.flags |= HO_FLAG_TIE;
   bool polished;

@@ -269,25 +269,42 @@ static int enqueue_check(ho_context* c, const TraceParams& P, const RoundParams&
   // that the check's threads are all busy
   uint32_t* list = reinterpret_cast<uint32_t*>(c->rounds.pelem);
   unsigned* n_list = c->rounds.ctr + 6;
+  unsigned* n_tie = c->rounds.ctr + 7;
   RT_TRY(cudaMemsetAsync(c->rounds.ctr + 3, 0, sizeof(unsigned), s));
-  RT_TRY(cudaMemsetAsync(n_list, 0, sizeof(unsigned), s));
+  RT_TRY(cudaMemsetAsync(n_list, 0, 2 * sizeof(unsigned), s));
   ray_list_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P.qcount, R.state, true, list, n_list,
                                                                              P.stats);
   RT_TRY(cudaGetLastError());
-  c->launches += 3;
+  c->launches += 4;  // ray list, check, tie rule, fallback
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaError_t e;
   switch (c->N) {
-    case 2: e = launch_check_n<2>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 3: e = launch_check_n<3>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 4: e = launch_check_n<4>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 5: e = launch_check_n<5>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 6: e = launch_check_n<6>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 7: e = launch_check_n<7>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 8: e = launch_check_n<8>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
-    case 9: e = launch_check_n<9>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_cap, sms, s); break;
+    case 2:
+      e = launch_check_n<2>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 3:
+      e = launch_check_n<3>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 4:
+      e = launch_check_n<4>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 5:
+      e = launch_check_n<5>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 6:
+      e = launch_check_n<6>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 7:
+      e = launch_check_n<7>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 8:
+      e = launch_check_n<8>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
+    case 9:
+      e = launch_check_n<9>(P, R.state, list, n_list, c->rounds.fail, c->rounds.ctr + 3, n_tie, n_cap, sms, s);
+      break;
     default: e = cudaErrorInvalidValue; break;
   }
   RT_TRY(e);

@@ -413,7 +413,7 @@ __device__ __forceinline__ void begin_task(WS& W, uint32_t tw, LaneSolve& s, int
 __device__ __forceinline__ void commit_hit(const RoundParams& P, const PairSm& p, int kind, int face, float t, float3 xi,
                                            float3 n, float u) {
   HitState& b = P.state[p.item].best;
-  note_tie(b, t, &P.state[p.item].tie);
+  note_tie(b, p.best_t, t, &P.state[p.item].tie);  // p.best_t: b.t, read when the pair was admitted
   b.t = t;
   b.elem = p.elem;
   b.face = face;
@@ -1023,7 +1023,7 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
     float iso;
     bool iso_on;
     query_ray(P, P.work[item], o, d, iso, iso_on);
-    HitState best = r.best, tie = r.tie;
+    HitState best = r.best;
     float kt = r.kt;
     int ke = r.ke, pass = r.pass, first = r.cursor;
     bool overflow = r.ovf != 0;
@@ -1077,7 +1077,7 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
             pr.te = te;
           }
           visit_warp<N, L>(el, P.fbox + static_cast<int64_t>(ce) * kFaceBoxFloats, ce, o, d, te, tx, iso, iso_on,
-                           best, w, wu, pr, &tie);
+                           best, w, wu, pr, &r.tie);
         }
         kt = ct;
         ke = ce;
@@ -1100,7 +1100,6 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
     __syncwarp();
     if (lane == 0) {
       r.best = best;
-      r.tie = tie;
       r.its += static_cast<int>(its + wu.newton + wu.face - it0);
       r.done = 1;
     }

@@ -11,5 +11,5 @@ template cudaError_t launch_residuals_n<6>(const float*, const uint32_t*, int64_
 template cudaError_t launch_tail_n<6>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, unsigned*, bool,
                                       cudaStream_t);
 template cudaError_t launch_check_n<6>(const TraceParams&, RayState*, const uint32_t*, const unsigned*, uint32_t*,
-                                         unsigned*, int64_t, int, cudaStream_t);
+                                         unsigned*, unsigned*, int64_t, int, cudaStream_t);
 }  // namespace ho
