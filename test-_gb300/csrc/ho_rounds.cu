@@ -141,8 +141,10 @@ __global__ void round_scatter_kernel(const RoundPair* __restrict__ pairs, const 
   sorted[eoff[pelem[k]] + prank[k]] = pairs[k];
 }
 
-// Ctr layout: [0] pairs of the round, [3] failed FP64 checks, and per order n
-// (2..9) the batch count, region start, write cursor and take cursor.
+// Ctr layout: [0] pairs of the round, [3] failed FP64 checks, [4..5] the
+// tail's list count and cursor, [6..7] the check's list count and tie count,
+// and per order n (2..9) the batch count, region start, write cursor and take
+// cursor.
 constexpr int kCtrOrderNb = 16, kCtrOrderOff = 26, kCtrOrderCur = 36, kCtrOrderNext = 46, kCtrWords = 64;
 
 __device__ __forceinline__ int batch_size(int chunk, int order, bool tc) {
