@@ -57,6 +57,10 @@ extern "C" {
 #define HO_FLAG_TIE 16u          /* the hit displaced another within 1e-4 in t (one
                                     surface point claimed twice) and the FP64 tie
                                     rule chose between the two (FP64 check on)       */
+#define HO_FLAG_GRAZING 32u      /* grazing hit: |cos| of the angle between the ray
+                                    and the surface normal below 0.05; a rounding
+                                    can move such a hit to a neighbouring face or
+                                    element                                          */
 
 typedef struct ho_context ho_context;
 
@@ -165,6 +169,7 @@ typedef struct {
   uint64_t fp64_ties_swapped;  /* of those, rays where the displaced hit won
                                 (nearer exact root, or the same point and the
                                 lower element / face index)                  */
+  uint64_t grazing_hits;     /* hits flagged HO_FLAG_GRAZING                  */
 } ho_stats;
 
 /* Replaces: CUDA context/stream set-up and cudaMalloc in FEM-AABB/main.cu:322-511. */

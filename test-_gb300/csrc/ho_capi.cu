@@ -166,6 +166,7 @@ int read_stats(ho_context* c) {
   s.fp64_polished = ds.c[ho::ST_POLISHED];
   s.fp64_ties = ds.c[ho::ST_TIES];
   s.fp64_ties_swapped = ds.c[ho::ST_TIES_SWAPPED];
+  s.grazing_hits = ds.c[ho::ST_GRAZING];
   s.prim_kernel_ns = 0;
   if (c->prim_timed) {
     float ms = 0.f;

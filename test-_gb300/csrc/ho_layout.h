@@ -90,6 +90,7 @@ enum StatSlot {
   ST_POLISHED,  // hits refined by the FP64 polish (check and plain kernels)
   ST_TIES,      // rays with a tie partner that the FP64 tie rule weighed
   ST_TIES_SWAPPED,  // of those, rays whose partner won
+  ST_GRAZING,       // hits with |cos| between ray and surface below kGrazeCos
   ST_COUNT
 };
 

@@ -221,6 +221,7 @@ int path_trace(ho_context* c, const CamArgs& cam, float iso, bool iso_on, int sp
     tot.fp64_polished += st.fp64_polished;
     tot.fp64_ties += st.fp64_ties;
     tot.fp64_ties_swapped += st.fp64_ties_swapped;
+    tot.grazing_hits += st.grazing_hits;
     tot.graph = st.graph;
     tot.max_modes = st.max_modes;
     tot.status |= st.status;

@@ -196,7 +196,9 @@ __global__ void round_batch_kernel(const uint32_t* __restrict__ ecount, const ui
   }
 }
 
-__global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ st) {
+// The queued rays' answers into the call's outputs; count: tally the grazing
+// hits (once per call: a second write-out after extra rounds does not).
+__global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ st, bool count) {
   const unsigned item = blockIdx.x * blockDim.x + threadIdx.x;
   if (item >= *P.qcount) return;
   const int64_t q = P.work[item];
@@ -204,7 +206,14 @@ __global__ void round_finish_kernel(TraceParams P, const RayState* __restrict__ 
   float iso;
   bool iso_on;
   query_ray(P, q, o, d, iso, iso_on);
-  write_result(P, q, d, st[item].best, static_cast<uint32_t>(st[item].its));
+  const HitState& b = st[item].best;
+  write_result(P, q, d, b, static_cast<uint32_t>(st[item].its));
+  if (count) {
+    const unsigned act = __activemask();
+    const unsigned g = __ballot_sync(act, is_grazing(b, d));
+    if (g && static_cast<int>(threadIdx.x & 31) == __ffs(act) - 1)
+      atomicAdd(&P.stats->c[ST_GRAZING], static_cast<unsigned long long>(__popc(g)));
+  }
 }
 
 // Grow-only device buffer of `want` elements of `size` bytes.
@@ -473,7 +482,7 @@ int enqueue_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lea
     const int rc = enqueue_check(c, P, R, s, n_cap);
     if (rc) return rc;
   }
-  round_finish_kernel<<<gi, 256, 0, s>>>(P, R.state);
+  round_finish_kernel<<<gi, 256, 0, s>>>(P, R.state, true);
   RT_TRY(cudaGetLastError());
   return 0;
 }
@@ -498,7 +507,7 @@ int finish_rounds(ho_context* c, const TraceParams& P, cudaStream_t s, bool lear
   if (extra) {
     const int rc = enqueue_check(c, P, R, s, n_cap);
     if (rc) return rc;
-    round_finish_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P, R.state);
+    round_finish_kernel<<<static_cast<unsigned>((n_cap + 255) / 256), 256, 0, s>>>(P, R.state, false);
     RT_TRY(cudaGetLastError());
     ++c->launches;
   }

@@ -253,6 +253,16 @@ __device__ __forceinline__ void query_ray(const TraceParams& P, int64_t q, float
   query_ray_from(P.rays, P.n_rays, P.cam, P.iso, P.iso_on_mask, P.views, P.n_views, q, o, d, iso, iso_on);
 }
 
+// A hit whose ray meets the surface at |cos| below this is grazing: there a
+// rounding can move the hit to a neighbouring face or element, or off the
+// surface (HO_FLAG_GRAZING, ho_stats.grazing_hits).
+constexpr float kGrazeCos = 0.05f;
+__device__ __forceinline__ bool is_grazing(const HitState& b, float3 d) {
+  if (b.kind == HO_HIT_MISS) return false;
+  const float dn = fabsf(b.n.x * d.x + b.n.y * d.y + b.n.z * d.z);
+  return dn < kGrazeCos * sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+}
+
 __device__ __forceinline__ void write_result(const TraceParams& P, int64_t q, float3 d, const HitState& best,
                                              uint32_t iters) {
   if (P.hits) {
@@ -264,7 +274,7 @@ __device__ __forceinline__ void write_result(const TraceParams& P, int64_t q, fl
     h.xi[0] = best.xi.x; h.xi[1] = best.xi.y; h.xi[2] = best.xi.z;
     h.n[0] = best.n.x; h.n[1] = best.n.y; h.n[2] = best.n.z;
     h.u = best.u;
-    h.flags = best.flags;
+    h.flags = best.flags | (is_grazing(best, d) ? HO_FLAG_GRAZING : 0u);
     h.iters = iters;
     P.hits[q] = h;
   }
@@ -501,8 +511,9 @@ __global__ void __launch_bounds__(kTraceBlock) plain_kernel(TraceParams P, int64
   }
   flush_work(P.stats, w, active);
   const unsigned pm = __ballot_sync(kFull, polished), tm = __ballot_sync(kFull, tie_seen),
-                 sm = __ballot_sync(kFull, tie_swapped);
+                 sm = __ballot_sync(kFull, tie_swapped), gm = __ballot_sync(kFull, active && is_grazing(best, d));
   if ((threadIdx.x & 31) == 0) {
+    if (gm) atomicAdd(&P.stats->c[ST_GRAZING], static_cast<unsigned long long>(__popc(gm)));
     if (pm) atomicAdd(&P.stats->c[ST_POLISHED], static_cast<unsigned long long>(__popc(pm)));
     if (tm) atomicAdd(&P.stats->c[ST_TIES], static_cast<unsigned long long>(__popc(tm)));
     if (sm) atomicAdd(&P.stats->c[ST_TIES_SWAPPED], static_cast<unsigned long long>(__popc(sm)));

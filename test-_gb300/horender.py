@@ -31,7 +31,7 @@ MLP_PARAMS, MLP_IN, MLP_OUT = 40328, 48, 8
 NOALLOC_MAX_RAYS = 32768
 HIT_MISS, HIT_FACE, HIT_ISO = 0, 1, 2
 HIT_PRISM, HIT_QUAD, HIT_TRI = 3, 4, 5
-FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW, FLAG_INCOMPLETE, FLAG_TIE = 1, 2, 4, 8, 16
+FLAG_FALLBACK, FLAG_FP64_FAIL, FLAG_OVERFLOW, FLAG_INCOMPLETE, FLAG_TIE, FLAG_GRAZING = 1, 2, 4, 8, 16, 32
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("elem", "<i4"), ("face", "<i2"), ("kind", "<i2"), ("xi", "<f4", 3),
                       ("n", "<f4", 3), ("u", "<f4"), ("flags", "<u4"), ("iters", "<u4")])
@@ -72,7 +72,8 @@ class _Stats(C.Structure):
         ("kernel_launches", C.c_uint64), ("round_kernel_ns", C.c_uint64), ("round_launches", C.c_uint64),
         ("tail_rays", C.c_uint64), ("prim_candidates", C.c_uint64), ("prim_iters", C.c_uint64),
         ("prim_flops", C.c_uint64), ("prim_kernel_ns", C.c_uint64), ("prim_node_visits", C.c_uint64),
-        ("fp64_polished", C.c_uint64), ("fp64_ties", C.c_uint64), ("fp64_ties_swapped", C.c_uint64)]
+        ("fp64_polished", C.c_uint64), ("fp64_ties", C.c_uint64), ("fp64_ties_swapped", C.c_uint64),
+        ("grazing_hits", C.c_uint64)]
 
 
 def _load():

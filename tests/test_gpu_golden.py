@@ -126,6 +126,12 @@ def test_against_reference_and_judge(golden, mode):
         # every ray the FP64 tie rule weighed carries the tie flag
         tied = (g["flags"] & hr.FLAG_TIE) != 0
         assert int(tied.sum()) == st["fp64_ties"] and st["fp64_ties_swapped"] <= st["fp64_ties"]
+        # grazing hits (|cos| < 0.05 between ray and normal) are flagged and counted
+        grazed = (g["flags"] & hr.FLAG_GRAZING) != 0
+        assert int(grazed.sum()) == st["grazing_hits"]
+        d = rays[:, 3:].astype(np.float64)
+        cos = np.abs((g["n"].astype(np.float64) * d).sum(1)) / np.linalg.norm(d, axis=1)
+        assert np.sum(grazed != ((g["kind"] > 0) & (cos < parity.GRAZE))) <= 2  # rounding at the bound
 
         def trace(r, iso=iso):
             return ctx.intersect(r, iso, True)
@@ -135,7 +141,8 @@ def test_against_reference_and_judge(golden, mode):
         print(f"{name} {mode} iso {iso}: rays {rays.shape[0]}, hits {int((ref['kind'] > 0).sum())}, identical "
               f"{agree:.4f}; differ {ex['differ']}: order-dependent {ex['order_dependent']}, tie {ex['tie']}, "
               f"grazing {ex['grazing']}, unstable {ex['unstable']}, unexplained {len(ex['unexplained'])}; "
-              f"FP64 tie rule: weighed {st['fp64_ties']}, partner won {st['fp64_ties_swapped']}")
+              f"FP64 tie rule: weighed {st['fp64_ties']}, partner won {st['fp64_ties_swapped']}; "
+              f"grazing hits {st['grazing_hits']}")
         for i in ex["unexplained"][:5]:
             print("   unexplained", i, g[i][["kind", "elem", "face", "t"]], ref[i][["kind", "elem", "face", "t"]])
         assert not ex["unexplained"]
