@@ -135,15 +135,16 @@ def flops_field(n):  # u and grad: (2n^3 + 3n^2 + 4n) FMA + basis (3 x 8n)
 
 
 # DRAM bytes (read + write) per round-kernel launch, averaged over the 4
-# launches of one step, from an ncu capture of the same workload
-# (dram__bytes_read.sum + dram__bytes_write.sum; the capture command is in
-# profiles/launches_hex32_p6.md). Keyed by workload, image size and mode;
-# absent -> null.
+# launches of a step, from an ncu capture of the same workload
+# (dram__bytes_read.sum + dram__bytes_write.sum over the launches of two
+# learned calls; the capture commands are kept with the launch-list
+# summaries). Keyed by workload, image size and mode; absent -> null.
 ISECT_TRAFFIC = {
     ("hex32_p6", 1920, 1080, "learned"): (424.06e6 + 26.06e6) / 4,
+    ("hex64_p5", 3840, 2160, "learned"): 1540.01e6 / 8,
 }
 # The same for the primitive pass (prim_trace_kernel), per launch, averaged
-# over 5 launches (profiles/launches_prims_sheet.md). Nearly all of it is the
+# over 5 launches. Nearly all of it is the
 # write-back of the threads' spilled stack frames, not algorithmic traffic.
 PRIM_TRAFFIC = {
     ("prims_sheet", 1920, 1080): 176.53e6 + 4569.10e6,

@@ -17,8 +17,9 @@
 //   isosurface:  x(xi) = o + t d and u(xi) = iso (unknowns: xi and t), a
 //                4x4 solve through J^-1.
 // The step's error is quadratic in its size plus the FP32 Jacobian's
-// relative error times its size, so from a residual of 1e-4 it usually lands
-// within about 1e-8; a larger step is followed by up to three more with the
+// relative error times its size, so a step of at most 1e-4 in t and xi
+// (kPolishDone) lands within about 1e-8 times the equations' curvature and
+// ends the polish; a larger step is followed by up to three more with the
 // residual re-evaluated in FP64 (kPolishSteps). The hit keeps its
 // element, face and kind; t, xi and u move to the root of the same equations,
 // which leaves t within FP32 rounding of the exact root. A step in t larger
@@ -166,6 +167,9 @@ __device__ void fp64_residuals(const float* __restrict__ rec_all, int elem, floa
 // keeps the previous one: a chord step, whose error shrinks by about the
 // relative change of J across that step).
 constexpr int kPolishSteps = 4;
+// A step at most this large in t and in xi ends the polish without another
+// FP64 evaluation (its remaining error is about its square).
+constexpr double kPolishDone = 1e-4;
 
 // One Newton step on a hit's defining equations (file header): from the
 // FP64 residual r and field value u at (t, xi), with the FP32 Jacobian J and
@@ -263,7 +267,7 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
     un = u + (g.x * dx[0] + g.y * dx[1] + g.z * dx[2]);
     // a step this small leaves an error far below FP32 rounding of t and xi
     const double mx = fmax(fabs(dx[0]), fmax(fabs(dx[1]), fabs(dx[2])));
-    if (step + 1 == kPolishSteps || (mx <= 1e-5 && fabs(dt) <= 1e-7)) break;
+    if (step + 1 == kPolishSteps || (mx <= kPolishDone && fabs(dt) <= kPolishDone)) break;
     if (mx > 1e-3)
       jacobian_at(make_float3(static_cast<float>(x0), static_cast<float>(x1), static_cast<float>(x2)));
     fp64_residual_vec<N>(rec_all, h.elem, o, d, t, x0, x1, x2, has_field, r, u);
