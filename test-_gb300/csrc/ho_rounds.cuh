@@ -192,6 +192,7 @@ struct LaneSolve {
   float t;    // inverse map: the sample's t; face Newton: tau
   int it, cap;
   bool warm, post, inited;
+  bool nb;     // sample: the neighbour restart was taken
   float prev;  // face Newton: residual of the last iteration
 };
 
@@ -219,6 +220,7 @@ __device__ __forceinline__ void start_sample_solve(LaneSolve& s, float t, bool w
   s.it = 0;
   s.cap = warm ? warm_cap : 50;
   s.post = false;
+  s.nb = false;
 }
 
 
@@ -559,7 +561,7 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
     s.t = 0.f;
     s.it = 0;
     s.cap = 0;
-    s.warm = s.post = s.inited = false;
+    s.warm = s.post = s.inited = s.nb = false;
     s.prev = FLT_MAX;
     // every task ends within a bounded number of steps; the guard is far above
     // the longest legal batch and only reports a broken invariant
@@ -750,14 +752,35 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
           if (s.warm && end != 0) {
             if (end == 1) {
               ++w.accepted;
-            } else {  // the warm start failed: the plain cold start answers
+            } else {
               ++w.rejected;
-              atomicOr(&p.fl, 8);
               atomicAdd(&p.its, s.it);
-              s.warm = false;
-              s.xi = make_float3(0.f, 0.f, 0.f);
+              // a sample whose network start failed starts once more from
+              // the converged sample of its pair nearest to it (stored in an
+              // earlier step); then, or without one, the plain cold start
+              // answers
+              int nb = -1;
+              if (s.kind == TK_SAMPLE && !s.nb) {
+                int bd = kSamples;
+                for (unsigned m = ld_ctl(&p.okm); m; m &= m - 1u) {
+                  const int j = __ffs(m) - 1, dj = abs(j - s.arg);
+                  if (dj < bd) {
+                    bd = dj;
+                    nb = j;
+                  }
+                }
+              }
+              if (nb >= 0) {
+                s.nb = true;
+                s.xi = ld3(p.sx[nb]);
+                s.cap = P.warm_cap;
+              } else {
+                atomicOr(&p.fl, 8);
+                s.warm = false;
+                s.xi = make_float3(0.f, 0.f, 0.f);
+                s.cap = 50;
+              }
               s.it = 0;
-              s.cap = 50;
               s.post = false;
               end = 0;
             }
@@ -814,6 +837,9 @@ __global__ void __launch_bounds__(kRoundBlock) round_kernel(RoundParams P) {
         }
         if (end != 0) atomicAdd(&p.its, s.it);
       }
+      // every lane has read the pair state of this step (the neighbour
+      // restart reads the sample store) before any lane writes to it
+      __syncwarp();
       // face seeds: the lowest accepted seed index of each face wins
       const bool seed_ok = act && end == 1 && s.kind == TK_FSEED;
       if (seed_ok) atomicMin(&W.pr[s.pp].fseed[s.arg / 9], s.arg % 9);
