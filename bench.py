@@ -347,8 +347,10 @@ def cpu_baseline(name, n_queries, seed=12345):
     w, views, path_kw = hex_workload(name)
     ob, osc = oracle_scene(w)
     rng = np.random.default_rng(seed)
-    rays, isos = sample_queries(ob, w, views, n_queries, rng)
     threads = os.cpu_count() or 1
+    warm_rays, warm_isos = sample_queries(ob, w, views, 256, rng)
+    trace_sample(osc, warm_rays, warm_isos, threads)  # untimed: threads and pages warm, as the reference arm's warm-up
+    rays, isos = sample_queries(ob, w, views, n_queries, rng)
     t0 = time.perf_counter()
     trace_sample(osc, rays, isos, threads)
     dt = time.perf_counter() - t0
