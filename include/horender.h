@@ -319,6 +319,10 @@ int ho_intersect(ho_context* ctx, int64_t n, const float* rays, float iso, int i
 /* Device-buffer variant (rays_dev, out_dev on the device). */
 int ho_intersect_device(ho_context* ctx, int64_t n, const float* rays_dev, float iso, int iso_enabled,
                         ho_hit* out_dev, void* stream);
+/* ho_intersect with the rays as structure of arrays: ray_soa holds 6 arrays
+ * of n floats back to back (origin x, y, z, then direction x, y, z), host
+ * memory. The same answers as ho_intersect on the same rays. */
+int ho_intersect_soa(ho_context* ctx, int64_t n, const float* ray_soa, float iso, int iso_enabled, ho_hit* out);
 
 /* Allocation-free variant of ho_intersect_device (batched mode). No
  * reference counterpart. For callers that may not call the CUDA allocator

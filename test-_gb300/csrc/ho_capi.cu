@@ -833,6 +833,37 @@ int ho_intersect(ho_context* c, int64_t n, const float* rays, float iso, int iso
   return read_stats(c);
 }
 
+namespace {
+// rays from 6 arrays of n (ox, oy, oz, dx, dy, dz) to n records of 6 floats
+__global__ void soa_to_rays_kernel(const float* __restrict__ soa, int64_t n, float* __restrict__ rays) {
+  const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) rays[6 * i + k] = soa[k * n + i];
+}
+}  // namespace
+
+int ho_intersect_soa(ho_context* c, int64_t n, const float* ray_soa, float iso, int iso_enabled, ho_hit* out) {
+  if (!c) return HO_ERR_ARG;
+  if (!c->built) return fail(c, HO_ERR_STATE, "call ho_build_bvh first");
+  if (n < 0) return fail(c, HO_ERR_ARG, "n must be >= 0");
+  if (n > 0 && (!ray_soa || !out)) return fail(c, HO_ERR_ARG, "null buffer");
+  int rc;
+  // the upload in the second half of the ray buffer, the records in the first
+  if ((rc = ensure_buf(c, c->d_rays, c->rays_cap, static_cast<size_t>(n) * 12, "cudaMalloc(rays)"))) return rc;
+  if ((rc = ensure_buf(c, c->d_hits, c->hits_cap, static_cast<size_t>(n), "cudaMalloc(hits)"))) return rc;
+  if (n > 0) {
+    float* soa = c->d_rays + static_cast<size_t>(n) * 6;
+    CK(cudaMemcpyAsync(soa, ray_soa, n * 6 * sizeof(float), cudaMemcpyHostToDevice, c->stream), "upload rays");
+    soa_to_rays_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, c->stream>>>(soa, n, c->d_rays);
+    CK(cudaGetLastError(), "soa_to_rays_kernel");
+  }
+  rc = ho_intersect_device(c, n, c->d_rays, iso, iso_enabled, c->d_hits, c->stream);
+  if (rc) return rc;
+  if (n > 0) CK(cudaMemcpyAsync(out, c->d_hits, n * sizeof(ho_hit), cudaMemcpyDeviceToHost, c->stream), "read hits");
+  return read_stats(c);
+}
+
 int ho_path_trace_device(ho_context* c, const ho_camera* cam, const float* iso, int n_iso, int W, int H, int spp,
                          int max_depth, uint64_t seed, int iso_zero_disables, uint8_t* rgb_dev, int64_t* rays_traced,
                          void* stream) {

@@ -113,6 +113,7 @@ def _load():
     L.ho_intersect.argtypes = [vp, i64, vp, f32, i32, vp]
     L.ho_hit_residuals.argtypes = [vp, i64, vp, vp, vp]
     L.ho_intersect_device.argtypes = [vp, i64, vp, f32, i32, vp, vp]
+    L.ho_intersect_soa.argtypes = [vp, i64, vp, f32, i32, vp]
     L.ho_set_mode.argtypes = [vp, i32]
     L.ho_set_option.argtypes = [vp, i32, i64]
     L.ho_get_option.argtypes = [vp, i32, C.POINTER(C.c_int64)]
@@ -431,6 +432,13 @@ class Context:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
         out = np.zeros(rays.shape[0], HIT_DTYPE)
         self._ck(lib.ho_intersect(self.h, rays.shape[0], _p(rays), float(iso), int(iso_enabled), _p(out)))
+        return out
+
+    def intersect_soa(self, ray_soa: np.ndarray, iso: float, iso_enabled: bool = True) -> np.ndarray:
+        """ho_intersect_soa: ray_soa is (6, n) (origin x, y, z, direction x, y, z)."""
+        ray_soa = np.ascontiguousarray(ray_soa, np.float32).reshape(6, -1)
+        out = np.zeros(ray_soa.shape[1], HIT_DTYPE)
+        self._ck(lib.ho_intersect_soa(self.h, ray_soa.shape[1], _p(ray_soa), float(iso), int(iso_enabled), _p(out)))
         return out
 
     def hit_residuals(self, rays: np.ndarray, hits: np.ndarray) -> np.ndarray:

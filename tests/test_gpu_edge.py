@@ -62,6 +62,22 @@ def test_rays_from_inside_and_outside_match_oracle(small, oracle, mode):
         ctx.set_mode(hr.MODE_BATCHED)
 
 
+@pytest.mark.parametrize("n", [0, 1, 33, 5000])
+def test_soa_rays_give_the_same_hits(small, n):
+    """ho_intersect_soa (6 arrays of n floats) answers as ho_intersect on the
+    same rays, bit for bit, for empty and ragged counts."""
+    ctx, w, osc = small
+    rng = np.random.default_rng(7 + n)
+    o = rng.uniform(-0.5, 1.5, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.maximum(np.linalg.norm(d, axis=1, keepdims=True), 1e-6)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    a = ctx.intersect(rays, 0.2, True)
+    b = ctx.intersect_soa(np.ascontiguousarray(rays.T), 0.2, True)
+    assert a.shape == b.shape == (n,)
+    assert a.tobytes() == b.tobytes()
+
+
 def test_rays_pointing_away_all_miss(small):
     ctx, w, osc = small
     n = 500
