@@ -153,7 +153,11 @@ def errors(gpu, judge, rays, h: float) -> dict:
         du = np.abs(gpu["u"][m].astype(np.float64) - judge["u"][m])[inside]
         if not inside.any():
             dxi = du = np.zeros(1)
-        res[lab] = {"n": int(m.sum()), "t_max_over_h": float(dt.max() / h),
+        # hits whose reference coordinates lie outside the element ([-1, 1]^3
+        # by more than 1e-4): isosurface roots found in the padded box's
+        # extrapolation beyond the element, as the reference finds them
+        outside = int((np.abs(gx).max(1) > 1.0 + 1e-4).sum())
+        res[lab] = {"n": int(m.sum()), "xi_outside_element": outside, "t_max_over_h": float(dt.max() / h),
                     "t_p99_over_h": float(np.quantile(dt, .99) / h), "xi_max": float(dxi.max()),
                     "xi_p99": float(np.quantile(dxi, .99)), "u_max": float(du.max()),
                     "u_p99": float(np.quantile(du, .99)), "other_preimage": int((~inside).sum())}
