@@ -75,26 +75,62 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// A double-single number: the unevaluated sum hi + lo of two floats, |lo| at
+// most half an ulp of hi, about 48 significant bits.
+struct Ds {
+  float hi, lo;
+};
+
+__device__ __forceinline__ Ds ds_of(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - static_cast<double>(h))};
+}
+
+// (s, e) with s + e == a + b exactly, s the rounded sum (renormalisation).
+__device__ __forceinline__ Ds ds_norm(float a, float b) {
+  Ds r;
+  two_sum(a, b, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ Ds ds_add(Ds a, Ds b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  return ds_norm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+// The product's high part exact by an FMA-based TwoProduct, the cross terms
+// added in FP32.
+__device__ __forceinline__ Ds ds_mul(Ds a, Ds b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return ds_norm(p, e);
+}
+
 // Value of one coefficient block (rows padded to row_stride(N), a multiple of
-// 4 floats, so a row is RS/4 aligned float4 loads), FP64-accurate.
+// 4 floats, so a row is RS/4 aligned float4 loads), FP64-accurate, computed
+// in double-single arithmetic on the FP32 pipes.
 //
-// The coefficients are FP32, so the innermost sums sum_i c_i a_i are formed
-// in double-single arithmetic on the FP32 pipes: a_i = ah_i + al_i (two
-// floats), c_i ah_i = p + ep exactly (FMA-based TwoProduct), the running sum
-// kept as sh + sl with TwoSum, the small parts added in FP32. That is about
-// 2^-44 relative per row, below FP64's own rounding of the outer sums, and
-// avoids an FP64 conversion and FMA per coefficient (FP64 runs at a small
-// fraction of the FP32 rate here). The sums over j and k, and the residuals,
-// are FP64.
+// The coefficients are FP32. The innermost sums sum_i c_i a_i: a_i = ah_i +
+// al_i (two floats), c_i ah_i = p + ep exactly (TwoProduct), the running sum
+// kept as sh + sl with TwoSum, the small parts added in FP32. The sums over j
+// and k multiply and add double-single numbers (ds_mul, ds_add). Each
+// operation is good to about 2^-44 relative, below what the check and the
+// polish need by orders of magnitude (the residuals agree with the FP64
+// oracle's to 1e-10), and no FP64 instruction runs per coefficient or per
+// row: GB300's FP64 rate is a small fraction of its FP32 rate, and with FP64
+// sums over j and k the check kernel kept the FP64 pipe 72% busy.
 template <int N>
 __device__ double value64(const float* __restrict__ blk, const float (&ah)[N], const float (&al)[N],
-                          const double (&as)[N], const double (&at)[N]) {
+                          const Ds (&as)[N], const Ds (&at)[N]) {
   constexpr int RS = row_stride(N);
   static_assert(RS % 4 == 0, "rows are whole float4s");
-  double v = 0.0;
+  Ds v = {0.f, 0.f};
 #pragma unroll 1
   for (int k = 0; k < N; ++k) {
-    double q = 0.0;
+    Ds q = {0.f, 0.f};
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       const float4* row = reinterpret_cast<const float4*>(blk + (k * N + j) * RS);
@@ -117,15 +153,15 @@ __device__ double value64(const float* __restrict__ blk, const float (&ah)[N], c
         sh = s;
         sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(es, ep), __fmul_rn(c[i], al[i])));
       }
-      q = fma(static_cast<double>(sh) + static_cast<double>(sl), as[j], q);
+      q = ds_add(q, ds_mul(ds_norm(sh, sl), as[j]));
     }
-    double atk = 0.0;  // at[k] by selection: the array stays in registers
+    Ds atk = at[0];  // at[k] by selection: the array stays in registers
 #pragma unroll
-    for (int kk = 0; kk < N; ++kk)
+    for (int kk = 1; kk < N; ++kk)
       if (kk == k) atk = at[kk];
-    v = fma(q, atk, v);
+    v = ds_add(v, ds_mul(q, atk));
   }
-  return v;
+  return static_cast<double>(v.hi) + static_cast<double>(v.lo);
 }
 
 // The FP64 residual vector r = x(xi) - (o + t d) of a point in element elem,
@@ -140,15 +176,18 @@ __device__ __noinline__ void fp64_residual_vec(const float* __restrict__ rec_all
   basis_val64<N>(x1, as);
   basis_val64<N>(x2, at);
   float ah[N], al[N];  // ar as two floats
+  Ds sd[N], td[N];     // as, at double-single
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     ah[i] = static_cast<float>(ar[i]);
     al[i] = static_cast<float>(ar[i] - static_cast<double>(ah[i]));
+    sd[i] = ds_of(as[i]);
+    td[i] = ds_of(at[i]);
   }
-  r[0] = value64<N>(rec, ah, al, as, at) - (static_cast<double>(o.x) + t * d.x);
-  r[1] = value64<N>(rec + block_floats(N), ah, al, as, at) - (static_cast<double>(o.y) + t * d.y);
-  r[2] = value64<N>(rec + 2 * block_floats(N), ah, al, as, at) - (static_cast<double>(o.z) + t * d.z);
-  u = want_field ? value64<N>(rec + 3 * block_floats(N), ah, al, as, at) : 0.0;
+  r[0] = value64<N>(rec, ah, al, sd, td) - (static_cast<double>(o.x) + t * d.x);
+  r[1] = value64<N>(rec + block_floats(N), ah, al, sd, td) - (static_cast<double>(o.y) + t * d.y);
+  r[2] = value64<N>(rec + 2 * block_floats(N), ah, al, sd, td) - (static_cast<double>(o.z) + t * d.z);
+  u = want_field ? value64<N>(rec + 3 * block_floats(N), ah, al, sd, td) : 0.0;
 }
 
 // The FP64 residuals of a hit at xi in element elem: the largest component
