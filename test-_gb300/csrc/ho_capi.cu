@@ -242,6 +242,7 @@ void ho_destroy(ho_context* c) {
     cudaFree(c->rounds.batches);
     cudaFree(c->rounds.ecount);
     cudaFree(c->rounds.eoff);
+    cudaFree(c->rounds.tile_sums);
     cudaFree(c->rounds.ctr);
     cudaFree(c->rounds.fail);
     if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);

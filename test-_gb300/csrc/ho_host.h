@@ -133,6 +133,8 @@ struct RoundBufs {
   size_t ecount_cap = 0;
   uint32_t* eoff = nullptr;
   size_t eoff_cap = 0;
+  uint32_t* tile_sums = nullptr;  // per 4096 elements, for the offsets' scan
+  size_t tile_sums_cap = 0;
   unsigned* ctr = nullptr;   // pairs, batches, next batch, failed FP64 checks
   size_t ctr_cap = 0;
   uint32_t* fail = nullptr;  // queue items whose hit failed the FP64 check
