@@ -1058,7 +1058,12 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
     float kt = r.kt;
     int ke = r.ke, pass = r.pass, first = r.cursor;
     bool overflow = r.ovf != 0;
-    const uint32_t it0 = wu.newton + wu.face + w.newton + w.face;
+    // this ray's iterations: the warp's (per-lane w summed, wu once) now less
+    // at the start
+    uint32_t w0 = w.newton + w.face;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) w0 += __shfl_xor_sync(kFull, w0, off);
+    const uint32_t it0 = wu.newton + wu.face + w0;
     float bt[kCandK];
     int be[kCandK];
     const float2* kb = P.kbuf + static_cast<int64_t>(item) * kCandK;
@@ -1147,12 +1152,18 @@ __global__ void __launch_bounds__(kTraceBlock) tail_kernel(TraceParams P, RaySta
 template <int N>
 cudaError_t launch_tail_n(const TraceParams& P, RayState* st, const uint32_t* list, const unsigned* n_list,
                           unsigned* next, bool learned, cudaStream_t s) {
-  static int grid[2] = {0, 0};
+  // persistent grid per device and form (kernel attributes are set per
+  // device); two host threads that fill the same entry at once store the same
+  // value
+  static std::atomic<int> grid[kGridCacheDevices][2];
   const size_t smem = static_cast<size_t>(kTraceBlock / 32) * record_floats(N) * sizeof(float);
-  int& g = grid[learned ? 1 : 0];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kGridCacheDevices) return cudaErrorInvalidDevice;
+  int g = grid[dev][learned ? 1 : 0].load(std::memory_order_acquire);
   if (g == 0) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
+    int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (learned) {
       cudaFuncSetAttribute(tail_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -1162,6 +1173,7 @@ cudaError_t launch_tail_n(const TraceParams& P, RayState* st, const uint32_t* li
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tail_kernel<N, false>, kTraceBlock, smem);
     }
     g = sms * (per > 0 ? per : 1);
+    grid[dev][learned ? 1 : 0].store(g, std::memory_order_release);
   }
   if (learned) tail_kernel<N, true><<<g, kTraceBlock, smem, s>>>(P, st, list, n_list, next);
   else tail_kernel<N, false><<<g, kTraceBlock, smem, s>>>(P, st, list, n_list, next);
@@ -1173,11 +1185,20 @@ static cudaError_t launch_round_kernel(const RoundParams& R, cudaStream_t s) {
   // persistent grid: resident blocks per SM x SMs (the tensor-core form holds
   // all of an SM's tensor memory, so one CTA per SM: its shared memory request
   // is raised to more than half of the SM's)
-  static int grid = 0;
-  static size_t smem = 0;
-  if (grid == 0) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
+  // per device (kernel attributes are set per device); two host threads that
+  // fill the same entry at once store the same values. The grid is stored
+  // last (release) and read first (acquire), so a thread that sees it sees
+  // the shared-memory size and the attribute set before it.
+  static std::atomic<int> grid[kGridCacheDevices];
+  static std::atomic<int> smem_of[kGridCacheDevices];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kGridCacheDevices) return cudaErrorInvalidDevice;
+  int g = grid[dev].load(std::memory_order_acquire);
+  size_t smem = static_cast<size_t>(smem_of[dev].load(std::memory_order_relaxed));
+  if (g == 0) {
+    int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     smem = round_tc_off<N, TC>() + (kRoundBlock / 32) * ((sizeof(WarpSm<N, !TC>) + 15) / 16 * 16);
     if (TC) {
@@ -1187,9 +1208,11 @@ static cudaError_t launch_round_kernel(const RoundParams& R, cudaStream_t s) {
     }
     cudaFuncSetAttribute(round_kernel<N, L, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, round_kernel<N, L, TC>, kRoundBlock, smem);
-    grid = sms * (TC ? 1 : (per > 0 ? per : 1));
+    g = sms * (TC ? 1 : (per > 0 ? per : 1));
+    smem_of[dev].store(static_cast<int>(smem), std::memory_order_relaxed);
+    grid[dev].store(g, std::memory_order_release);
   }
-  round_kernel<N, L, TC><<<grid, kRoundBlock, smem, s>>>(R);
+  round_kernel<N, L, TC><<<g, kRoundBlock, smem, s>>>(R);
   return cudaGetLastError();
 }
 

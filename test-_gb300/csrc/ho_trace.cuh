@@ -536,7 +536,7 @@ cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads,
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kGridCacheDevices) return cudaErrorInvalidDevice;
-  int g = grid[dev][learned ? 1 : 0].load(std::memory_order_relaxed);
+  int g = grid[dev][learned ? 1 : 0].load(std::memory_order_acquire);
   if (g == 0) {
     const int smem_i = static_cast<int>((kTraceBlock / 32) * record_floats(N) * sizeof(float));
     int sms = 0, per = 0;
@@ -549,7 +549,7 @@ cudaError_t launch_n(const TraceParams& P, int64_t n_queries, int64_t n_threads,
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, isect_kernel<N, false>, kTraceBlock, smem_i);
     }
     g = sms * (per > 0 ? per : 1);
-    grid[dev][learned ? 1 : 0].store(g, std::memory_order_relaxed);
+    grid[dev][learned ? 1 : 0].store(g, std::memory_order_release);
   }
   const size_t smem = static_cast<size_t>(kTraceBlock / 32) * record_floats(N) * sizeof(float);
   if (learned) isect_kernel<N, true><<<g, kTraceBlock, smem, s>>>(P);

@@ -65,7 +65,8 @@ def test_rays_from_inside_and_outside_match_oracle(small, oracle, mode):
 @pytest.mark.parametrize("n", [0, 1, 33, 5000])
 def test_soa_rays_give_the_same_hits(small, n):
     """ho_intersect_soa (6 arrays of n floats) answers as ho_intersect on the
-    same rays, bit for bit, for empty and ragged counts."""
+    same rays, bit for bit, for empty and ragged counts (all fields but the
+    per-hit iteration count, which the order of a round's pairs can move)."""
     ctx, w, osc = small
     rng = np.random.default_rng(7 + n)
     o = rng.uniform(-0.5, 1.5, (n, 3)).astype(np.float32)
@@ -75,6 +76,8 @@ def test_soa_rays_give_the_same_hits(small, n):
     a = ctx.intersect(rays, 0.2, True)
     b = ctx.intersect_soa(np.ascontiguousarray(rays.T), 0.2, True)
     assert a.shape == b.shape == (n,)
+    a["iters"] = 0
+    b["iters"] = 0
     assert a.tobytes() == b.tobytes()
 
 
