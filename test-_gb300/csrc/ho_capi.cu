@@ -1337,17 +1337,20 @@ int ho_save_ppm(const uint8_t* rgb, int W, int H, const char* path) {
 // 0, the image data a zlib stream (RFC 1950) of stored deflate blocks
 // (RFC 1951, uncompressed), chunk CRC-32 over type and data.
 namespace {
-uint32_t png_crc(const uint8_t* p, size_t n, uint32_t c = 0xffffffffu) {
-  static uint32_t table[256];
-  static bool ready = false;
-  if (!ready) {
+struct CrcTable {
+  uint32_t v[256];
+  CrcTable() {
     for (uint32_t i = 0; i < 256; ++i) {
-      uint32_t v = i;
-      for (int k = 0; k < 8; ++k) v = (v & 1u) ? 0xedb88320u ^ (v >> 1) : v >> 1;
-      table[i] = v;
+      uint32_t x = i;
+      for (int k = 0; k < 8; ++k) x = (x & 1u) ? 0xedb88320u ^ (x >> 1) : x >> 1;
+      v[i] = x;
     }
-    ready = true;
   }
+};
+
+uint32_t png_crc(const uint8_t* p, size_t n, uint32_t c = 0xffffffffu) {
+  static const CrcTable crc;  // built once, thread-safe
+  const uint32_t* table = crc.v;
   for (size_t i = 0; i < n; ++i) c = table[(c ^ p[i]) & 0xffu] ^ (c >> 8);
   return c;
 }

@@ -226,15 +226,18 @@ void id_range(const std::string& tok, int& lo, int& hi) {
 }
 
 // ---- base64 + inflate (RFC 1950/1951) --------------------------------------
-std::vector<uint8_t> base64(const std::string& in) {
-  static int8_t lut[256];
-  static bool init = false;
-  if (!init) {
-    std::memset(lut, -1, sizeof(lut));
+struct B64Table {
+  int8_t v[256];
+  B64Table() {
+    std::memset(v, -1, sizeof(v));
     const char* a = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
-    for (int i = 0; i < 64; ++i) lut[static_cast<unsigned char>(a[i])] = static_cast<int8_t>(i);
-    init = true;
+    for (int i = 0; i < 64; ++i) v[static_cast<unsigned char>(a[i])] = static_cast<int8_t>(i);
   }
+};
+
+std::vector<uint8_t> base64(const std::string& in) {
+  static const B64Table table;  // built once, thread-safe
+  const int8_t* lut = table.v;
   std::vector<uint8_t> out;
   uint32_t acc = 0;
   int bits = 0;

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -189,12 +190,17 @@ size_t mlp_infer_smem() { return sizeof(InferSmem); }
 
 int mlp_infer(const MlpDev& P, const void* X, int64_t M, const unsigned* m_dev, int rows_per_item, float* Y,
               cudaStream_t s, int grid) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(sizeof(InferSmem)));
+  // the attribute is set once per device
+  static std::atomic<bool> attr[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return int(e);
+  if (dev < 0 || dev >= 64) return int(cudaErrorInvalidDevice);
+  if (!attr[dev].load(std::memory_order_acquire)) {
+    e = cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(sizeof(InferSmem)));
     if (e != cudaSuccess) return int(e);
-    attr = true;
+    attr[dev].store(true, std::memory_order_release);
   }
   mlp_infer_kernel<<<grid, 256, sizeof(InferSmem), s>>>(P, static_cast<const bf16*>(X), M, m_dev, rows_per_item, Y);
   return int(cudaGetLastError());

@@ -112,12 +112,17 @@ __global__ void __launch_bounds__(256) pred_kernel(MlpDev M, TraceParams P, int3
 }
 
 static int launch_pred(ho_context* c, const TraceParams& P, cudaStream_t s, int sms) {
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(pred_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               static_cast<int>(sizeof(InferSmem)));
+  // the attribute is set once per device
+  static std::atomic<bool> attr[kGridCacheDevices];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return int(e);
+  if (dev < 0 || dev >= kGridCacheDevices) return int(cudaErrorInvalidDevice);
+  if (!attr[dev].load(std::memory_order_acquire)) {
+    e = cudaFuncSetAttribute(pred_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(sizeof(InferSmem)));
     if (e != cudaSuccess) return int(e);
-    attr = true;
+    attr[dev].store(true, std::memory_order_release);
   }
   pred_kernel<<<sms, 256, sizeof(InferSmem), s>>>(c->mlp.dev(), P, c->d_cand, c->d_pred);
   return int(cudaGetLastError());
