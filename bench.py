@@ -427,7 +427,7 @@ def error_vs_fp64(ctx, hr, args, w, views, modes, codes):
         for iso in np.unique(isos):
             m = isos == iso
             g[m] = ctx.intersect(rays[m], float(iso), True)
-        cls = {k: 0 for k in ("differ", "tie", "grazing", "unstable", "other")}
+        cls = {k: 0 for k in ("differ", "tie", "grazing", "second_root", "unstable", "other")}
         for iso in np.unique(isos):
             m = np.where(isos == iso)[0]
             c = parity.counts(parity.classify(g[m], o64[m], rays[m], osc, float(iso),

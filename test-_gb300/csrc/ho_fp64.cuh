@@ -207,7 +207,8 @@ __device__ void fp64_residuals(const float* __restrict__ rec_all, int elem, floa
 // relative change of J across that step).
 constexpr int kPolishSteps = 4;
 // A step at most this large in t and in xi ends the polish without another
-// FP64 evaluation (its remaining error is about its square).
+// FP64 evaluation (its remaining error is about its square), where the ray
+// meets the surface at |cos| >= 0.2.
 constexpr double kPolishDone = 1e-4;
 
 // One Newton step on a hit's defining equations (file header): from the
@@ -295,6 +296,8 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
     }
   };
   jacobian_at(h.xi);
+  const float dn = fabsf(h.n.x * d.x + h.n.y * d.y + h.n.z * d.z);
+  const bool steep = dn >= 0.2f * sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
   double t = h.t, x0 = h.xi.x, x1 = h.xi.y, x2 = h.xi.z, un = u;
   for (int step = 0; step < kPolishSteps; ++step) {
     double dx[3], dt;
@@ -304,9 +307,13 @@ __device__ bool fp64_check_polish(const float* __restrict__ rec_all, const uint3
     x1 += dx[1];
     x2 += dx[2];
     un = u + (g.x * dx[0] + g.y * dx[1] + g.z * dx[2]);
-    // a step this small leaves an error far below FP32 rounding of t and xi
+    // a step this small leaves an error far below FP32 rounding of t and xi;
+    // on a ray that meets the surface at a shallow angle the equations are
+    // ill-conditioned (the error grows like 1/|d.n|), so there only a step
+    // below FP32 rounding ends the polish without another FP64 evaluation
     const double mx = fmax(fabs(dx[0]), fmax(fabs(dx[1]), fabs(dx[2])));
-    if (step + 1 == kPolishSteps || (mx <= kPolishDone && fabs(dt) <= kPolishDone)) break;
+    const double done = steep ? kPolishDone : 1e-7;
+    if (step + 1 == kPolishSteps || (mx <= done && fabs(dt) <= done)) break;
     if (mx > 1e-3)
       jacobian_at(make_float3(static_cast<float>(x0), static_cast<float>(x1), static_cast<float>(x2)));
     fp64_residual_vec<N>(rec_all, h.elem, o, d, t, x0, x1, x2, has_field, r, u);

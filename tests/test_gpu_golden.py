@@ -84,7 +84,8 @@ def explain(g, ref, rays, order, count, osc, iso, trace):
     """Indices of the differing rays per explanation; 'unexplained' must be empty."""
     judge = osc.polish(rays, ref, iso)
     diff = np.where(~parity.same_hit(g, ref, judge))[0]
-    out = {"differ": diff.size, "order_dependent": 0, "tie": 0, "grazing": 0, "unstable": 0, "unexplained": []}
+    out = {"differ": diff.size, "order_dependent": 0, "tie": 0, "grazing": 0, "second_root": 0, "unstable": 0,
+           "unexplained": []}
     if diff.size == 0:
         return out
     replay = osc.trace_replay(rays[diff], iso, True, order[diff], count[diff], precision=32)
@@ -96,7 +97,7 @@ def explain(g, ref, rays, order, count, osc, iso, trace):
     if gi.size:
         c = parity.classify(g[diff[gi]], ours[gi], rays[diff[gi]], osc, iso, product_trace=trace,
                             judge=osc.polish(rays[diff[gi]], ours[gi], iso))
-        for k in ("tie", "grazing", "unstable"):
+        for k in ("tie", "grazing", "second_root", "unstable"):
             out[k] += c[k].size
         out["unexplained"] += list(diff[gi][c["other"]])
     # the rest: the product against the reference directly
@@ -104,7 +105,7 @@ def explain(g, ref, rays, order, count, osc, iso, trace):
     if ri.size:
         c = parity.classify(g[diff[ri]], ref[diff[ri]], rays[diff[ri]], osc, iso, product_trace=trace,
                             judge=judge[diff[ri]])
-        for k in ("tie", "grazing", "unstable"):
+        for k in ("tie", "grazing", "second_root", "unstable"):
             out[k] += c[k].size
         out["unexplained"] += list(diff[ri][c["other"]])
     return out

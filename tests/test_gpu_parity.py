@@ -367,22 +367,56 @@ def test_render_views_equals_single_views(small, mode):
 def test_uneven_multiview_matches_oracle(mixed, oracle):
     """The uneven-work configuration at small scale: mixed orders, 8 seeded
     sphere views of different resolutions and 1-4 isovalues each, all in one
-    call, batched and learned, against the oracle view by view."""
+    call, batched and learned, against the FP64 oracle view by view: every
+    identity difference classified (tests/parity.py), errors within the
+    bounds."""
     ctx, arrs, osc = mixed
     cams, ws, hs, isos = hr.sphere_views(n_views=8, seed=3, shrink=16)
     ctx.train_mlp(n_samples=200_000, steps=300, batch=2048, lr=2e-3, seed=5)
     for mode in (hr.MODE_BATCHED, hr.MODE_LEARNED):
         ctx.set_mode(mode)
         _, hits, offs = ctx.render_views(cams, ws, hs, isos, want_rgb=False, want_hits=True)
-        bad = total = 0
         for v in range(len(cams)):
             rays = oracle.camera_rays(cams[v].lookfrom, cams[v].lookat, cams[v].vup, cams[v].vfov_deg, ws[v], hs[v])
             npix = ws[v] * hs[v]
             for k, iso in enumerate(isos[v]):
                 h = hits[offs[v] + k * npix:offs[v] + (k + 1) * npix]
-                ref, _ = osc.trace(rays, iso, True, precision=32)
-                bad += int((~classify(h, ref)).sum())
-                total += npix
-        print(f"uneven multi-view, mode {mode}: {total} queries, {bad} differ from the oracle")
-        assert bad <= max(2, int(0.005 * total))
+                # the multi-view call answers as the single-ray path on the same
+                # rays (learned: a failed network start restarts from whichever
+                # neighbour converged first, which the batch order decides, so
+                # a ray at a decision boundary may take the other answer)
+                same = classify(h, ctx.intersect(rays, iso, True))
+                assert same.all() if mode == hr.MODE_BATCHED else same.mean() >= 0.999
+                parity.check_against_oracle(h, rays, osc, iso, True, mixed_h(arrs),
+                                            product_trace=lambda r, iso=iso: ctx.intersect(r, iso, True),
+                                            label=f"multi-view mode {mode} view {v} iso {iso}")
     ctx.set_mode(hr.MODE_BATCHED)
+
+
+def test_views64_scene_against_oracle(oracle):
+    """The uneven-work configuration's own scene (48^3 hexes, P 2..8 per
+    element) with two of its 64 sphere views at 1/8 resolution and their first
+    isovalue, batched and learned: every identity difference classified and
+    errors within the bounds of the FP64 judge."""
+    w = hr.WORKLOADS["hex48_mixed"]
+    ctx = hr.Context(0)
+    try:
+        ctx.generate_synthetic(**w.synth())
+        ctx.build_bvh()
+        ctx.train_mlp(n_samples=2_000_000, steps=600, batch=4096, lr=2e-3, seed=1)
+        osc = oracle.OracleScene(scene_arrays_from_ctx(ctx))
+        cams, ws, hs, isos = hr.sphere_views(n_views=64, seed=7, shrink=8)
+        for mode in (hr.MODE_BATCHED, hr.MODE_LEARNED):
+            ctx.set_mode(mode)
+            for v in (5, 40):
+                rays = oracle.camera_rays(cams[v].lookfrom, cams[v].lookat, cams[v].vup, cams[v].vfov_deg, ws[v],
+                                          hs[v])
+                rays = np.ascontiguousarray(rays[:: max(1, rays.shape[0] // 3000)])
+                iso = isos[v][0]
+                h = ctx.intersect(rays, iso, True)
+                cnt = parity.check_against_oracle(h, rays, osc, iso, True, 1.0 / w.nx,
+                                                  product_trace=lambda r, iso=iso: ctx.intersect(r, iso, True),
+                                                  label=f"views64 scene, mode {mode}, view {v}, iso {iso}")
+                assert (h["kind"] > 0).sum() > 100 and cnt["rays"] == rays.shape[0]
+    finally:
+        ctx.close()

@@ -94,6 +94,7 @@ def test_render_and_views_shade_like_oracle(prim_scene, oracle):
     rays = oracle.camera_rays(CAM.lookfrom, CAM.lookat, CAM.vup, CAM.vfov_deg, W, H)
     ref = op.trace(rays, None, 32)
     same = (hits[0].reshape(-1)["kind"] == ref["kind"]) & (hits[0].reshape(-1)["elem"] == ref["elem"])
+    print("render vs oracle, primitives:", int((~same).sum()), "of", same.size, "differ")
     assert same.mean() >= 0.995
     want = oracle.shade(rays, ref).reshape(H, W, 3)
     diff = np.abs(rgb[0].astype(int) - want.astype(int)).max(axis=2)
