@@ -22,10 +22,13 @@
 // search after its 17 samples) are queued by the lane that finishes the
 // last task they depend on.
 //
-// Results equal the warp-per-ray kernel's: the same solves with the same
-// start points, iteration caps and acceptance rules, the same bracket (first
-// sign change in sample order) and the same face choice (per face the lowest
-// accepted seed index, faces compared in index order).
+// With cold starts (batched mode) the results equal the warp-per-ray
+// kernel's: the same solves with the same start points, iteration caps and
+// acceptance rules, the same bracket (first sign change in sample order) and
+// the same face choice (per face the lowest accepted seed index, faces
+// compared in index order). With network starts (learned mode) a failed warm
+// start restarts from whichever neighbouring sample has converged by then,
+// so the two kernels agree to the solvers' tolerance.
 #pragma once
 
 #include <cuda_fp16.h>
