@@ -43,30 +43,6 @@ constexpr double kCheckFaceTol = 1.5e-4;
 constexpr double kCheckIsoPosTol = 1e-4;
 constexpr double kCheckIsoFieldTol = 2e-5;
 
-// Modified-A basis values in FP64, the recurrence of basis_val.
-template <int N>
-__device__ __forceinline__ void basis_val64(double x, double (&a)[N]) {
-  a[0] = 0.5 * (1.0 - x);
-  if (N > 1) a[1] = 0.5 * (1.0 + x);
-  const double w = 0.25 * (1.0 - x * x);
-  double pm2 = 1.0, pm1 = 2.0 * x;
-#pragma unroll
-  for (int i = 2; i < N; ++i) {
-    const int m = i - 2;
-    double p;
-    if (m == 0) p = 1.0;
-    else if (m == 1) p = pm1;
-    else {
-      const double A = double((2 * m + 1) * (m + 1)) / double(m * (m + 2));
-      const double B = double(m + 1) / double(m + 2);
-      p = A * x * pm1 - B * pm2;
-      pm2 = pm1;
-      pm1 = p;
-    }
-    a[i] = w * p;
-  }
-}
-
 // Knuth's TwoSum: s + e == a + b exactly (round-to-nearest FP32; the
 // intrinsics keep the compiler from fusing or reordering the steps).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -107,6 +83,36 @@ __device__ __forceinline__ Ds ds_mul(Ds a, Ds b) {
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
   return ds_norm(p, e);
+}
+
+__device__ __forceinline__ Ds ds_sub(Ds a, Ds b) { return ds_add(a, {-b.hi, -b.lo}); }
+// times a power of two (exact)
+__device__ __forceinline__ Ds ds_scale2(Ds a, float s) { return {__fmul_rn(a.hi, s), __fmul_rn(a.lo, s)}; }
+
+// Modified-A basis values in double-single, the recurrence of basis_val
+// (the constants A_m, B_m rounded from FP64).
+template <int N>
+__device__ __forceinline__ void basis_val_ds(Ds x, Ds (&a)[N]) {
+  const Ds one = {1.f, 0.f};
+  a[0] = ds_scale2(ds_sub(one, x), 0.5f);
+  if (N > 1) a[1] = ds_scale2(ds_add(one, x), 0.5f);
+  const Ds w = ds_scale2(ds_sub(one, ds_mul(x, x)), 0.25f);
+  Ds pm2 = one, pm1 = ds_scale2(x, 2.f);
+#pragma unroll
+  for (int i = 2; i < N; ++i) {
+    const int m = i - 2;
+    Ds p;
+    if (m == 0) p = one;
+    else if (m == 1) p = pm1;
+    else {
+      const Ds A = ds_of(double((2 * m + 1) * (m + 1)) / double(m * (m + 2)));
+      const Ds B = ds_of(double(m + 1) / double(m + 2));
+      p = ds_sub(ds_mul(ds_mul(A, x), pm1), ds_mul(B, pm2));
+      pm2 = pm1;
+      pm1 = p;
+    }
+    a[i] = ds_mul(w, p);
+  }
 }
 
 // Value of one coefficient block (rows padded to row_stride(N), a multiple of
@@ -171,18 +177,15 @@ __device__ __noinline__ void fp64_residual_vec(const float* __restrict__ rec_all
                                                double t, double x0, double x1, double x2, bool want_field,
                                                double* __restrict__ r, double& u) {
   const float* rec = rec_all + static_cast<int64_t>(elem) * record_floats(N);
-  double ar[N], as[N], at[N];
-  basis_val64<N>(x0, ar);
-  basis_val64<N>(x1, as);
-  basis_val64<N>(x2, at);
-  float ah[N], al[N];  // ar as two floats
-  Ds sd[N], td[N];     // as, at double-single
+  Ds rd[N], sd[N], td[N];  // the basis values in r, s, t, double-single
+  basis_val_ds<N>(ds_of(x0), rd);
+  basis_val_ds<N>(ds_of(x1), sd);
+  basis_val_ds<N>(ds_of(x2), td);
+  float ah[N], al[N];  // the r values' two parts
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    ah[i] = static_cast<float>(ar[i]);
-    al[i] = static_cast<float>(ar[i] - static_cast<double>(ah[i]));
-    sd[i] = ds_of(as[i]);
-    td[i] = ds_of(at[i]);
+    ah[i] = rd[i].hi;
+    al[i] = rd[i].lo;
   }
   r[0] = value64<N>(rec, ah, al, sd, td) - (static_cast<double>(o.x) + t * d.x);
   r[1] = value64<N>(rec + block_floats(N), ah, al, sd, td) - (static_cast<double>(o.y) + t * d.y);
