@@ -371,7 +371,10 @@ int ho_set_mode(ho_context* ctx, int mode);
  *                     learned mode a failing hit is traced again by the plain
  *                     solver (HO_FLAG_FALLBACK) and flagged
  *                     HO_FLAG_FP64_FAIL if that fails too; in plain mode it
- *                     is flagged. 0: off (the solvers' own answers).
+ *                     is flagged. A hit that displaced another within 1e-4
+ *                     in t is weighed against it by the FP64 tie rule
+ *                     (HO_FLAG_TIE, ho_stats.fp64_ties). 0: off (the
+ *                     solvers' own answers).
  * HO_OPT_ROUND_CHUNK  pairs per element batch of the round kernel (1..4096;
  *                     default: the kernel's pair slots, 20 per warp up to 7
  *                     modes per direction, 12 at 8, 8 at 9, times 4 warps in
