@@ -276,7 +276,9 @@ def scaling_of(args):
 
 
 # ---- the CPU arm: FP32 oracle port on a bounded sample --------------------------
-CPU_BASELINE_QUERIES = 16384  # the GPU line's cpu_baseline entry (at most)
+# the GPU line's cpu_baseline entry (at most): the reference arm's sample size,
+# since a query's cost is heavy-tailed and smaller samples vary widely
+CPU_BASELINE_QUERIES = 65536
 
 
 def oracle_scene(w):
